@@ -6,5 +6,12 @@ Import with importlib (the directory name contains hyphens):
 
     import importlib
     cs = importlib.import_module("collocation-solver-cuda_gb300")
+    prob = cs.ocp.Problem.from_file("vdp.ocp")
+    sol = cs.solver.solve_single(prob, m=4)
+
+The GPU path needs libcs_gb300.so (built by build.py) and a CUDA device; there
+is no CPU fallback.
 """
-from . import tables, ocp, codegen, io  # noqa: F401
+from . import tables, ocp, codegen, io, _lib, module, solver, build  # noqa: F401
+from .ocp import Problem  # noqa: F401
+from .module import Batch, CompiledProblem, default_opts  # noqa: F401

@@ -192,11 +192,6 @@ def cuda_problem_source(pc):
     flat = [e for row in pc.Dr for e in row]
     out += _cuda_body(flat, ["Dr[%d]" % k for k in range(len(flat))], pr)
     out.append("}")
-    # structural nonzeros, usable in constant expressions by the kernels
-    out.append("static constexpr unsigned char CS_DF_NZ[%d] = {%s};" % (
-        max(1, ny * nc), ",".join(str(int(v)) for v in pc.Df_nz.ravel()) or "0"))
-    out.append("static constexpr unsigned char CS_DG_NZ[%d] = {%s};" % (
-        max(1, nz * nc), ",".join(str(int(v)) for v in pc.Dg_nz.ravel()) or "0"))
     return "\n".join(out) + "\n"
 
 

@@ -1,0 +1,991 @@
+// Collocation Newton-loop kernels for GB300 (sm_103a), FP64.
+//
+// This file is compiled at run time by NVRTC, once per (problem, m), after a
+// prelude that defines the sizes as compile-time constants and the problem
+// functions cs_f/cs_g/cs_Df/cs_Dg/cs_r/cs_Dr (emitted from the OCP's sympy
+// derivation), plus the collocation tables:
+//
+//   CS_NY, CS_NZ, CS_NP   sizes of y, z, p
+//   CS_NPE                parameters f and g depend on (leading entries of p)
+//   CS_NTH                instance constants
+//   CS_M                  Lobatto collocation points
+//   CS_A[M*M], CS_B[M], CS_C[M]                    Lobatto IIIA tableau
+//   CS_GW[M+1], CS_GL[(M+1)*M], CS_GI[(M+1)*M]     Gauss weights, basis L_k
+//                                                  and its integral I_k at the
+//                                                  (M+1) Gauss points
+//   CS_L0[M], CS_L1[M]    basis at t = 0 and t = 1
+//   CS_CGW                warps per condensation group (1: one warp per
+//                         interval, several intervals per CTA; >1: one CTA
+//                         per interval)
+//
+// Data layout in HBM (batch of B instances, packed by node):
+//   instance b owns node slots off[b] .. off[b]+N[b]-1; interval i of b uses
+//   slot off[b]+i (i < N[b]-1).  Per node: t, y[NY], dy[NY], z-at-node[NZ]
+//   (remesh scratch), segment residual.  Per interval slot: y'[M][NY],
+//   z~[M][NZ], their Newton steps, X = W^-1 [J | V_eff | f_a] stored
+//   column-major [NRHS][S], the level-0 BABD block row, the tree record of the
+//   node eliminated at that slot.
+//
+// Reference counterparts (UW-OCP/Collocation-Solver-CUDA):
+//   k_form_initial   form_initial_input_kernel        collocation_solver_parallel_2d_shared.py:316-356
+//   k_residual       collocation_update_kernel + compute_f_q_kernel1/2 + host
+//                    assembly and norm                 collocation_solver_parallel_2d_shared.py:399-559, 116
+//   k_condense       construct_jacobian_kernel + reduce_jacobian_parallel_kernel
+//                                                      collocation_solver_parallel_2d_shared.py:680-1001
+//   k_babd           partition_factorization_kernel, the host reduced solve,
+//                    partition_backward_substitution_kernel, recover_delta_k_kernel
+//                                                      solve_babd_system.py:161-572, collocation_solver_parallel_2d_shared.py:1619-1650
+//   k_decide/k_accept  Newton loop and line search    collocation_solver_parallel_2d_shared.py:105-180
+//   k_segres         compute_segment_residual_kernel   collocation_solver_parallel_2d_shared.py:1833-1892
+//   k_remesh_*       recover_solution_kernel + remesh  collocation_solver_parallel_2d_shared.py:2049-2311
+
+#define CS_S (CS_M * (CS_NY + CS_NZ))          // stage unknowns per interval
+#define CS_NRHS (CS_NY + CS_NPE + 1)           // right-hand sides of the condensation
+#define CS_NCOL (CS_S + CS_NRHS)               // augmented condensation matrix width
+#define CS_LDW (CS_NCOL | 1)                   // odd leading dimension in shared memory
+#define CS_ROWSZ (CS_NY * (2 * CS_NY + CS_NPE + 1))   // block row: A | C | H | b (column-major)
+#define CS_TREESZ (CS_NY * (3 * CS_NY + CS_NPE + 1))  // tree record: R | G | E | J | d
+#define CS_QC (3 * CS_NY + CS_NPE + 1)         // columns of a merge
+#define CS_QLD ((2 * CS_NY) | 1)               // leading dim (rows) of a merge, column-major
+#define CS_NT (2 * CS_NY + CS_NP)              // top system size
+#define CS_TLD (CS_NT | 1)
+#define CS_NFG (CS_NY + CS_NZ + CS_NP)         // columns of Df, Dg
+
+#define ST_FRESH 0
+#define ST_LS 1
+#define ST_SEG 2
+#define ST_DONE 3
+#define ST_FAIL 4
+#define ST_REMESH 5
+
+#define FAIL_NONE 0
+#define FAIL_ITER 1
+#define FAIL_NODES 2
+#define FAIL_MESH 3
+#define FAIL_NAN 4
+
+struct CsInst {
+  int status, it, ls_it, alphacal;
+  int need_jac, accepted, fail_reason, N_new;
+  int residual_count, jac_count, seg_count, remesh_count;
+  int iter_time, singular, pad0, pad1;
+  double alpha_ls, norm_x, alpha, max_res;
+  unsigned long long norm_bits, res_bits;
+};
+
+struct CsConsts {
+  double tol, alpha_m, beta;
+  int max_iter, max_mesh, max_nodes, min_nodes, max_ls;
+};
+
+struct CsBatch {
+  int B, T;                 // instances, node slots in use
+  const int* N;             // nodes per instance
+  const int* off;           // first node slot per instance
+  const int* inst_of;       // instance owning each slot
+  double* t;                // [T]
+  double* y;                // [T][NY]
+  double* ydot;             // [T][M][NY]
+  double* zt;               // [T][M][NZ]
+  double* p;                // [B][NP]
+  const double* th;         // [B][NTH]
+  double* dy;               // [T][NY]
+  double* dydot;            // [T][M][NY]
+  double* dzt;              // [T][M][NZ]
+  double* dp;               // [B][NP]
+  double* X;                // [T][NRHS][S]
+  double* rows0;            // [T][ROWSZ]
+  double* rows1;            // [T][ROWSZ]
+  double* tree;             // [T][TREESZ]
+  double* res;              // [T] segment residual per node
+  double* znode;            // [T][NZ] z at nodes (remesh / initial input)
+  CsInst* inst;             // [B]
+  int* counters;            // [8]
+  double* fa_out;           // optional [T][S]: residual pieces (stage entry point)
+  double* fb_out;           // optional [T][NY]
+};
+
+static constexpr double CS_EPS = 2.220446049250313e-16;
+
+__device__ __forceinline__ unsigned long long cs_abs_bits(double v) {
+  return (unsigned long long)__double_as_longlong(fabs(v));
+}
+__device__ __forceinline__ double cs_from_bits(unsigned long long b) { return __longlong_as_double((long long)b); }
+
+// Max of non-negative double bit patterns over the lanes of a warp that share
+// an instance, then one atomicMax per instance.  All 32 lanes must call it.
+__device__ __forceinline__ void cs_warp_max_atomic(unsigned long long* dst, int key, unsigned long long v, bool active) {
+  const unsigned peers = __match_any_sync(0xffffffffu, active ? key : -1);
+  const unsigned hi = (unsigned)(v >> 32), lo = (unsigned)(v & 0xffffffffull);
+  const unsigned mhi = __reduce_max_sync(peers, hi);
+  const unsigned mlo = __reduce_max_sync(peers, hi == mhi ? lo : 0u);
+  const int leader = __ffs(peers) - 1;
+  if (active && (int)(threadIdx.x & 31) == leader) atomicMax(dst, ((unsigned long long)mhi << 32) | mlo);
+}
+
+// ------------------------------------------------------------------------
+// Initial stage values on a (new) mesh: y~ = (1-c) y_i + c y_{i+1},
+// z~ likewise from z at nodes, y' = f(y~, z~, p).
+extern "C" __global__ void k_form_initial(CsBatch bt, int only_status) {
+  int slot = blockIdx.x * blockDim.x + threadIdx.x;
+  if (slot >= bt.T) return;
+  int b = bt.inst_of[slot];
+  int i = slot - bt.off[b];
+  if (i >= bt.N[b] - 1) return;
+  if (only_status >= 0 && bt.inst[b].status != only_status) return;
+  const double* p = bt.p + (size_t)b * CS_NP;
+  const double* th = bt.th + (size_t)b * (CS_NTH > 0 ? CS_NTH : 1);
+  double pl[CS_NP > 0 ? CS_NP : 1];
+  for (int k = 0; k < CS_NP; ++k) pl[k] = p[k];
+  const double* y0 = bt.y + (size_t)slot * CS_NY;
+  const double* y1 = y0 + CS_NY;
+  const double* z0 = bt.znode + (size_t)slot * CS_NZ;
+  const double* z1 = z0 + CS_NZ;
+#pragma unroll 1
+  for (int j = 0; j < CS_M; ++j) {
+    double c = CS_C[j];
+    double yt[CS_NY], ztl[CS_NZ > 0 ? CS_NZ : 1], f[CS_NY];
+    for (int k = 0; k < CS_NY; ++k) yt[k] = (1.0 - c) * y0[k] + c * y1[k];
+    for (int k = 0; k < CS_NZ; ++k) ztl[k] = (1.0 - c) * z0[k] + c * z1[k];
+    cs_f(yt, ztl, pl, th, f);
+    double* yd = bt.ydot + ((size_t)slot * CS_M + j) * CS_NY;
+    for (int k = 0; k < CS_NY; ++k) yd[k] = f[k];
+    double* zo = bt.zt + ((size_t)slot * CS_M + j) * CS_NZ;
+    for (int k = 0; k < CS_NZ; ++k) zo[k] = ztl[k];
+  }
+}
+
+// ------------------------------------------------------------------------
+// Residual infinity norm at the trial point x + alpha_ls * dx (LS) or x
+// (FRESH): collocation update, f_a = [f(y~,z~,p) - y'; g], f_b and, on
+// interval 0, the boundary conditions.
+extern "C" __global__ void k_residual(CsBatch bt) {
+  int slot = blockIdx.x * blockDim.x + threadIdx.x;
+  bool active = slot < bt.T;
+  int b = 0, i = 0;
+  if (active) {
+    b = bt.inst_of[slot];
+    i = slot - bt.off[b];
+    active = i < bt.N[b] - 1;
+  }
+  int st = active ? bt.inst[b].status : -1;
+  active = active && (st == ST_FRESH || st == ST_LS);
+  unsigned long long nb = 0;
+  if (active) {
+    const bool ls = (st == ST_LS);
+    const double a = ls ? bt.inst[b].alpha_ls : 0.0;
+    const double* th = bt.th + (size_t)b * (CS_NTH > 0 ? CS_NTH : 1);
+    double pl[CS_NP > 0 ? CS_NP : 1];
+    for (int k = 0; k < CS_NP; ++k) {
+      double v = bt.p[(size_t)b * CS_NP + k];
+      pl[k] = ls ? fma(a, bt.dp[(size_t)b * CS_NP + k], v) : v;
+    }
+    double yi[CS_NY], yi1[CS_NY];
+    for (int k = 0; k < CS_NY; ++k) {
+      double v0 = bt.y[(size_t)slot * CS_NY + k], v1 = bt.y[(size_t)(slot + 1) * CS_NY + k];
+      yi[k] = ls ? fma(a, bt.dy[(size_t)slot * CS_NY + k], v0) : v0;
+      yi1[k] = ls ? fma(a, bt.dy[(size_t)(slot + 1) * CS_NY + k], v1) : v1;
+    }
+    double yd[CS_M][CS_NY];
+    for (int j = 0; j < CS_M; ++j)
+      for (int k = 0; k < CS_NY; ++k) {
+        size_t q = ((size_t)slot * CS_M + j) * CS_NY + k;
+        yd[j][k] = ls ? fma(a, bt.dydot[q], bt.ydot[q]) : bt.ydot[q];
+      }
+    const double h = bt.t[slot + 1] - bt.t[slot];
+    double mx = 0.0;
+    bool nan = false;
+#pragma unroll 1
+    for (int j = 0; j < CS_M; ++j) {
+      double yt[CS_NY], zl[CS_NZ > 0 ? CS_NZ : 1], f[CS_NY];
+      for (int k = 0; k < CS_NY; ++k) {
+        double s = 0.0;
+        for (int q = 0; q < CS_M; ++q) s += CS_A[j * CS_M + q] * yd[q][k];
+        yt[k] = yi[k] + h * s;
+      }
+      for (int k = 0; k < CS_NZ; ++k) {
+        size_t q = ((size_t)slot * CS_M + j) * CS_NZ + k;
+        zl[k] = ls ? fma(a, bt.dzt[q], bt.zt[q]) : bt.zt[q];
+      }
+      cs_f(yt, zl, pl, th, f);
+      for (int k = 0; k < CS_NY; ++k) {
+        double r = f[k] - yd[j][k];
+        nan |= (r != r);
+        mx = fmax(mx, fabs(r));
+        if (bt.fa_out) bt.fa_out[(size_t)slot * CS_S + j * (CS_NY + CS_NZ) + k] = r;
+      }
+#if CS_NZ > 0
+      double g[CS_NZ];
+      cs_g(yt, zl, pl, th, bt.inst[b].alpha, g);
+      for (int k = 0; k < CS_NZ; ++k) {
+        nan |= (g[k] != g[k]);
+        mx = fmax(mx, fabs(g[k]));
+        if (bt.fa_out) bt.fa_out[(size_t)slot * CS_S + j * (CS_NY + CS_NZ) + CS_NY + k] = g[k];
+      }
+#endif
+    }
+    for (int k = 0; k < CS_NY; ++k) {
+      double s = 0.0;
+      for (int j = 0; j < CS_M; ++j) s += CS_B[j] * yd[j][k];
+      double r = yi1[k] - yi[k] - h * s;
+      nan |= (r != r);
+      mx = fmax(mx, fabs(r));
+      if (bt.fb_out) bt.fb_out[(size_t)slot * CS_NY + k] = r;
+    }
+    if (i == 0) {
+      int last = bt.off[b] + bt.N[b] - 1;
+      double ya[CS_NY], yb[CS_NY], r[CS_NY + CS_NP];
+      for (int k = 0; k < CS_NY; ++k) {
+        double v0 = bt.y[(size_t)slot * CS_NY + k], v1 = bt.y[(size_t)last * CS_NY + k];
+        ya[k] = ls ? fma(a, bt.dy[(size_t)slot * CS_NY + k], v0) : v0;
+        yb[k] = ls ? fma(a, bt.dy[(size_t)last * CS_NY + k], v1) : v1;
+      }
+      cs_r(ya, yb, pl, th, r);
+      for (int k = 0; k < CS_NY + CS_NP; ++k) {
+        nan |= (r[k] != r[k]);
+        mx = fmax(mx, fabs(r[k]));
+      }
+    }
+    nb = nan ? 0x7ff8000000000000ull : cs_abs_bits(mx);
+  }
+  cs_warp_max_atomic(active ? &bt.inst[b].norm_bits : nullptr, b, nb, active);
+}
+
+// ------------------------------------------------------------------------
+// Newton / line-search control, one thread per instance.
+__device__ void cs_post_newton(CsInst& s, int N, const CsConsts& c, int iter_time) {
+  s.need_jac = 0;
+  s.iter_time = iter_time;
+  if (s.alphacal >= c.max_iter - 1 || iter_time >= c.max_iter - 1) { s.status = ST_FAIL; s.fail_reason = FAIL_ITER; return; }
+  if (N > c.max_nodes || N < c.min_nodes) { s.status = ST_FAIL; s.fail_reason = FAIL_NODES; return; }
+  if (0 > c.max_mesh) { s.status = ST_FAIL; s.fail_reason = FAIL_MESH; return; }
+  s.status = ST_SEG;
+}
+
+// start of Newton iteration s.it, residual norm at x known (s.norm_x)
+__device__ void cs_iteration_start(CsInst& s, int N, const CsConsts& c, bool count_residual) {
+  if (s.it == c.max_iter) { cs_post_newton(s, N, c, c.max_iter - 1); return; }
+  if (count_residual) s.residual_count += 1;
+  if (s.norm_x < c.tol) { cs_post_newton(s, N, c, s.it); return; }
+  s.need_jac = 1;
+  s.it += 1;
+  s.jac_count += 1;
+}
+
+extern "C" __global__ void k_decide(CsBatch bt, CsConsts c) {
+  int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= bt.B) return;
+  CsInst s = bt.inst[b];
+  s.accepted = 0;
+  s.need_jac = 0;
+  if (s.status == ST_FRESH || s.status == ST_LS) {
+    double nt = cs_from_bits(s.norm_bits);
+    s.norm_bits = 0ull;
+    s.residual_count += 1;
+    if (s.status == ST_FRESH) {
+      s.norm_x = nt;
+      cs_iteration_start(s, bt.N[b], c, false);
+    } else if (nt < s.norm_x) {
+      s.accepted = 1;
+      s.norm_x = nt;
+      cs_iteration_start(s, bt.N[b], c, true);
+    } else {
+      s.ls_it += 1;
+      s.alpha_ls *= 0.5;
+      if (s.ls_it >= c.max_ls) cs_iteration_start(s, bt.N[b], c, true);
+    }
+    if (s.status == ST_FRESH || s.status == ST_LS || s.need_jac) atomicAdd(&bt.counters[0], 1);
+  }
+  bt.inst[b] = s;
+}
+
+// x += alpha_ls * dx for instances whose trial was accepted
+extern "C" __global__ void k_accept(CsBatch bt) {
+  int slot = blockIdx.x * blockDim.x + threadIdx.x;
+  if (slot >= bt.T) return;
+  int b = bt.inst_of[slot];
+  if (!bt.inst[b].accepted) return;
+  int i = slot - bt.off[b];
+  int N = bt.N[b];
+  double a = bt.inst[b].alpha_ls;
+  for (int k = 0; k < CS_NY; ++k) bt.y[(size_t)slot * CS_NY + k] = fma(a, bt.dy[(size_t)slot * CS_NY + k], bt.y[(size_t)slot * CS_NY + k]);
+  if (i >= N - 1) return;
+  for (int q = 0; q < CS_M * CS_NY; ++q) {
+    size_t o = (size_t)slot * CS_M * CS_NY + q;
+    bt.ydot[o] = fma(a, bt.dydot[o], bt.ydot[o]);
+  }
+  for (int q = 0; q < CS_M * CS_NZ; ++q) {
+    size_t o = (size_t)slot * CS_M * CS_NZ + q;
+    bt.zt[o] = fma(a, bt.dzt[o], bt.zt[o]);
+  }
+  if (i == 0)
+    for (int k = 0; k < CS_NP; ++k) bt.p[(size_t)b * CS_NP + k] = fma(a, bt.dp[(size_t)b * CS_NP + k], bt.p[(size_t)b * CS_NP + k]);
+}
+
+// ------------------------------------------------------------------------
+// Condensation: per interval, build [W | J | V_eff | f_a] in shared memory,
+// partial-pivot LU (pivot: largest |entry|, first one wins, as
+// matrix_factorization_cuda.py:133-146), back substitution, then
+//   A = -I + D X_J, H = D X_V, b = -f_b - D X_f  with D = h b_j I on y rows,
+// written as the level-0 block row [A | C=I | H | b]; X kept for recovery.
+template <int GW>
+struct CsGroup {
+  static constexpr int NT = 32 * GW;
+  __device__ static __forceinline__ int tid() { return GW == 1 ? (int)(threadIdx.x & 31) : (int)threadIdx.x; }
+  __device__ static __forceinline__ void sync() {
+    if (GW == 1) __syncwarp(); else __syncthreads();
+  }
+};
+
+template <int GW>
+__device__ void cs_condense_group(const CsBatch& bt, int slot, double* Wm, double* aux) {
+  typedef CsGroup<GW> G;
+  const int tid = G::tid();
+  const int b = bt.inst_of[slot];
+  const int i = slot - bt.off[b];
+  const double h = bt.t[slot + 1] - bt.t[slot];
+  const double* th = bt.th + (size_t)b * (CS_NTH > 0 ? CS_NTH : 1);
+  double* fb = aux;                       // [NY]
+  int* piv = (int*)(aux + CS_NY);         // [GW] partial argmax rows (GW > 1)
+  double* pvv = aux + CS_NY + GW;         // [GW] partial max values
+  // ---- build rows of stage j on thread j (stage Jacobians at y~_j)
+  for (int j = tid; j < CS_M; j += G::NT) {
+    double pl[CS_NP > 0 ? CS_NP : 1];
+    for (int k = 0; k < CS_NP; ++k) pl[k] = bt.p[(size_t)b * CS_NP + k];
+    const double* yi = bt.y + (size_t)slot * CS_NY;
+    const double* yd = bt.ydot + (size_t)slot * CS_M * CS_NY;
+    double yt[CS_NY], zl[CS_NZ > 0 ? CS_NZ : 1];
+    for (int k = 0; k < CS_NY; ++k) {
+      double s = 0.0;
+      for (int q = 0; q < CS_M; ++q) s += CS_A[j * CS_M + q] * yd[q * CS_NY + k];
+      yt[k] = yi[k] + h * s;
+    }
+    for (int k = 0; k < CS_NZ; ++k) zl[k] = bt.zt[((size_t)slot * CS_M + j) * CS_NZ + k];
+    double f[CS_NY];
+    double Df[CS_NY * CS_NFG];
+    cs_f(yt, zl, pl, th, f);
+    cs_Df(yt, zl, pl, th, Df);
+    for (int a = 0; a < CS_NY; ++a) {
+      double* row = Wm + (size_t)(j * (CS_NY + CS_NZ) + a) * CS_LDW;
+      for (int k = 0; k < CS_M; ++k) {
+        double hA = h * CS_A[j * CS_M + k];
+        for (int q = 0; q < CS_NY; ++q) row[k * (CS_NY + CS_NZ) + q] = hA * Df[a * CS_NFG + q] - ((k == j && q == a) ? 1.0 : 0.0);
+        for (int q = 0; q < CS_NZ; ++q) row[k * (CS_NY + CS_NZ) + CS_NY + q] = (k == j) ? Df[a * CS_NFG + CS_NY + q] : 0.0;
+      }
+      for (int q = 0; q < CS_NY; ++q) row[CS_S + q] = Df[a * CS_NFG + q];
+      for (int q = 0; q < CS_NPE; ++q) row[CS_S + CS_NY + q] = Df[a * CS_NFG + CS_NY + CS_NZ + q];
+      row[CS_S + CS_NY + CS_NPE] = f[a] - yd[j * CS_NY + a];
+    }
+#if CS_NZ > 0
+    double g[CS_NZ];
+    double Dg[CS_NZ * CS_NFG];
+    cs_g(yt, zl, pl, th, bt.inst[b].alpha, g);
+    cs_Dg(yt, zl, pl, th, bt.inst[b].alpha, Dg);
+    for (int a = 0; a < CS_NZ; ++a) {
+      double* row = Wm + (size_t)(j * (CS_NY + CS_NZ) + CS_NY + a) * CS_LDW;
+      for (int k = 0; k < CS_M; ++k) {
+        double hA = h * CS_A[j * CS_M + k];
+        for (int q = 0; q < CS_NY; ++q) row[k * (CS_NY + CS_NZ) + q] = hA * Dg[a * CS_NFG + q];
+        for (int q = 0; q < CS_NZ; ++q) row[k * (CS_NY + CS_NZ) + CS_NY + q] = (k == j) ? Dg[a * CS_NFG + CS_NY + q] : 0.0;
+      }
+      for (int q = 0; q < CS_NY; ++q) row[CS_S + q] = Dg[a * CS_NFG + q];
+      for (int q = 0; q < CS_NPE; ++q) row[CS_S + CS_NY + q] = Dg[a * CS_NFG + CS_NY + CS_NZ + q];
+      row[CS_S + CS_NY + CS_NPE] = g[a];
+    }
+#endif
+  }
+  if (tid == G::NT - 1 || (G::NT <= CS_M && tid == 0)) {
+    const double* yi = bt.y + (size_t)slot * CS_NY;
+    const double* yd = bt.ydot + (size_t)slot * CS_M * CS_NY;
+    for (int k = 0; k < CS_NY; ++k) {
+      double s = 0.0;
+      for (int j = 0; j < CS_M; ++j) s += CS_B[j] * yd[j * CS_NY + k];
+      fb[k] = yi[CS_NY + k] - yi[k] - h * s;
+    }
+  }
+  G::sync();
+  // ---- LU with partial pivoting on the augmented matrix
+  int singular = 0;
+#pragma unroll 1
+  for (int k = 0; k < CS_S; ++k) {
+    // pivot search over rows k..S-1 of column k (first maximum wins)
+    double best = -1.0;
+    int brow = k;
+    for (int r = k + tid; r < CS_S; r += G::NT) {
+      double v = fabs(Wm[(size_t)r * CS_LDW + k]);
+      if (v > best) { best = v; brow = r; }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      double ob = __shfl_xor_sync(0xffffffffu, best, o);
+      int orow = __shfl_xor_sync(0xffffffffu, brow, o);
+      if (ob > best || (ob == best && orow < brow)) { best = ob; brow = orow; }
+    }
+    if (GW > 1) {
+      if ((tid & 31) == 0) { pvv[tid >> 5] = best; piv[tid >> 5] = brow; }
+      __syncthreads();
+      best = pvv[0]; brow = piv[0];
+      for (int w = 1; w < GW; ++w) {
+        double ob = pvv[w];
+        int orow = piv[w];
+        if (ob > best || (ob == best && orow < brow)) { best = ob; brow = orow; }
+      }
+      __syncthreads();
+    }
+    if (brow != k) {
+      for (int c = tid; c < CS_NCOL; c += G::NT) {
+        double tmp = Wm[(size_t)k * CS_LDW + c];
+        Wm[(size_t)k * CS_LDW + c] = Wm[(size_t)brow * CS_LDW + c];
+        Wm[(size_t)brow * CS_LDW + c] = tmp;
+      }
+      G::sync();
+    }
+    const double pv = Wm[(size_t)k * CS_LDW + k];
+    if (fabs(pv) < 10.0 * CS_EPS) {
+      singular = 1;
+      G::sync();
+      continue;
+    }
+    const double inv = 1.0 / pv;
+    // multipliers
+    for (int r = k + 1 + tid; r < CS_S; r += G::NT) Wm[(size_t)r * CS_LDW + k] *= inv;
+    G::sync();
+    // trailing update, threads over columns
+    for (int c = k + 1 + tid; c < CS_NCOL; c += G::NT) {
+      const double ukc = Wm[(size_t)k * CS_LDW + c];
+      for (int r = k + 1; r < CS_S; ++r) Wm[(size_t)r * CS_LDW + c] = fma(-Wm[(size_t)r * CS_LDW + k], ukc, Wm[(size_t)r * CS_LDW + c]);
+    }
+    G::sync();
+  }
+  // ---- back substitution, threads over right-hand-side columns
+  for (int c = CS_S + tid; c < CS_NCOL; c += G::NT) {
+    for (int r = CS_S - 1; r >= 0; --r) {
+      double xr = Wm[(size_t)r * CS_LDW + c] / Wm[(size_t)r * CS_LDW + r];
+      Wm[(size_t)r * CS_LDW + c] = xr;
+      for (int q = 0; q < r; ++q) Wm[(size_t)q * CS_LDW + c] = fma(-Wm[(size_t)q * CS_LDW + r], xr, Wm[(size_t)q * CS_LDW + c]);
+    }
+  }
+  G::sync();
+  // ---- condensed block row and X
+  double* row = bt.rows0 + (size_t)slot * CS_ROWSZ;
+  double* X = bt.X + (size_t)slot * CS_NRHS * CS_S;
+  for (int c = tid; c < CS_NRHS; c += G::NT) {
+    const int col = CS_S + c;
+    for (int r = 0; r < CS_S; ++r) X[(size_t)c * CS_S + r] = Wm[(size_t)r * CS_LDW + col];
+    for (int a = 0; a < CS_NY; ++a) {
+      double s = 0.0;
+      for (int j = 0; j < CS_M; ++j) s += CS_B[j] * Wm[(size_t)(j * (CS_NY + CS_NZ) + a) * CS_LDW + col];
+      double dx = h * s;
+      if (c < CS_NY) {
+        row[c * CS_NY + a] = dx - (a == c ? 1.0 : 0.0);                 // A column c
+        row[(CS_NY + c) * CS_NY + a] = (a == c ? 1.0 : 0.0);             // C = I column c
+      } else if (c < CS_NY + CS_NPE) {
+        row[(2 * CS_NY + (c - CS_NY)) * CS_NY + a] = dx;                 // H
+      } else {
+        row[(2 * CS_NY + CS_NPE) * CS_NY + a] = -fb[a] - dx;             // b
+      }
+    }
+  }
+  if (singular && tid == 0) atomicAdd(&bt.inst[b].singular, 1);
+  (void)i;
+}
+
+template <int GW>
+__device__ __forceinline__ void cs_condense_entry(const CsBatch& bt) {
+  extern __shared__ double smem[];
+  const int per = CS_S * CS_LDW + CS_NY + 2 * GW + 2;
+  if (GW == 1) {
+    const int w = threadIdx.x >> 5;
+    const int slot = blockIdx.x * (blockDim.x >> 5) + w;
+    if (slot >= bt.T) return;
+    const int b = bt.inst_of[slot];
+    if (slot - bt.off[b] >= bt.N[b] - 1 || !bt.inst[b].need_jac) return;
+    double* Wm = smem + (size_t)w * per;
+    cs_condense_group<1>(bt, slot, Wm, Wm + CS_S * CS_LDW);
+  } else {
+    const int slot = blockIdx.x;
+    if (slot >= bt.T) return;
+    const int b = bt.inst_of[slot];
+    if (slot - bt.off[b] >= bt.N[b] - 1 || !bt.inst[b].need_jac) return;
+    cs_condense_group<GW>(bt, slot, smem, smem + CS_S * CS_LDW);
+  }
+}
+
+extern "C" __global__ void k_condense(CsBatch bt) { cs_condense_entry<CS_CGW>(bt); }
+
+// ------------------------------------------------------------------------
+// BABD solve, one CTA per instance: tree of pairwise QR eliminations over
+// the block rows (row k couples y_left, y_right), the dense top system with
+// the boundary conditions, back substitution down the tree, recovery of the
+// stage steps.
+//
+// Merge of rows a (y_l, y_m) and b (y_m, y_r):
+//   [C_a; A_b] = Q [R; 0];  Q^T [A_a | 0 ; 0 | C_b ; H_a H_b ; b_a b_b]
+//   top rows    -> tree record at node m: R y_m + G y_l + E y_r + J p = d
+//   bottom rows -> new row:  At y_l + Ct y_r + Ht p = bt
+// Householder sign rule as matrix_factorization_cuda.py:37-54.
+
+// column-major merge matrix Q[col * CS_QLD + row], rows 0..2NY-1
+__device__ void cs_merge_warp(const double* ra, const double* rb, double* out_row, double* rec, double* Q) {
+  const int lane = threadIdx.x & 31;
+  // load: col 0..NY-1: [C_a; A_b]; NY..2NY-1: [A_a; 0]; 2NY..3NY-1: [0; C_b]; H; b
+  for (int c = lane; c < CS_QC; c += 32) {
+    double* col = Q + (size_t)c * CS_QLD;
+    for (int r = 0; r < CS_NY; ++r) {
+      double top, bot;
+      if (c < CS_NY) { top = ra[(CS_NY + c) * CS_NY + r]; bot = rb[c * CS_NY + r]; }
+      else if (c < 2 * CS_NY) { top = ra[(c - CS_NY) * CS_NY + r]; bot = 0.0; }
+      else if (c < 3 * CS_NY) { top = 0.0; bot = rb[(CS_NY + c - 2 * CS_NY) * CS_NY + r]; }
+      else if (c < 3 * CS_NY + CS_NPE) { top = ra[(2 * CS_NY + c - 3 * CS_NY) * CS_NY + r]; bot = rb[(2 * CS_NY + c - 3 * CS_NY) * CS_NY + r]; }
+      else { top = ra[(2 * CS_NY + CS_NPE) * CS_NY + r]; bot = rb[(2 * CS_NY + CS_NPE) * CS_NY + r]; }
+      col[r] = top;
+      col[CS_NY + r] = bot;
+    }
+  }
+  __syncwarp();
+#pragma unroll 1
+  for (int k = 0; k < CS_NY; ++k) {
+    const double* vk = Q + (size_t)k * CS_QLD;
+    double ss = 0.0;
+    for (int r = k + lane; r < 2 * CS_NY; r += 32) ss += vk[r] * vk[r];
+    for (int o = 16; o > 0; o >>= 1) ss += __shfl_xor_sync(0xffffffffu, ss, o);
+    const double x0 = vk[k];
+    const double sgn = (x0 >= 0.0) ? 1.0 : -1.0;
+    const double g = -sgn * sqrt(ss);
+    const double v0 = x0 - g;
+    const double vs = ss - x0 * x0 + v0 * v0;
+    __syncwarp();
+    if (vs < CS_EPS) continue;  // nothing to eliminate in this column
+    const double beta = -2.0 / vs;
+    for (int c = k + 1 + lane; c < CS_QC; c += 32) {
+      double* col = Q + (size_t)c * CS_QLD;
+      double w = v0 * col[k];
+      for (int r = k + 1; r < 2 * CS_NY; ++r) w += vk[r] * col[r];
+      const double bw = beta * w;
+      col[k] = fma(bw, v0, col[k]);
+      for (int r = k + 1; r < 2 * CS_NY; ++r) col[r] = fma(bw, vk[r], col[r]);
+    }
+    __syncwarp();
+    if (lane == 0) {
+      double* col = Q + (size_t)k * CS_QLD;
+      col[k] = g;
+      for (int r = k + 1; r < 2 * CS_NY; ++r) col[r] = 0.0;
+    }
+    __syncwarp();
+  }
+  // outputs
+  for (int c = lane; c < CS_QC; c += 32) {
+    const double* col = Q + (size_t)c * CS_QLD;
+    for (int r = 0; r < CS_NY; ++r) rec[(size_t)c * CS_NY + r] = col[r];
+    if (c >= CS_NY) {
+      // new row: At (from A_a cols), Ct (from C_b cols), Ht, bt
+      for (int r = 0; r < CS_NY; ++r) out_row[(size_t)(c - CS_NY) * CS_NY + r] = col[CS_NY + r];
+    }
+  }
+  __syncwarp();
+}
+
+// y_m = R^-1 (d - G y_l - E y_r - J p), one warp, lanes over rows
+__device__ void cs_backsub_warp(const double* rec, const double* yl, const double* yr, const double* dpv, double* ym) {
+  const int lane = threadIdx.x & 31;
+  double rhs[(CS_NY + 31) / 32];
+  for (int q = 0; q < (CS_NY + 31) / 32; ++q) {
+    int a = lane + 32 * q;
+    double v = 0.0;
+    if (a < CS_NY) {
+      v = rec[(size_t)(3 * CS_NY + CS_NPE) * CS_NY + a];
+      for (int c = 0; c < CS_NY; ++c) v -= rec[(size_t)(CS_NY + c) * CS_NY + a] * yl[c];
+      for (int c = 0; c < CS_NY; ++c) v -= rec[(size_t)(2 * CS_NY + c) * CS_NY + a] * yr[c];
+      for (int c = 0; c < CS_NPE; ++c) v -= rec[(size_t)(3 * CS_NY + c) * CS_NY + a] * dpv[c];
+    }
+    rhs[q] = v;
+  }
+  for (int r = CS_NY - 1; r >= 0; --r) {
+    const int owner = r & 31, qq = r >> 5;
+    double xr = 0.0;
+    for (int q = 0; q < (CS_NY + 31) / 32; ++q)
+      if (q == qq) xr = __shfl_sync(0xffffffffu, rhs[q], owner);
+    const double rr = rec[(size_t)r * CS_NY + r];
+    xr = (rr != 0.0) ? xr / rr : 0.0;
+    if (lane == owner) {
+      for (int q = 0; q < (CS_NY + 31) / 32; ++q)
+        if (q == qq) rhs[q] = xr;
+      ym[r] = xr;
+    }
+    for (int q = 0; q < (CS_NY + 31) / 32; ++q) {
+      int a = lane + 32 * q;
+      if (a < r) rhs[q] -= rec[(size_t)r * CS_NY + a] * xr;
+    }
+  }
+  __syncwarp();
+}
+
+extern "C" __global__ void k_babd(CsBatch bt) {
+  extern __shared__ double smem[];
+  const int b = blockIdx.x;
+  if (b >= bt.B) return;
+  if (!bt.inst[b].need_jac) return;
+  const int nw = blockDim.x >> 5;
+  const int w = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31;
+  const int N = bt.N[b];
+  const int off = bt.off[b];
+  const int n0 = N - 1;  // block rows at level 0
+  double* Qw = smem + (size_t)w * CS_QLD * CS_QC;
+  double* top = smem + (size_t)nw * CS_QLD * CS_QC;   // CS_NT x (CS_NT+1), column-major, ld CS_TLD
+  double* dpv = top + (size_t)CS_TLD * (CS_NT + 1);    // [NP]
+  // ---- tree reduction
+  double* src = bt.rows0 + (size_t)off * CS_ROWSZ;
+  double* dst = bt.rows1 + (size_t)off * CS_ROWSZ;
+  int n = n0, stride = 1, levels = 0;
+  while (n > 1) {
+    const int merges = n >> 1;
+    for (int mi = w; mi < merges; mi += nw) {
+      const int mid = (2 * mi + 1) * stride;
+      cs_merge_warp(src + (size_t)(2 * mi) * CS_ROWSZ, src + (size_t)(2 * mi + 1) * CS_ROWSZ,
+                    dst + (size_t)mi * CS_ROWSZ, bt.tree + (size_t)(off + mid) * CS_TREESZ, Qw);
+    }
+    if (n & 1) {
+      const double* s = src + (size_t)(n - 1) * CS_ROWSZ;
+      double* d = dst + (size_t)merges * CS_ROWSZ;
+      for (int q = threadIdx.x; q < CS_ROWSZ; q += blockDim.x) d[q] = s[q];
+    }
+    __syncthreads();
+    double* tmp = src; src = dst; dst = tmp;
+    n = (n + 1) >> 1;
+    stride <<= 1;
+    levels += 1;
+  }
+  // ---- top system: [At Ct Ht 0; B0 Bn Vn] [y0; yN; p] = [bt; -r]
+  if (w == 0) {
+    const double* row = src;  // the single remaining block row
+    for (int c = lane; c < CS_NT + 1; c += 32) {
+      double* col = top + (size_t)c * CS_TLD;
+      for (int r = 0; r < CS_NY; ++r) {
+        double v;
+        if (c < CS_NY) v = row[c * CS_NY + r];
+        else if (c < 2 * CS_NY) v = row[c * CS_NY + r];
+        else if (c < 2 * CS_NY + CS_NPE) v = row[c * CS_NY + r];
+        else if (c < CS_NT) v = 0.0;
+        else v = row[(2 * CS_NY + CS_NPE) * CS_NY + r];
+        col[r] = v;
+      }
+    }
+    if (lane == 0) {
+      const double* th = bt.th + (size_t)b * (CS_NTH > 0 ? CS_NTH : 1);
+      double ya[CS_NY], yb[CS_NY], pl[CS_NP > 0 ? CS_NP : 1], r[CS_NY + CS_NP];
+      double Dr[(CS_NY + CS_NP) * (2 * CS_NY + CS_NP)];
+      for (int k = 0; k < CS_NY; ++k) { ya[k] = bt.y[(size_t)off * CS_NY + k]; yb[k] = bt.y[(size_t)(off + N - 1) * CS_NY + k]; }
+      for (int k = 0; k < CS_NP; ++k) pl[k] = bt.p[(size_t)b * CS_NP + k];
+      cs_r(ya, yb, pl, th, r);
+      cs_Dr(ya, yb, pl, th, Dr);
+      for (int q = 0; q < CS_NY + CS_NP; ++q) {
+        for (int c = 0; c < CS_NY; ++c) top[(size_t)c * CS_TLD + CS_NY + q] = Dr[q * (2 * CS_NY + CS_NP) + c];            // B_0
+        for (int c = 0; c < CS_NY; ++c) top[(size_t)(CS_NY + c) * CS_TLD + CS_NY + q] = Dr[q * (2 * CS_NY + CS_NP) + CS_NY + c];  // B_n
+        for (int c = 0; c < CS_NP; ++c) top[(size_t)(2 * CS_NY + c) * CS_TLD + CS_NY + q] = Dr[q * (2 * CS_NY + CS_NP) + 2 * CS_NY + c];
+        top[(size_t)CS_NT * CS_TLD + CS_NY + q] = -r[q];
+      }
+    }
+    __syncwarp();
+    // Householder QR of the NT x NT system with its right-hand side
+#pragma unroll 1
+    for (int k = 0; k < CS_NT; ++k) {
+      const double* vk = top + (size_t)k * CS_TLD;
+      double ss = 0.0;
+      for (int r = k + lane; r < CS_NT; r += 32) ss += vk[r] * vk[r];
+      for (int o = 16; o > 0; o >>= 1) ss += __shfl_xor_sync(0xffffffffu, ss, o);
+      const double x0 = vk[k];
+      const double sgn = (x0 >= 0.0) ? 1.0 : -1.0;
+      const double g = -sgn * sqrt(ss);
+      const double v0 = x0 - g;
+      const double vs = ss - x0 * x0 + v0 * v0;
+      __syncwarp();
+      if (vs < CS_EPS) continue;
+      const double beta = -2.0 / vs;
+      for (int c = k + 1 + lane; c < CS_NT + 1; c += 32) {
+        double* col = top + (size_t)c * CS_TLD;
+        double wv = v0 * col[k];
+        for (int r = k + 1; r < CS_NT; ++r) wv += vk[r] * col[r];
+        const double bw = beta * wv;
+        col[k] = fma(bw, v0, col[k]);
+        for (int r = k + 1; r < CS_NT; ++r) col[r] = fma(bw, vk[r], col[r]);
+      }
+      __syncwarp();
+      if (lane == 0) {
+        double* col = top + (size_t)k * CS_TLD;
+        col[k] = g;
+        for (int r = k + 1; r < CS_NT; ++r) col[r] = 0.0;
+      }
+      __syncwarp();
+    }
+    if (lane == 0) {
+      double* rhs = top + (size_t)CS_NT * CS_TLD;
+      bool sing = false;
+      for (int r = CS_NT - 1; r >= 0; --r) {
+        double v = rhs[r];
+        for (int c = r + 1; c < CS_NT; ++c) v -= top[(size_t)c * CS_TLD + r] * rhs[c];
+        double d = top[(size_t)r * CS_TLD + r];
+        if (d == 0.0) sing = true;
+        rhs[r] = (d != 0.0) ? v / d : 0.0;
+      }
+      if (sing) {
+        for (int r = 0; r < CS_NT; ++r) rhs[r] = 0.0;
+        bt.inst[b].singular += 1;
+      }
+      for (int k = 0; k < CS_NY; ++k) {
+        bt.dy[(size_t)off * CS_NY + k] = rhs[k];
+        bt.dy[(size_t)(off + N - 1) * CS_NY + k] = rhs[CS_NY + k];
+      }
+      for (int k = 0; k < CS_NP; ++k) { dpv[k] = rhs[2 * CS_NY + k]; bt.dp[(size_t)b * CS_NP + k] = rhs[2 * CS_NY + k]; }
+    }
+  }
+  __syncthreads();
+  // ---- back substitution down the tree
+  for (int l = levels - 1; l >= 0; --l) {
+    int nl = n0;
+    for (int q = 0; q < l; ++q) nl = (nl + 1) >> 1;
+    const int st = 1 << l;
+    const int merges = nl >> 1;
+    for (int mi = w; mi < merges; mi += nw) {
+      const int mid = (2 * mi + 1) * st;
+      const int left = 2 * mi * st;
+      int right = (2 * mi + 2) * st;
+      if (right > n0) right = n0;
+      cs_backsub_warp(bt.tree + (size_t)(off + mid) * CS_TREESZ, bt.dy + (size_t)(off + left) * CS_NY,
+                      bt.dy + (size_t)(off + right) * CS_NY, dpv, bt.dy + (size_t)(off + mid) * CS_NY);
+    }
+    __syncthreads();
+  }
+  // ---- recovery: dk = -(X_f + X_J dy_i + X_V dp), lanes over stage rows
+  for (int iv = w; iv < n0; iv += nw) {
+    const int slot = off + iv;
+    const double* X = bt.X + (size_t)slot * CS_NRHS * CS_S;
+    const double* dyi = bt.dy + (size_t)slot * CS_NY;
+    for (int r = lane; r < CS_S; r += 32) {
+      double v = X[(size_t)(CS_NY + CS_NPE) * CS_S + r];
+      for (int q = 0; q < CS_NY; ++q) v = fma(X[(size_t)q * CS_S + r], dyi[q], v);
+      for (int q = 0; q < CS_NPE; ++q) v = fma(X[(size_t)(CS_NY + q) * CS_S + r], dpv[q], v);
+      const int j = r / (CS_NY + CS_NZ), a = r % (CS_NY + CS_NZ);
+      if (a < CS_NY) bt.dydot[((size_t)slot * CS_M + j) * CS_NY + a] = -v;
+      else bt.dzt[((size_t)slot * CS_M + j) * CS_NZ + (a - CS_NY)] = -v;
+    }
+  }
+  if (threadIdx.x == 0) {
+    bt.inst[b].status = ST_LS;
+    bt.inst[b].alpha_ls = 1.0;
+    bt.inst[b].ls_it = 0;
+  }
+}
+
+// ------------------------------------------------------------------------
+// Segment residual at the M+1 Gauss points (residual_type 1, with the running
+// sum multiplied by h after each component, as the reference does), and
+// |r|_inf / tol in the last node's slot.
+extern "C" __global__ void k_segres(CsBatch bt, double tol) {
+  int slot = blockIdx.x * blockDim.x + threadIdx.x;
+  if (slot >= bt.T) return;
+  int b = bt.inst_of[slot];
+  int i = slot - bt.off[b];
+  int N = bt.N[b];
+  if (bt.inst[b].status != ST_SEG) return;
+  const double* th = bt.th + (size_t)b * (CS_NTH > 0 ? CS_NTH : 1);
+  double pl[CS_NP > 0 ? CS_NP : 1];
+  for (int k = 0; k < CS_NP; ++k) pl[k] = bt.p[(size_t)b * CS_NP + k];
+  double val;
+  if (i < N - 1) {
+    const double h = bt.t[slot + 1] - bt.t[slot];
+    const double* yi = bt.y + (size_t)slot * CS_NY;
+    const double* yd = bt.ydot + (size_t)slot * CS_M * CS_NY;
+    const double* zz = bt.zt + (size_t)slot * CS_M * CS_NZ;
+    double rho_h = 0.0, rho_g = 0.0;
+#pragma unroll 1
+    for (int gi = 0; gi < CS_M + 1; ++gi) {
+      double yv[CS_NY], ydv[CS_NY], zv[CS_NZ > 0 ? CS_NZ : 1], f[CS_NY];
+      for (int k = 0; k < CS_NY; ++k) {
+        double sl = 0.0, si = 0.0;
+        for (int q = 0; q < CS_M; ++q) {
+          sl += CS_GL[gi * CS_M + q] * yd[q * CS_NY + k];
+          si += CS_GI[gi * CS_M + q] * yd[q * CS_NY + k];
+        }
+        ydv[k] = sl;
+        yv[k] = yi[k] + h * si;
+      }
+      for (int k = 0; k < CS_NZ; ++k) {
+        double sl = 0.0;
+        for (int q = 0; q < CS_M; ++q) sl += CS_GL[gi * CS_M + q] * zz[q * CS_NZ + k];
+        zv[k] = sl;
+      }
+      cs_f(yv, zv, pl, th, f);
+      const double wgt = CS_GW[gi];
+      for (int k = 0; k < CS_NY; ++k) {
+        rho_h += wgt * fabs(f[k] - ydv[k]);
+        rho_h *= h;
+      }
+#if CS_NZ > 0
+      double g[CS_NZ];
+      cs_g(yv, zv, pl, th, bt.inst[b].alpha, g);
+      for (int k = 0; k < CS_NZ; ++k) {
+        rho_g += wgt * fabs(g[k]);
+        rho_g *= h;
+      }
+#endif
+    }
+    val = (fabs(rho_h) + fabs(rho_g)) / tol;
+  } else {
+    double ya[CS_NY], yb[CS_NY], r[CS_NY + CS_NP];
+    const int first = bt.off[b];
+    for (int k = 0; k < CS_NY; ++k) { ya[k] = bt.y[(size_t)first * CS_NY + k]; yb[k] = bt.y[(size_t)slot * CS_NY + k]; }
+    cs_r(ya, yb, pl, th, r);
+    double mx = 0.0;
+    for (int k = 0; k < CS_NY + CS_NP; ++k) mx = fmax(mx, fabs(r[k]));
+    val = mx / tol;
+  }
+  bt.res[slot] = val;
+  unsigned long long bits = (val != val) ? 0x7ff8000000000000ull : cs_abs_bits(val);
+  atomicMax(&bt.inst[b].res_bits, bits);
+}
+
+// after k_segres: accept the mesh, continue the continuation, or ask for a remesh
+extern "C" __global__ void k_mesh_decide(CsBatch bt, CsConsts c) {
+  int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= bt.B) return;
+  CsInst s = bt.inst[b];
+  if (s.status != ST_SEG) return;
+  s.max_res = cs_from_bits(s.res_bits);
+  s.res_bits = 0ull;
+  s.seg_count += 1;
+  if (s.max_res > 1.0) {
+    s.status = ST_REMESH;
+  } else if (s.alpha <= c.alpha_m) {
+    s.status = ST_DONE;
+  } else {
+    s.alpha *= c.beta;
+    s.alphacal += 1;
+    s.status = ST_FRESH;
+    s.it = 0;
+  }
+  bt.inst[b].max_res = s.max_res;
+  bt.inst[b] = s;
+}
+
+// ------------------------------------------------------------------------
+// Remesh (collocation_solver_parallel_2d_shared.py:2106-2311), one thread per
+// instance.  Pass 1 counts the new nodes; pass 2 writes t, y and z-at-node
+// into the new packed arrays.  Deletion: five consecutive residuals <= 1e-2
+// keep the 1st, 3rd and 5th node; insertion: residual > 10 adds three
+// equispaced nodes, > 1 the midpoint; y and z are interpolated linearly.
+__device__ __forceinline__ void cs_znode(const CsBatch& bt, int off, int N, int i, double* z) {
+  if (i < N - 1) {
+    const double* zz = bt.zt + (size_t)(off + i) * CS_M * CS_NZ;
+    for (int k = 0; k < CS_NZ; ++k) {
+      double s = 0.0;
+      for (int q = 0; q < CS_M; ++q) s += CS_L0[q] * zz[q * CS_NZ + k];
+      z[k] = s;
+    }
+  } else {
+    const double* zz = bt.zt + (size_t)(off + N - 2) * CS_M * CS_NZ;
+    for (int k = 0; k < CS_NZ; ++k) {
+      double s = 0.0;
+      for (int q = 0; q < CS_M; ++q) s += CS_L1[q] * zz[q * CS_NZ + k];
+      z[k] = s;
+    }
+  }
+}
+
+// iterate the nodes kept by the deletion pass; calls fn(kept_index)
+template <typename F>
+__device__ void cs_kept_nodes(const double* res, int N, F fn) {
+  int i = 0;
+  while (i < N - 4) {
+    if (res[i] <= 1e-2 && res[i + 1] <= 1e-2 && res[i + 2] <= 1e-2 && res[i + 3] <= 1e-2 && res[i + 4] <= 1e-2) {
+      fn(i); fn(i + 2); fn(i + 4);
+      i += 5;
+    } else {
+      fn(i);
+      i += 1;
+    }
+  }
+  while (i < N) { fn(i); i += 1; }
+}
+
+extern "C" __global__ void k_remesh_count(CsBatch bt) {
+  int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= bt.B) return;
+  if (bt.inst[b].status != ST_REMESH) { bt.inst[b].N_new = bt.N[b]; return; }
+  const int N = bt.N[b];
+  const double* res = bt.res + bt.off[b];
+  int cnt = 0, prev = -1;
+  cs_kept_nodes(res, N, [&](int k) {
+    if (prev >= 0) {
+      double r = res[prev];
+      cnt += (r > 10.0) ? 4 : (r > 1.0 ? 2 : 1);
+    }
+    prev = k;
+  });
+  bt.inst[b].N_new = cnt + 1;
+}
+
+// new arrays: t2, y2, z2 (z at nodes) at offsets off2
+extern "C" __global__ void k_remesh_write(CsBatch bt, const int* off2, double* t2, double* y2, double* z2) {
+  int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= bt.B) return;
+  if (bt.inst[b].status != ST_REMESH) return;
+  const int N = bt.N[b], off = bt.off[b];
+  const double* res = bt.res + off;
+  int o = off2[b];
+  int prev = -1;
+  auto emit = [&](int a, int bnode, int q) {
+    // node a itself, then q-1 interpolated nodes towards bnode
+    double za[CS_NZ > 0 ? CS_NZ : 1], zb[CS_NZ > 0 ? CS_NZ : 1];
+    cs_znode(bt, off, N, a, za);
+    cs_znode(bt, off, N, bnode, zb);
+    const double ta = bt.t[off + a], tb = bt.t[off + bnode];
+    const double dt = (tb - ta) / (double)q;
+    t2[o] = ta;
+    for (int k = 0; k < CS_NY; ++k) y2[(size_t)o * CS_NY + k] = bt.y[(size_t)(off + a) * CS_NY + k];
+    for (int k = 0; k < CS_NZ; ++k) z2[(size_t)o * CS_NZ + k] = za[k];
+    ++o;
+    for (int s = 1; s < q; ++s) {
+      t2[o] = __dadd_rn(ta, __dmul_rn((double)s, dt));
+      for (int k = 0; k < CS_NY; ++k) {
+        const double ya = bt.y[(size_t)(off + a) * CS_NY + k], yb = bt.y[(size_t)(off + bnode) * CS_NY + k];
+        y2[(size_t)o * CS_NY + k] = __dadd_rn(ya, __dmul_rn((double)s, (yb - ya) / (double)q));
+      }
+      for (int k = 0; k < CS_NZ; ++k) z2[(size_t)o * CS_NZ + k] = __dadd_rn(za[k], __dmul_rn((double)s, (zb[k] - za[k]) / (double)q));
+      ++o;
+    }
+  };
+  cs_kept_nodes(res, N, [&](int k) {
+    if (prev >= 0) {
+      double r = res[prev];
+      emit(prev, k, (r > 10.0) ? 4 : (r > 1.0 ? 2 : 1));
+    }
+    prev = k;
+  });
+  emit(prev, prev, 1);
+}
+
+// copy an unchanged instance into the new packed layout
+extern "C" __global__ void k_repack(CsBatch bt, const int* off2, double* t2, double* y2, double* ydot2, double* zt2) {
+  int slot = blockIdx.x * blockDim.x + threadIdx.x;
+  if (slot >= bt.T) return;
+  int b = bt.inst_of[slot];
+  if (bt.inst[b].status == ST_REMESH) return;
+  int i = slot - bt.off[b];
+  int d = off2[b] + i;
+  t2[d] = bt.t[slot];
+  for (int k = 0; k < CS_NY; ++k) y2[(size_t)d * CS_NY + k] = bt.y[(size_t)slot * CS_NY + k];
+  if (i < bt.N[b] - 1) {
+    for (int q = 0; q < CS_M * CS_NY; ++q) ydot2[(size_t)d * CS_M * CS_NY + q] = bt.ydot[(size_t)slot * CS_M * CS_NY + q];
+    for (int q = 0; q < CS_M * CS_NZ; ++q) zt2[(size_t)d * CS_M * CS_NZ + q] = bt.zt[(size_t)slot * CS_M * CS_NZ + q];
+  }
+}
+
+// z at every node (output / diagnostics)
+extern "C" __global__ void k_znodes(CsBatch bt) {
+  int slot = blockIdx.x * blockDim.x + threadIdx.x;
+  if (slot >= bt.T) return;
+  int b = bt.inst_of[slot];
+  double z[CS_NZ > 0 ? CS_NZ : 1];
+  cs_znode(bt, bt.off[b], bt.N[b], slot - bt.off[b], z);
+  for (int k = 0; k < CS_NZ; ++k) bt.znode[(size_t)slot * CS_NZ + k] = z[k];
+}

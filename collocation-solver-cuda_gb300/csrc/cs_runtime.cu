@@ -1,0 +1,1076 @@
+// Host runtime of the GB300 collocation solver: run-time compilation of the
+// problem-specialised kernels (NVRTC, sm_103a, cached cubins), the batch
+// workspace in HBM, the solve driver and the C ABI declared in cs_gb300.h.
+//
+// The driver follows collocation_solver_parallel (collocation_solver_parallel_2d_shared.py:36-251)
+// but keeps the whole Newton loop on the device: each "super-step" launches
+//   k_residual -> k_decide -> k_accept -> k_condense -> k_babd
+// and every instance advances its own state machine (fresh residual, line
+// search trial, converged, failed) inside those kernels.  The host only
+// checks, every few super-steps, whether any instance is still in Newton, and
+// runs the mesh phase (segment residual, remesh with repacking) between
+// Newton phases.
+#include <cuda.h>
+#include <cuda_runtime.h>
+#include <nvrtc.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <mutex>
+#include <sstream>
+#include <string>
+#include <sys/stat.h>
+#include <unistd.h>
+#include <vector>
+
+#include "cs_gb300.h"
+#include "cs_kernels_src.h"  // generated: const char* cs_kernels_source
+
+namespace {
+
+thread_local std::string g_err;
+
+int set_err(int code, const std::string& msg) {
+  g_err = msg;
+  return code;
+}
+
+#define CS_CUDA(call)                                                                            \
+  do {                                                                                           \
+    cudaError_t e_ = (call);                                                                     \
+    if (e_ != cudaSuccess)                                                                       \
+      return set_err(e_ == cudaErrorMemoryAllocation ? CS_ERR_NOMEM : CS_ERR_CUDA,               \
+                     std::string(#call) + ": " + cudaGetErrorString(e_));                        \
+  } while (0)
+
+// Driver API entry points, resolved through the runtime on first use so that
+// the library loads (and its C ABI can be inspected) on a machine without a
+// CUDA driver.
+struct DriverApi {
+  decltype(&cuModuleLoadData) moduleLoadData = nullptr;
+  decltype(&cuModuleGetFunction) moduleGetFunction = nullptr;
+  decltype(&cuModuleUnload) moduleUnload = nullptr;
+  decltype(&cuLaunchKernel) launchKernel = nullptr;
+  decltype(&cuFuncSetAttribute) funcSetAttribute = nullptr;
+  decltype(&cuGetErrorString) getErrorString = nullptr;
+  bool ok = false;
+};
+DriverApi g_drv;
+
+const char* drv_err(CUresult r) {
+  const char* s = nullptr;
+  if (g_drv.getErrorString) g_drv.getErrorString(r, &s);
+  return s ? s : "unknown driver error";
+}
+
+#define CS_CU(call)                                                                              \
+  do {                                                                                           \
+    CUresult r_ = (call);                                                                        \
+    if (r_ != CUDA_SUCCESS) {                                                                    \
+      const char* s_ = drv_err(r_);                                                              \
+      return set_err(r_ == CUDA_ERROR_OUT_OF_MEMORY ? CS_ERR_NOMEM : CS_ERR_CUDA,                \
+                     std::string(#call) + ": " + (s_ ? s_ : "?"));                               \
+    }                                                                                            \
+  } while (0)
+
+#define CS_TRY(call)           \
+  do {                         \
+    int rc_ = (call);          \
+    if (rc_ != CS_OK) return rc_; \
+  } while (0)
+
+// Must match struct CsInst in cs_kernels.cuh.
+struct CsInst {
+  int status, it, ls_it, alphacal;
+  int need_jac, accepted, fail_reason, N_new;
+  int residual_count, jac_count, seg_count, remesh_count;
+  int iter_time, singular, pad0, pad1;
+  double alpha_ls, norm_x, alpha, max_res;
+  unsigned long long norm_bits, res_bits;
+};
+static_assert(sizeof(CsInst) == 112, "CsInst layout");
+
+struct CsConsts {
+  double tol, alpha_m, beta;
+  int max_iter, max_mesh, max_nodes, min_nodes, max_ls;
+};
+
+// Must match struct CsBatch in cs_kernels.cuh.
+struct CsBatchDev {
+  int B, T;
+  const int* N;
+  const int* off;
+  const int* inst_of;
+  double* t;
+  double* y;
+  double* ydot;
+  double* zt;
+  double* p;
+  const double* th;
+  double* dy;
+  double* dydot;
+  double* dzt;
+  double* dp;
+  double* X;
+  double* rows0;
+  double* rows1;
+  double* tree;
+  double* res;
+  double* znode;
+  CsInst* inst;
+  int* counters;
+  double* fa_out;
+  double* fb_out;
+};
+
+enum { ST_FRESH = 0, ST_LS = 1, ST_SEG = 2, ST_DONE = 3, ST_FAIL = 4, ST_REMESH = 5 };
+enum { FAIL_NONE = 0, FAIL_ITER = 1, FAIL_NODES = 2, FAIL_MESH = 3 };
+
+uint64_t fnv1a(const std::string& s, uint64_t h = 1469598103934665603ull) {
+  for (unsigned char c : s) {
+    h ^= c;
+    h *= 1099511628211ull;
+  }
+  return h;
+}
+
+std::string fmt_array(const double* a, int n) {
+  std::ostringstream o;
+  o.precision(17);
+  for (int i = 0; i < n; ++i) o << (i ? "," : "") << std::scientific << a[i];
+  if (n == 0) o << "0.0";
+  return o.str();
+}
+
+bool read_file(const std::string& path, std::vector<char>& out) {
+  std::ifstream f(path, std::ios::binary);
+  if (!f) return false;
+  out.assign(std::istreambuf_iterator<char>(f), std::istreambuf_iterator<char>());
+  return !out.empty();
+}
+
+void mkdirs(const std::string& path) {
+  std::string cur;
+  for (size_t i = 0; i < path.size(); ++i) {
+    cur += path[i];
+    if (path[i] == '/' || i + 1 == path.size()) mkdir(cur.c_str(), 0755);
+  }
+}
+
+int resolve(const char* name, void** fn) {
+  cudaDriverEntryPointQueryResult q;
+  cudaError_t e = cudaGetDriverEntryPointByVersion(name, fn, 12000, cudaEnableDefault, &q);
+  if (e != cudaSuccess || q != cudaDriverEntryPointSuccess || !*fn)
+    return set_err(CS_ERR_CUDA, std::string("driver entry point not found: ") + name);
+  return CS_OK;
+}
+
+int ensure_context() {
+  static std::mutex mu;
+  std::lock_guard<std::mutex> lk(mu);
+  CS_CUDA(cudaFree(nullptr));  // creates / binds the primary context for the driver API too
+  if (!g_drv.ok) {
+    CS_TRY(resolve("cuModuleLoadData", (void**)&g_drv.moduleLoadData));
+    CS_TRY(resolve("cuModuleGetFunction", (void**)&g_drv.moduleGetFunction));
+    CS_TRY(resolve("cuModuleUnload", (void**)&g_drv.moduleUnload));
+    CS_TRY(resolve("cuLaunchKernel", (void**)&g_drv.launchKernel));
+    CS_TRY(resolve("cuFuncSetAttribute", (void**)&g_drv.funcSetAttribute));
+    CS_TRY(resolve("cuGetErrorString", (void**)&g_drv.getErrorString));
+    g_drv.ok = true;
+  }
+  return CS_OK;
+}
+
+__global__ void k_fill_inst_of(int B, const int* off, const int* N, int* inst_of) {
+  int b = blockIdx.x;
+  if (b >= B) return;
+  for (int i = threadIdx.x; i < N[b]; i += blockDim.x) inst_of[off[b] + i] = b;
+}
+
+__global__ void k_dfma_peak(double* out, int iters) {
+  double a0 = threadIdx.x * 1e-3, a1 = a0 + 1, a2 = a0 + 2, a3 = a0 + 3, a4 = a0 + 4, a5 = a0 + 5, a6 = a0 + 6,
+         a7 = a0 + 7;
+  const double m = 0.999999, c = 1e-7;
+  for (int i = 0; i < iters; ++i) {
+    a0 = fma(a0, m, c); a1 = fma(a1, m, c); a2 = fma(a2, m, c); a3 = fma(a3, m, c);
+    a4 = fma(a4, m, c); a5 = fma(a5, m, c); a6 = fma(a6, m, c); a7 = fma(a7, m, c);
+  }
+  double s = a0 + a1 + a2 + a3 + a4 + a5 + a6 + a7;
+  if (s == 12345.678) out[0] = s;
+}
+
+}  // namespace
+
+// ============================================================== module ===
+struct cs_module {
+  int ny, nz, np, npe, nth, m, s, nrhs, cgw;
+  size_t rowsz, treesz;
+  CUmodule mod = nullptr;
+  CUfunction f_form_initial, f_residual, f_decide, f_accept, f_condense, f_babd, f_segres, f_mesh_decide,
+      f_remesh_count, f_remesh_write, f_repack, f_znodes;
+  int condense_block, condense_per_cta;
+  size_t condense_smem;
+  int babd_block;
+  size_t babd_smem;
+};
+
+static std::string build_source(const cs_module_desc* d, int cgw) {
+  std::ostringstream o;
+  o << "// generated prelude\n";
+  o << "#define CS_NY " << d->ny << "\n#define CS_NZ " << d->nz << "\n#define CS_NP " << d->np << "\n";
+  o << "#define CS_NPE " << d->np_eff << "\n#define CS_NTH " << d->n_theta << "\n#define CS_M " << d->m << "\n";
+  o << "#define CS_CGW " << cgw << "\n";
+  const int m = d->m;
+  o << "__constant__ double CS_A[" << m * m << "] = {" << fmt_array(d->lobatto_A, m * m) << "};\n";
+  o << "__constant__ double CS_B[" << m << "] = {" << fmt_array(d->lobatto_b, m) << "};\n";
+  o << "__constant__ double CS_C[" << m << "] = {" << fmt_array(d->lobatto_c, m) << "};\n";
+  o << "__constant__ double CS_GW[" << m + 1 << "] = {" << fmt_array(d->gauss_w, m + 1) << "};\n";
+  o << "__constant__ double CS_GL[" << (m + 1) * m << "] = {" << fmt_array(d->gauss_L, (m + 1) * m) << "};\n";
+  o << "__constant__ double CS_GI[" << (m + 1) * m << "] = {" << fmt_array(d->gauss_I, (m + 1) * m) << "};\n";
+  o << "__constant__ double CS_L0[" << m << "] = {" << fmt_array(d->L0, m) << "};\n";
+  o << "__constant__ double CS_L1[" << m << "] = {" << fmt_array(d->L1, m) << "};\n";
+  o << "// problem functions\n" << d->problem_src << "\n";
+  o << cs_kernels_source;
+  return o.str();
+}
+
+static int compile_cubin(const std::string& src, const std::string& cache_dir, std::vector<char>& cubin) {
+  const char* opts[] = {"--gpu-architecture=sm_103a", "-std=c++17", "-lineinfo"};
+  const int nopt = 3;
+  int major = 0, minor = 0;
+  nvrtcVersion(&major, &minor);
+  std::string key_src = src;
+  for (int i = 0; i < nopt; ++i) key_src += std::string("\n//opt ") + opts[i];
+  key_src += "\n//nvrtc " + std::to_string(major) + "." + std::to_string(minor);
+  char name[64];
+  snprintf(name, sizeof(name), "cs_%016llx.cubin", (unsigned long long)fnv1a(key_src));
+  std::string path = cache_dir.empty() ? std::string() : cache_dir + "/" + name;
+  if (!path.empty() && read_file(path, cubin)) return CS_OK;
+  nvrtcProgram prog;
+  if (nvrtcCreateProgram(&prog, src.c_str(), "cs_kernels.cu", 0, nullptr, nullptr) != NVRTC_SUCCESS)
+    return set_err(CS_ERR_NVRTC, "nvrtcCreateProgram failed");
+  nvrtcResult rc = nvrtcCompileProgram(prog, nopt, opts);
+  if (rc != NVRTC_SUCCESS) {
+    size_t n = 0;
+    nvrtcGetProgramLogSize(prog, &n);
+    std::string log(n, '\0');
+    nvrtcGetProgramLog(prog, &log[0]);
+    nvrtcDestroyProgram(&prog);
+    return set_err(CS_ERR_NVRTC, std::string("NVRTC compile failed: ") + nvrtcGetErrorString(rc) + "\n" + log);
+  }
+  size_t n = 0;
+  nvrtcGetCUBINSize(prog, &n);
+  cubin.resize(n);
+  nvrtcGetCUBIN(prog, cubin.data());
+  nvrtcDestroyProgram(&prog);
+  if (!path.empty()) {
+    mkdirs(cache_dir);
+    std::string tmp = path + ".tmp" + std::to_string((long long)getpid());
+    std::ofstream f(tmp, std::ios::binary);
+    if (f) {
+      f.write(cubin.data(), (std::streamsize)cubin.size());
+      f.close();
+      rename(tmp.c_str(), path.c_str());
+    }
+  }
+  return CS_OK;
+}
+
+extern "C" int cs_module_load(const cs_module_desc* d, cs_module** out) {
+  if (!d || !out || !d->problem_src) return set_err(CS_ERR_INVALID, "cs_module_load: null argument");
+  if (d->ny < 1 || d->nz < 0 || d->np < 0 || d->np_eff < 0 || d->np_eff > d->np || d->n_theta < 0 || d->m < 2 ||
+      d->m > 10)
+    return set_err(CS_ERR_INVALID, "cs_module_load: sizes out of range");
+  if (!d->lobatto_A || !d->lobatto_b || !d->lobatto_c || !d->gauss_w || !d->gauss_L || !d->gauss_I || !d->L0 || !d->L1)
+    return set_err(CS_ERR_INVALID, "cs_module_load: missing table");
+  CS_TRY(ensure_context());
+  int dev = 0;
+  CS_CUDA(cudaGetDevice(&dev));
+  int smem_optin = 0;
+  CS_CUDA(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  cs_module* M = new cs_module();
+  M->ny = d->ny; M->nz = d->nz; M->np = d->np; M->npe = d->np_eff; M->nth = d->n_theta; M->m = d->m;
+  M->s = d->m * (d->ny + d->nz);
+  M->nrhs = d->ny + d->np_eff + 1;
+  M->rowsz = (size_t)d->ny * (2 * d->ny + d->np_eff + 1);
+  M->treesz = (size_t)d->ny * (3 * d->ny + d->np_eff + 1);
+  // condensation: shared memory for one augmented matrix per group
+  const int ldw = (M->s + M->nrhs) | 1;
+  const size_t per_mat = ((size_t)M->s * ldw + M->ny + 2 * 8 + 2) * sizeof(double);
+  int cgw = 1;
+  if (M->s > 48) cgw = 8;  // one CTA of 8 warps per interval
+  size_t per = (cgw == 1) ? ((size_t)M->s * ldw + M->ny + 2 * 1 + 2) * sizeof(double) : per_mat;
+  if (per > (size_t)smem_optin) {
+    delete M;
+    return set_err(CS_ERR_INVALID, "cs_module_load: stage system of size " + std::to_string(M->s) +
+                                       " does not fit in shared memory");
+  }
+  M->cgw = cgw;
+  if (cgw == 1) {
+    int per_cta = (int)std::min<size_t>(4, (size_t)smem_optin / per);
+    if (per_cta < 1) per_cta = 1;
+    M->condense_per_cta = per_cta;
+    M->condense_block = 32 * per_cta;
+    M->condense_smem = per * per_cta;
+  } else {
+    M->condense_per_cta = 1;
+    M->condense_block = 32 * cgw;
+    M->condense_smem = per;
+  }
+  // BABD: one CTA per instance, 8 warps, a merge matrix per warp + the top system
+  M->babd_block = 256;
+  const int qld = (2 * M->ny) | 1, qc = 3 * M->ny + M->npe + 1;
+  const int nt = 2 * M->ny + M->np, tld = nt | 1;
+  M->babd_smem = ((size_t)8 * qld * qc + (size_t)tld * (nt + 1) + M->np + 2) * sizeof(double);
+  if (M->babd_smem > (size_t)smem_optin) {
+    delete M;
+    return set_err(CS_ERR_INVALID, "cs_module_load: BABD blocks do not fit in shared memory");
+  }
+
+  std::string src = build_source(d, cgw);
+  std::string cache = d->cache_dir ? d->cache_dir : "";
+  if (cache.empty()) {
+    const char* env = getenv("CS_GB300_CACHE");
+    if (env) cache = env;
+  }
+  std::vector<char> cubin;
+  int rc = compile_cubin(src, cache, cubin);
+  if (rc != CS_OK) {
+    delete M;
+    return rc;
+  }
+  CUresult r = g_drv.moduleLoadData(&M->mod, cubin.data());
+  if (r != CUDA_SUCCESS) {
+    delete M;
+    return set_err(CS_ERR_CUDA, std::string("cuModuleLoadData: ") + drv_err(r));
+  }
+  struct {
+    CUfunction* f;
+    const char* name;
+  } fns[] = {{&M->f_form_initial, "k_form_initial"}, {&M->f_residual, "k_residual"},   {&M->f_decide, "k_decide"},
+             {&M->f_accept, "k_accept"},             {&M->f_condense, "k_condense"},   {&M->f_babd, "k_babd"},
+             {&M->f_segres, "k_segres"},             {&M->f_mesh_decide, "k_mesh_decide"},
+             {&M->f_remesh_count, "k_remesh_count"}, {&M->f_remesh_write, "k_remesh_write"},
+             {&M->f_repack, "k_repack"},             {&M->f_znodes, "k_znodes"}};
+  for (auto& e : fns) {
+    CUresult rr = g_drv.moduleGetFunction(e.f, M->mod, e.name);
+    if (rr != CUDA_SUCCESS) {
+      g_drv.moduleUnload(M->mod);
+      delete M;
+      return set_err(CS_ERR_CUDA, std::string("missing kernel ") + e.name);
+    }
+  }
+  if (M->condense_smem > 48 * 1024)
+    CS_CU(g_drv.funcSetAttribute(M->f_condense, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, (int)M->condense_smem));
+  if (M->babd_smem > 48 * 1024)
+    CS_CU(g_drv.funcSetAttribute(M->f_babd, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, (int)M->babd_smem));
+  *out = M;
+  return CS_OK;
+}
+
+extern "C" void cs_module_free(cs_module* M) {
+  if (!M) return;
+  if (M->mod && g_drv.moduleUnload) g_drv.moduleUnload(M->mod);
+  delete M;
+}
+
+extern "C" void cs_opts_default(cs_opts* o) {
+  if (!o) return;
+  o->tol = 1e-6;
+  o->max_iter = 200;
+  o->max_mesh = 10;
+  o->max_nodes = 2000;
+  o->min_nodes = 3;
+  o->max_linesearch = 20;
+  o->alpha0 = 0.1;
+  o->alpha_m = 0.1;
+  o->beta = 0.9;
+  o->check_every = 4;
+}
+
+// =============================================================== batch ===
+struct DBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+};
+
+struct cs_batch {
+  cs_module* M = nullptr;
+  int B = 0;
+  long long cap = 0;  // node slots allocated
+  int T = 0;          // node slots in use
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  bool have_guess = false;
+  // per instance
+  DBuf dN, doff, doff2, dp, dth, ddp, dinst, dcounters;
+  // per slot (set 0 / set 1 for the arrays a remesh rewrites)
+  DBuf t[2], y[2], ydot[2], zt[2], znode[2];
+  int cur = 0;
+  DBuf inst_of, dy, dydot, dzt, X, rows0, rows1, tree, res;
+  std::vector<int> hN, hoff;
+  cs_opts opts;
+};
+
+static int dalloc(DBuf& b, size_t bytes) {
+  if (b.bytes >= bytes && b.p) return CS_OK;
+  if (b.p) cudaFree(b.p);
+  b.p = nullptr;
+  b.bytes = 0;
+  if (bytes == 0) bytes = 8;
+  CS_CUDA(cudaMalloc(&b.p, bytes));
+  b.bytes = bytes;
+  return CS_OK;
+}
+
+static void dfree(DBuf& b) {
+  if (b.p) cudaFree(b.p);
+  b.p = nullptr;
+  b.bytes = 0;
+}
+
+static int alloc_slots(cs_batch* bt, long long cap, bool keep_current) {
+  cs_module* M = bt->M;
+  const size_t c = (size_t)std::max<long long>(cap, 1);
+  const size_t d = sizeof(double);
+  for (int s = 0; s < 2; ++s) {
+    if (keep_current && s == bt->cur) continue;
+    CS_TRY(dalloc(bt->t[s], c * d));
+    CS_TRY(dalloc(bt->y[s], c * M->ny * d));
+    CS_TRY(dalloc(bt->ydot[s], c * M->m * M->ny * d));
+    CS_TRY(dalloc(bt->zt[s], c * M->m * std::max(M->nz, 1) * d));
+    CS_TRY(dalloc(bt->znode[s], c * std::max(M->nz, 1) * d));
+  }
+  CS_TRY(dalloc(bt->inst_of, c * sizeof(int)));
+  CS_TRY(dalloc(bt->dy, c * M->ny * d));
+  CS_TRY(dalloc(bt->dydot, c * M->m * M->ny * d));
+  CS_TRY(dalloc(bt->dzt, c * M->m * std::max(M->nz, 1) * d));
+  CS_TRY(dalloc(bt->X, c * M->nrhs * M->s * d));
+  CS_TRY(dalloc(bt->rows0, c * M->rowsz * d));
+  CS_TRY(dalloc(bt->rows1, c * M->rowsz * d));
+  CS_TRY(dalloc(bt->tree, c * M->treesz * d));
+  CS_TRY(dalloc(bt->res, c * d));
+  bt->cap = (long long)c;
+  return CS_OK;
+}
+
+// grow the current set too, preserving its contents (used before a remesh)
+static int grow_current(cs_batch* bt, long long need) {
+  if (need <= bt->cap) return CS_OK;
+  long long newcap = std::max<long long>(need, bt->cap + bt->cap / 2);
+  cs_module* M = bt->M;
+  const size_t d = sizeof(double);
+  const int s = bt->cur;
+  struct {
+    DBuf* b;
+    size_t per;
+  } keep[] = {{&bt->t[s], d}, {&bt->y[s], M->ny * d}, {&bt->ydot[s], M->m * M->ny * d},
+              {&bt->zt[s], M->m * std::max(M->nz, 1) * d}, {&bt->znode[s], std::max(M->nz, 1) * d},
+              {&bt->inst_of, sizeof(int)}, {&bt->res, d}};
+  for (auto& k : keep) {
+    DBuf nb;
+    CS_TRY(dalloc(nb, (size_t)newcap * k.per));
+    CS_CUDA(cudaMemcpyAsync(nb.p, k.b->p, (size_t)bt->T * k.per, cudaMemcpyDeviceToDevice, bt->stream));
+    CS_CUDA(cudaStreamSynchronize(bt->stream));
+    dfree(*k.b);
+    *k.b = nb;
+  }
+  return alloc_slots(bt, newcap, true);
+}
+
+static CsBatchDev devview(cs_batch* bt) {
+  CsBatchDev v;
+  memset(&v, 0, sizeof(v));
+  const int s = bt->cur;
+  v.B = bt->B;
+  v.T = bt->T;
+  v.N = (const int*)bt->dN.p;
+  v.off = (const int*)bt->doff.p;
+  v.inst_of = (const int*)bt->inst_of.p;
+  v.t = (double*)bt->t[s].p;
+  v.y = (double*)bt->y[s].p;
+  v.ydot = (double*)bt->ydot[s].p;
+  v.zt = (double*)bt->zt[s].p;
+  v.p = (double*)bt->dp.p;
+  v.th = (const double*)bt->dth.p;
+  v.dy = (double*)bt->dy.p;
+  v.dydot = (double*)bt->dydot.p;
+  v.dzt = (double*)bt->dzt.p;
+  v.dp = (double*)bt->ddp.p;
+  v.X = (double*)bt->X.p;
+  v.rows0 = (double*)bt->rows0.p;
+  v.rows1 = (double*)bt->rows1.p;
+  v.tree = (double*)bt->tree.p;
+  v.res = (double*)bt->res.p;
+  v.znode = (double*)bt->znode[s].p;
+  v.inst = (CsInst*)bt->dinst.p;
+  v.counters = (int*)bt->dcounters.p;
+  return v;
+}
+
+static int launch(cs_batch* bt, CUfunction f, unsigned grid, unsigned block, size_t smem, void** args) {
+  if (grid == 0) return CS_OK;
+  CS_CU(g_drv.launchKernel(f, grid, 1, 1, block, 1, 1, (unsigned)smem, (CUstream)bt->stream, args, nullptr));
+  return CS_OK;
+}
+
+static unsigned cdiv(long long a, long long b) { return (unsigned)((a + b - 1) / b); }
+
+static int run_slots(cs_batch* bt, CUfunction f, CsBatchDev& v) {
+  void* args[] = {&v};
+  return launch(bt, f, cdiv(bt->T, 256), 256, 0, args);
+}
+
+static int run_insts(cs_batch* bt, CUfunction f, void** args) { return launch(bt, f, cdiv(bt->B, 128), 128, 0, args); }
+
+static int run_condense(cs_batch* bt, CsBatchDev& v) {
+  cs_module* M = bt->M;
+  void* args[] = {&v};
+  unsigned grid = (M->cgw == 1) ? cdiv(bt->T, M->condense_per_cta) : (unsigned)bt->T;
+  return launch(bt, M->f_condense, grid, M->condense_block, M->condense_smem, args);
+}
+
+static int run_babd(cs_batch* bt, CsBatchDev& v) {
+  void* args[] = {&v};
+  return launch(bt, bt->M->f_babd, (unsigned)bt->B, bt->M->babd_block, bt->M->babd_smem, args);
+}
+
+static int fill_inst_of(cs_batch* bt) {
+  k_fill_inst_of<<<bt->B, 256, 0, bt->stream>>>(bt->B, (const int*)bt->doff.p, (const int*)bt->dN.p,
+                                                  (int*)bt->inst_of.p);
+  CS_CUDA(cudaGetLastError());
+  return CS_OK;
+}
+
+static CsConsts consts_of(const cs_opts& o) {
+  CsConsts c;
+  c.tol = o.tol;
+  c.alpha_m = o.alpha_m;
+  c.beta = o.beta;
+  c.max_iter = o.max_iter;
+  c.max_mesh = o.max_mesh;
+  c.max_nodes = o.max_nodes;
+  c.min_nodes = o.min_nodes;
+  c.max_ls = o.max_linesearch;
+  return c;
+}
+
+extern "C" int cs_batch_create(cs_module* M, int batch, long long node_capacity, void* stream, cs_batch** out) {
+  if (!M || !out || batch < 1) return set_err(CS_ERR_INVALID, "cs_batch_create: bad argument");
+  CS_TRY(ensure_context());
+  cs_batch* bt = new cs_batch();
+  bt->M = M;
+  bt->B = batch;
+  cs_opts_default(&bt->opts);
+  if (stream) {
+    bt->stream = (cudaStream_t)stream;
+  } else {
+    if (cudaStreamCreateWithFlags(&bt->stream, cudaStreamNonBlocking) != cudaSuccess) {
+      delete bt;
+      return set_err(CS_ERR_CUDA, "cudaStreamCreate failed");
+    }
+    bt->own_stream = true;
+  }
+  int rc = CS_OK;
+  const size_t d = sizeof(double);
+  if ((rc = dalloc(bt->dN, batch * sizeof(int))) || (rc = dalloc(bt->doff, batch * sizeof(int))) ||
+      (rc = dalloc(bt->doff2, batch * sizeof(int))) || (rc = dalloc(bt->dp, batch * std::max(M->np, 1) * d)) ||
+      (rc = dalloc(bt->ddp, batch * std::max(M->np, 1) * d)) ||
+      (rc = dalloc(bt->dth, batch * std::max(M->nth, 1) * d)) || (rc = dalloc(bt->dinst, batch * sizeof(CsInst))) ||
+      (rc = dalloc(bt->dcounters, 64)) || (rc = alloc_slots(bt, std::max<long long>(node_capacity, 2 * batch), false))) {
+    cs_batch_free(bt);
+    return rc;
+  }
+  *out = bt;
+  return CS_OK;
+}
+
+extern "C" void cs_batch_free(cs_batch* bt) {
+  if (!bt) return;
+  if (bt->stream) cudaStreamSynchronize(bt->stream);
+  DBuf* all[] = {&bt->dN, &bt->doff, &bt->doff2, &bt->dp, &bt->dth, &bt->ddp, &bt->dinst, &bt->dcounters,
+                 &bt->inst_of, &bt->dy, &bt->dydot, &bt->dzt, &bt->X, &bt->rows0, &bt->rows1, &bt->tree, &bt->res};
+  for (DBuf* b : all) dfree(*b);
+  for (int s = 0; s < 2; ++s) {
+    dfree(bt->t[s]); dfree(bt->y[s]); dfree(bt->ydot[s]); dfree(bt->zt[s]); dfree(bt->znode[s]);
+  }
+  if (bt->own_stream && bt->stream) cudaStreamDestroy(bt->stream);
+  delete bt;
+}
+
+static void init_inst(CsInst& s, double alpha0) {
+  memset(&s, 0, sizeof(s));
+  s.status = ST_FRESH;
+  s.alpha = alpha0;
+  s.alpha_ls = 1.0;
+}
+
+extern "C" int cs_batch_set_guess(cs_batch* bt, const int* N, const double* t, const double* y, const double* z,
+                                  const double* p, const double* theta) {
+  if (!bt || !N || !t || !y) return set_err(CS_ERR_INVALID, "cs_batch_set_guess: null argument");
+  cs_module* M = bt->M;
+  if (M->nz > 0 && !z) return set_err(CS_ERR_INVALID, "cs_batch_set_guess: z is required (nz > 0)");
+  if (M->np > 0 && !p) return set_err(CS_ERR_INVALID, "cs_batch_set_guess: p is required (np > 0)");
+  if (M->nth > 0 && !theta) return set_err(CS_ERR_INVALID, "cs_batch_set_guess: theta is required");
+  long long T = 0;
+  bt->hN.assign(N, N + bt->B);
+  bt->hoff.resize(bt->B);
+  for (int b = 0; b < bt->B; ++b) {
+    if (N[b] < 2) return set_err(CS_ERR_INVALID, "cs_batch_set_guess: every instance needs at least 2 nodes");
+    bt->hoff[b] = (int)T;
+    T += N[b];
+  }
+  if (T > 2000000000LL) return set_err(CS_ERR_INVALID, "cs_batch_set_guess: too many nodes");
+  if (T > bt->cap) CS_TRY(alloc_slots(bt, T, false));
+  bt->T = (int)T;
+  bt->cur = 0;
+  const size_t d = sizeof(double);
+  cudaStream_t st = bt->stream;
+  CS_CUDA(cudaMemcpyAsync(bt->dN.p, N, bt->B * sizeof(int), cudaMemcpyHostToDevice, st));
+  CS_CUDA(cudaMemcpyAsync(bt->doff.p, bt->hoff.data(), bt->B * sizeof(int), cudaMemcpyHostToDevice, st));
+  CS_CUDA(cudaMemcpyAsync(bt->t[0].p, t, T * d, cudaMemcpyHostToDevice, st));
+  CS_CUDA(cudaMemcpyAsync(bt->y[0].p, y, T * M->ny * d, cudaMemcpyHostToDevice, st));
+  if (M->nz > 0) CS_CUDA(cudaMemcpyAsync(bt->znode[0].p, z, T * M->nz * d, cudaMemcpyHostToDevice, st));
+  if (M->np > 0) CS_CUDA(cudaMemcpyAsync(bt->dp.p, p, (size_t)bt->B * M->np * d, cudaMemcpyHostToDevice, st));
+  if (M->nth > 0) CS_CUDA(cudaMemcpyAsync(bt->dth.p, theta, (size_t)bt->B * M->nth * d, cudaMemcpyHostToDevice, st));
+  std::vector<CsInst> hi(bt->B);
+  for (auto& s : hi) init_inst(s, bt->opts.alpha0);
+  CS_CUDA(cudaMemcpyAsync(bt->dinst.p, hi.data(), hi.size() * sizeof(CsInst), cudaMemcpyHostToDevice, st));
+  CS_TRY(fill_inst_of(bt));
+  CsBatchDev v = devview(bt);
+  int only = -1;
+  void* args[] = {&v, &only};
+  CS_TRY(launch(bt, M->f_form_initial, cdiv(bt->T, 256), 256, 0, args));
+  CS_CUDA(cudaStreamSynchronize(st));
+  bt->have_guess = true;
+  return CS_OK;
+}
+
+extern "C" int cs_batch_set_state(cs_batch* bt, const int* N, const double* t, const double* y, const double* ydot,
+                                  const double* zt, const double* p, const double* theta) {
+  if (!bt || !N || !t || !y || !ydot) return set_err(CS_ERR_INVALID, "cs_batch_set_state: null argument");
+  cs_module* M = bt->M;
+  if (M->nz > 0 && !zt) return set_err(CS_ERR_INVALID, "cs_batch_set_state: zt is required (nz > 0)");
+  if (M->np > 0 && !p) return set_err(CS_ERR_INVALID, "cs_batch_set_state: p is required (np > 0)");
+  if (M->nth > 0 && !theta) return set_err(CS_ERR_INVALID, "cs_batch_set_state: theta is required");
+  long long T = 0;
+  for (int b = 0; b < bt->B; ++b) {
+    if (N[b] < 2) return set_err(CS_ERR_INVALID, "cs_batch_set_state: every instance needs at least 2 nodes");
+    T += N[b];
+  }
+  if (T > 2000000000LL) return set_err(CS_ERR_INVALID, "cs_batch_set_state: too many nodes");
+  if (T > bt->cap) CS_TRY(alloc_slots(bt, T, false));
+  bt->hN.assign(N, N + bt->B);
+  bt->hoff.resize(bt->B);
+  // stage values: (N-1) rows per instance on the host, N slots on the device
+  const size_t ry = (size_t)M->m * M->ny, rz = (size_t)M->m * M->nz;
+  std::vector<double> yd((size_t)T * ry, 0.0), zz((size_t)T * std::max<size_t>(rz, 1), 0.0);
+  long long o = 0, hrow = 0;
+  for (int b = 0; b < bt->B; ++b) {
+    bt->hoff[b] = (int)o;
+    for (int i = 0; i < N[b] - 1; ++i, ++hrow) {
+      memcpy(&yd[(size_t)(o + i) * ry], ydot + (size_t)hrow * ry, ry * sizeof(double));
+      if (rz) memcpy(&zz[(size_t)(o + i) * rz], zt + (size_t)hrow * rz, rz * sizeof(double));
+    }
+    o += N[b];
+  }
+  bt->T = (int)T;
+  bt->cur = 0;
+  const size_t d = sizeof(double);
+  cudaStream_t st = bt->stream;
+  CS_CUDA(cudaMemcpyAsync(bt->dN.p, N, bt->B * sizeof(int), cudaMemcpyHostToDevice, st));
+  CS_CUDA(cudaMemcpyAsync(bt->doff.p, bt->hoff.data(), bt->B * sizeof(int), cudaMemcpyHostToDevice, st));
+  CS_CUDA(cudaMemcpyAsync(bt->t[0].p, t, T * d, cudaMemcpyHostToDevice, st));
+  CS_CUDA(cudaMemcpyAsync(bt->y[0].p, y, T * M->ny * d, cudaMemcpyHostToDevice, st));
+  CS_CUDA(cudaMemcpyAsync(bt->ydot[0].p, yd.data(), yd.size() * d, cudaMemcpyHostToDevice, st));
+  if (rz) CS_CUDA(cudaMemcpyAsync(bt->zt[0].p, zz.data(), (size_t)T * rz * d, cudaMemcpyHostToDevice, st));
+  if (M->np > 0) CS_CUDA(cudaMemcpyAsync(bt->dp.p, p, (size_t)bt->B * M->np * d, cudaMemcpyHostToDevice, st));
+  if (M->nth > 0) CS_CUDA(cudaMemcpyAsync(bt->dth.p, theta, (size_t)bt->B * M->nth * d, cudaMemcpyHostToDevice, st));
+  std::vector<CsInst> hi(bt->B);
+  for (auto& s : hi) init_inst(s, bt->opts.alpha0);
+  CS_CUDA(cudaMemcpyAsync(bt->dinst.p, hi.data(), hi.size() * sizeof(CsInst), cudaMemcpyHostToDevice, st));
+  CS_TRY(fill_inst_of(bt));
+  CS_CUDA(cudaStreamSynchronize(st));
+  bt->have_guess = true;
+  return CS_OK;
+}
+
+static int read_inst(cs_batch* bt, std::vector<CsInst>& hi) {
+  hi.resize(bt->B);
+  CS_CUDA(cudaMemcpyAsync(hi.data(), bt->dinst.p, hi.size() * sizeof(CsInst), cudaMemcpyDeviceToHost, bt->stream));
+  CS_CUDA(cudaStreamSynchronize(bt->stream));
+  return CS_OK;
+}
+
+static int write_inst(cs_batch* bt, const std::vector<CsInst>& hi) {
+  CS_CUDA(cudaMemcpyAsync(bt->dinst.p, hi.data(), hi.size() * sizeof(CsInst), cudaMemcpyHostToDevice, bt->stream));
+  return CS_OK;
+}
+
+static int super_step(cs_batch* bt, const CsConsts& c) {
+  CsBatchDev v = devview(bt);
+  cs_module* M = bt->M;
+  CS_TRY(run_slots(bt, M->f_residual, v));
+  CsConsts cc = c;
+  void* dargs[] = {&v, &cc};
+  CS_TRY(run_insts(bt, M->f_decide, dargs));
+  CS_TRY(run_slots(bt, M->f_accept, v));
+  CS_TRY(run_condense(bt, v));
+  CS_TRY(run_babd(bt, v));
+  return CS_OK;
+}
+
+// Remesh every instance whose status is ST_REMESH; node counts N_new are in
+// the device inst records after k_remesh_count.
+static int do_remesh(cs_batch* bt, std::vector<CsInst>& hi) {
+  cs_module* M = bt->M;
+  CsBatchDev v = devview(bt);
+  void* a1[] = {&v};
+  CS_TRY(run_insts(bt, M->f_remesh_count, a1));
+  CS_TRY(read_inst(bt, hi));
+  std::vector<int> off2(bt->B), N2(bt->B);
+  long long T2 = 0;
+  for (int b = 0; b < bt->B; ++b) {
+    off2[b] = (int)T2;
+    N2[b] = hi[b].N_new;
+    T2 += N2[b];
+  }
+  if (T2 > 2000000000LL) return set_err(CS_ERR_INVALID, "remesh: too many nodes");
+  CS_TRY(grow_current(bt, std::max<long long>(T2, bt->T)));
+  v = devview(bt);
+  const int o = 1 - bt->cur;
+  CS_CUDA(cudaMemcpyAsync(bt->doff2.p, off2.data(), bt->B * sizeof(int), cudaMemcpyHostToDevice, bt->stream));
+  double* t2 = (double*)bt->t[o].p;
+  double* y2 = (double*)bt->y[o].p;
+  double* yd2 = (double*)bt->ydot[o].p;
+  double* zt2 = (double*)bt->zt[o].p;
+  double* zn2 = (double*)bt->znode[o].p;
+  const int* doff2 = (const int*)bt->doff2.p;
+  void* aw[] = {&v, &doff2, &t2, &y2, &zn2};
+  CS_TRY(run_insts(bt, M->f_remesh_write, aw));
+  void* ar[] = {&v, &doff2, &t2, &y2, &yd2, &zt2};
+  CS_TRY(launch(bt, M->f_repack, cdiv(bt->T, 256), 256, 0, ar));
+  // switch to the new layout
+  bt->cur = o;
+  bt->T = (int)T2;
+  bt->hN = N2;
+  bt->hoff = off2;
+  CS_CUDA(cudaMemcpyAsync(bt->dN.p, N2.data(), bt->B * sizeof(int), cudaMemcpyHostToDevice, bt->stream));
+  CS_CUDA(cudaMemcpyAsync(bt->doff.p, off2.data(), bt->B * sizeof(int), cudaMemcpyHostToDevice, bt->stream));
+  CS_TRY(fill_inst_of(bt));
+  v = devview(bt);
+  int only = ST_REMESH;
+  void* af[] = {&v, &only};
+  CS_TRY(launch(bt, M->f_form_initial, cdiv(bt->T, 256), 256, 0, af));
+  CS_CUDA(cudaStreamSynchronize(bt->stream));
+  return CS_OK;
+}
+
+extern "C" int cs_solve(cs_batch* bt, const cs_opts* opts) {
+  if (!bt) return set_err(CS_ERR_INVALID, "cs_solve: null batch");
+  if (!bt->have_guess) return set_err(CS_ERR_STATE, "cs_solve: no initial guess");
+  cs_opts o;
+  if (opts) o = *opts; else cs_opts_default(&o);
+  if (o.check_every < 1) o.check_every = 1;
+  bt->opts = o;
+  const CsConsts c = consts_of(o);
+  std::vector<CsInst> hi;
+  CS_TRY(read_inst(bt, hi));
+  for (auto& s : hi) {
+    if (s.status != ST_FRESH) continue;
+    s.alpha = o.alpha0;
+  }
+  CS_TRY(write_inst(bt, hi));
+  int* hcount = nullptr;
+  CS_CUDA(cudaMallocHost(&hcount, sizeof(int)));
+  int rc = CS_OK;
+  const long long max_super = 1000000;
+  long long steps = 0;
+  for (int outer = 0; outer < 1000000 && rc == CS_OK; ++outer) {
+    // ---- Newton phase
+    for (;;) {
+      for (int k = 0; k < o.check_every && rc == CS_OK; ++k) {
+        if (cudaMemsetAsync(bt->dcounters.p, 0, sizeof(int), bt->stream) != cudaSuccess) {
+          rc = set_err(CS_ERR_CUDA, "memset");
+          break;
+        }
+        rc = super_step(bt, c);
+        ++steps;
+      }
+      if (rc != CS_OK) break;
+      if (cudaMemcpyAsync(hcount, bt->dcounters.p, sizeof(int), cudaMemcpyDeviceToHost, bt->stream) != cudaSuccess ||
+          cudaStreamSynchronize(bt->stream) != cudaSuccess) {
+        rc = set_err(CS_ERR_CUDA, std::string("Newton phase: ") + cudaGetErrorString(cudaGetLastError()));
+        break;
+      }
+      if (*hcount == 0) break;
+      if (steps > max_super) {
+        rc = set_err(CS_ERR_STATE, "Newton phase did not terminate");
+        break;
+      }
+    }
+    if (rc != CS_OK) break;
+    // ---- mesh phase
+    CsBatchDev v = devview(bt);
+    double tol = o.tol;
+    void* as[] = {&v, &tol};
+    if ((rc = launch(bt, bt->M->f_segres, cdiv(bt->T, 256), 256, 0, as)) != CS_OK) break;
+    CsConsts cc = c;
+    void* am[] = {&v, &cc};
+    if ((rc = run_insts(bt, bt->M->f_mesh_decide, am)) != CS_OK) break;
+    if ((rc = read_inst(bt, hi)) != CS_OK) break;
+    bool any_remesh = false, any_newton = false;
+    for (auto& s : hi) {
+      any_remesh |= (s.status == ST_REMESH);
+      any_newton |= (s.status == ST_FRESH || s.status == ST_LS);
+    }
+    if (any_remesh) {
+      if ((rc = do_remesh(bt, hi)) != CS_OK) break;
+      if ((rc = read_inst(bt, hi)) != CS_OK) break;
+      for (int b = 0; b < bt->B; ++b) {
+        CsInst& s = hi[b];
+        if (s.status != ST_REMESH) continue;
+        s.remesh_count += 1;
+        const int N = bt->hN[b];
+        // mesh_sanity_check (CS:2367-2377) with mesh_it = 1 (reset every continuation step, CS:107)
+        if (1 > o.max_mesh) { s.status = ST_FAIL; s.fail_reason = FAIL_MESH; continue; }
+        if (N > o.max_nodes || N < o.min_nodes) { s.status = ST_FAIL; s.fail_reason = FAIL_NODES; continue; }
+        s.status = ST_FRESH;
+        s.it = 0;
+        s.alphacal += 1;
+        s.norm_bits = 0;
+      }
+      if ((rc = write_inst(bt, hi)) != CS_OK) break;
+      any_newton = true;
+    }
+    if (!any_newton) break;
+  }
+  cudaFreeHost(hcount);
+  if (rc == CS_OK) CS_CUDA(cudaStreamSynchronize(bt->stream));
+  return rc;
+}
+
+extern "C" int cs_batch_sizes(cs_batch* bt, int* N_out, long long* total_out) {
+  if (!bt) return set_err(CS_ERR_INVALID, "cs_batch_sizes: null batch");
+  if (N_out) std::copy(bt->hN.begin(), bt->hN.end(), N_out);
+  if (total_out) *total_out = bt->T;
+  return CS_OK;
+}
+
+static int compute_znodes(cs_batch* bt) {
+  CsBatchDev v = devview(bt);
+  return run_slots(bt, bt->M->f_znodes, v);
+}
+
+extern "C" int cs_get_solution(cs_batch* bt, double* t, double* y, double* z, double* p, cs_stats* stats) {
+  if (!bt || !bt->have_guess) return set_err(CS_ERR_STATE, "cs_get_solution: nothing solved");
+  cs_module* M = bt->M;
+  const size_t d = sizeof(double);
+  const int s = bt->cur;
+  cudaStream_t st = bt->stream;
+  if (z && M->nz > 0) {
+    CS_TRY(compute_znodes(bt));
+    CS_CUDA(cudaMemcpyAsync(z, bt->znode[s].p, (size_t)bt->T * M->nz * d, cudaMemcpyDeviceToHost, st));
+  }
+  if (t) CS_CUDA(cudaMemcpyAsync(t, bt->t[s].p, (size_t)bt->T * d, cudaMemcpyDeviceToHost, st));
+  if (y) CS_CUDA(cudaMemcpyAsync(y, bt->y[s].p, (size_t)bt->T * M->ny * d, cudaMemcpyDeviceToHost, st));
+  if (p && M->np > 0) CS_CUDA(cudaMemcpyAsync(p, bt->dp.p, (size_t)bt->B * M->np * d, cudaMemcpyDeviceToHost, st));
+  if (stats) {
+    std::vector<CsInst> hi;
+    CS_TRY(read_inst(bt, hi));
+    for (int b = 0; b < bt->B; ++b) {
+      const CsInst& q = hi[b];
+      cs_stats& o = stats[b];
+      o.status = q.status;
+      o.N = bt->hN[b];
+      o.newton_steps = q.jac_count;
+      o.residual_evals = q.residual_count;
+      o.segment_evals = q.seg_count;
+      o.remeshes = q.remesh_count;
+      o.continuation_steps = q.alphacal;
+      o.singular = q.singular;
+      o.fail_reason = q.fail_reason;
+      o.alpha = q.alpha;
+      o.max_residual = q.max_res;
+      o.last_norm = q.norm_x;
+    }
+  }
+  CS_CUDA(cudaStreamSynchronize(st));
+  return CS_OK;
+}
+
+extern "C" int cs_get_state(cs_batch* bt, double* t, double* y, double* ydot, double* zt, double* z_nodes, double* p) {
+  if (!bt || !bt->have_guess) return set_err(CS_ERR_STATE, "cs_get_state: no state");
+  cs_module* M = bt->M;
+  const size_t d = sizeof(double);
+  const int s = bt->cur;
+  cudaStream_t st = bt->stream;
+  if (t) CS_CUDA(cudaMemcpyAsync(t, bt->t[s].p, (size_t)bt->T * d, cudaMemcpyDeviceToHost, st));
+  if (y) CS_CUDA(cudaMemcpyAsync(y, bt->y[s].p, (size_t)bt->T * M->ny * d, cudaMemcpyDeviceToHost, st));
+  if (ydot) CS_CUDA(cudaMemcpyAsync(ydot, bt->ydot[s].p, (size_t)bt->T * M->m * M->ny * d, cudaMemcpyDeviceToHost, st));
+  if (zt && M->nz > 0) CS_CUDA(cudaMemcpyAsync(zt, bt->zt[s].p, (size_t)bt->T * M->m * M->nz * d, cudaMemcpyDeviceToHost, st));
+  if (z_nodes && M->nz > 0) {
+    CS_TRY(compute_znodes(bt));
+    CS_CUDA(cudaMemcpyAsync(z_nodes, bt->znode[s].p, (size_t)bt->T * M->nz * d, cudaMemcpyDeviceToHost, st));
+  }
+  if (p && M->np > 0) CS_CUDA(cudaMemcpyAsync(p, bt->dp.p, (size_t)bt->B * M->np * d, cudaMemcpyDeviceToHost, st));
+  CS_CUDA(cudaStreamSynchronize(st));
+  return CS_OK;
+}
+
+// put every instance into `status` at continuation parameter alpha
+static int set_all_status(cs_batch* bt, int status, double alpha, int need_jac) {
+  std::vector<CsInst> hi;
+  CS_TRY(read_inst(bt, hi));
+  for (auto& s : hi) {
+    s.status = status;
+    s.alpha = alpha;
+    s.need_jac = need_jac;
+    s.accepted = 0;
+    s.norm_bits = 0;
+    s.res_bits = 0;
+  }
+  return write_inst(bt, hi);
+}
+
+extern "C" int cs_stage_residual(cs_batch* bt, double alpha, double* norms, double* f_a, double* f_b) {
+  if (!bt || !bt->have_guess) return set_err(CS_ERR_STATE, "cs_stage_residual: no state");
+  cs_module* M = bt->M;
+  CS_TRY(set_all_status(bt, ST_FRESH, alpha, 0));
+  DBuf fa, fb;
+  if (f_a) CS_TRY(dalloc(fa, (size_t)bt->T * M->s * sizeof(double)));
+  if (f_b) CS_TRY(dalloc(fb, (size_t)bt->T * M->ny * sizeof(double)));
+  CsBatchDev v = devview(bt);
+  v.fa_out = (double*)fa.p;
+  v.fb_out = (double*)fb.p;
+  int rc = run_slots(bt, M->f_residual, v);
+  std::vector<CsInst> hi;
+  if (rc == CS_OK) rc = read_inst(bt, hi);
+  if (rc == CS_OK && norms)
+    for (int b = 0; b < bt->B; ++b) {
+      unsigned long long bits = hi[b].norm_bits;
+      double x;
+      memcpy(&x, &bits, sizeof(x));
+      norms[b] = x;
+    }
+  if (rc == CS_OK && f_a && cudaMemcpy(f_a, fa.p, (size_t)bt->T * M->s * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess)
+    rc = set_err(CS_ERR_CUDA, "copy f_a");
+  if (rc == CS_OK && f_b && cudaMemcpy(f_b, fb.p, (size_t)bt->T * M->ny * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess)
+    rc = set_err(CS_ERR_CUDA, "copy f_b");
+  dfree(fa);
+  dfree(fb);
+  if (rc == CS_OK) {
+    for (auto& s : hi) s.norm_bits = 0;
+    rc = write_inst(bt, hi);
+  }
+  return rc;
+}
+
+extern "C" int cs_stage_newton_direction(cs_batch* bt, double alpha, double* rows, double* dy, double* dydot,
+                                         double* dzt, double* dp) {
+  if (!bt || !bt->have_guess) return set_err(CS_ERR_STATE, "cs_stage_newton_direction: no state");
+  cs_module* M = bt->M;
+  CS_TRY(set_all_status(bt, ST_FRESH, alpha, 1));
+  CsBatchDev v = devview(bt);
+  CS_TRY(run_condense(bt, v));
+  const size_t d = sizeof(double);
+  cudaStream_t st = bt->stream;
+  if (rows) CS_CUDA(cudaMemcpyAsync(rows, bt->rows0.p, (size_t)bt->T * M->rowsz * d, cudaMemcpyDeviceToHost, st));
+  CS_TRY(run_babd(bt, v));
+  if (dy) CS_CUDA(cudaMemcpyAsync(dy, bt->dy.p, (size_t)bt->T * M->ny * d, cudaMemcpyDeviceToHost, st));
+  if (dydot) CS_CUDA(cudaMemcpyAsync(dydot, bt->dydot.p, (size_t)bt->T * M->m * M->ny * d, cudaMemcpyDeviceToHost, st));
+  if (dzt && M->nz > 0) CS_CUDA(cudaMemcpyAsync(dzt, bt->dzt.p, (size_t)bt->T * M->m * M->nz * d, cudaMemcpyDeviceToHost, st));
+  if (dp && M->np > 0) CS_CUDA(cudaMemcpyAsync(dp, bt->ddp.p, (size_t)bt->B * M->np * d, cudaMemcpyDeviceToHost, st));
+  CS_CUDA(cudaStreamSynchronize(st));
+  return set_all_status(bt, ST_FRESH, alpha, 0);
+}
+
+extern "C" int cs_stage_segment_residual(cs_batch* bt, double alpha, double tol, double* res, double* max_res) {
+  if (!bt || !bt->have_guess) return set_err(CS_ERR_STATE, "cs_stage_segment_residual: no state");
+  CS_TRY(set_all_status(bt, ST_SEG, alpha, 0));
+  CsBatchDev v = devview(bt);
+  void* as[] = {&v, &tol};
+  CS_TRY(launch(bt, bt->M->f_segres, cdiv(bt->T, 256), 256, 0, as));
+  if (res) CS_CUDA(cudaMemcpyAsync(res, bt->res.p, (size_t)bt->T * sizeof(double), cudaMemcpyDeviceToHost, bt->stream));
+  std::vector<CsInst> hi;
+  CS_TRY(read_inst(bt, hi));
+  if (max_res)
+    for (int b = 0; b < bt->B; ++b) {
+      unsigned long long bits = hi[b].res_bits;
+      double x;
+      memcpy(&x, &bits, sizeof(x));
+      max_res[b] = x;
+    }
+  return set_all_status(bt, ST_FRESH, alpha, 0);
+}
+
+extern "C" int cs_stage_remesh(cs_batch* bt, const double* res, int* N_new) {
+  if (!bt || !bt->have_guess || !res) return set_err(CS_ERR_STATE, "cs_stage_remesh: no state");
+  CS_CUDA(cudaMemcpyAsync(bt->res.p, res, (size_t)bt->T * sizeof(double), cudaMemcpyHostToDevice, bt->stream));
+  std::vector<CsInst> hi;
+  CS_TRY(read_inst(bt, hi));
+  for (auto& s : hi) s.status = ST_REMESH;
+  CS_TRY(write_inst(bt, hi));
+  CS_TRY(do_remesh(bt, hi));
+  if (N_new) std::copy(bt->hN.begin(), bt->hN.end(), N_new);
+  double a = bt->opts.alpha0;
+  return set_all_status(bt, ST_FRESH, a, 0);
+}
+
+extern "C" int cs_time_condense(cs_batch* bt, int reps, double* ms) {
+  if (!bt || !bt->have_guess || !ms || reps < 1) return set_err(CS_ERR_INVALID, "cs_time_condense: bad argument");
+  CS_TRY(set_all_status(bt, ST_FRESH, bt->opts.alpha0, 1));
+  CsBatchDev v = devview(bt);
+  CS_TRY(run_condense(bt, v));
+  cudaEvent_t e0, e1;
+  CS_CUDA(cudaEventCreate(&e0));
+  CS_CUDA(cudaEventCreate(&e1));
+  CS_CUDA(cudaEventRecord(e0, bt->stream));
+  for (int r = 0; r < reps; ++r) CS_TRY(run_condense(bt, v));
+  CS_CUDA(cudaEventRecord(e1, bt->stream));
+  CS_CUDA(cudaEventSynchronize(e1));
+  float t = 0.f;
+  CS_CUDA(cudaEventElapsedTime(&t, e0, e1));
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  *ms = (double)t / reps;
+  return set_all_status(bt, ST_FRESH, bt->opts.alpha0, 0);
+}
+
+extern "C" int cs_measure_fp64_peak(double* tflops) {
+  if (!tflops) return set_err(CS_ERR_INVALID, "cs_measure_fp64_peak: null");
+  CS_TRY(ensure_context());
+  int dev = 0, sms = 0;
+  CS_CUDA(cudaGetDevice(&dev));
+  CS_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  double* out = nullptr;
+  CS_CUDA(cudaMalloc(&out, sizeof(double)));
+  const int iters = 4096, block = 256, grid = sms * 8;
+  k_dfma_peak<<<grid, block>>>(out, 64);
+  cudaEvent_t e0, e1;
+  CS_CUDA(cudaEventCreate(&e0));
+  CS_CUDA(cudaEventCreate(&e1));
+  CS_CUDA(cudaEventRecord(e0));
+  k_dfma_peak<<<grid, block>>>(out, iters);
+  CS_CUDA(cudaEventRecord(e1));
+  CS_CUDA(cudaEventSynchronize(e1));
+  float t = 0.f;
+  CS_CUDA(cudaEventElapsedTime(&t, e0, e1));
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(out);
+  const double flops = 2.0 * 8.0 * iters * (double)grid * block;
+  *tflops = flops / (t * 1e-3) / 1e12;
+  return CS_OK;
+}
+
+extern "C" int cs_last_error(char* buf, size_t len) {
+  if (!buf || len == 0) return (int)g_err.size();
+  size_t n = std::min(len - 1, g_err.size());
+  memcpy(buf, g_err.data(), n);
+  buf[n] = '\0';
+  return (int)g_err.size();
+}

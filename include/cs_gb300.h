@@ -1,0 +1,189 @@
+/*
+ * cs_gb300.h — C ABI of the GB300-native collocation solver (libcs_gb300.so).
+ *
+ * Solves the BVP-DAEs that the Pontryagin conditions of a nonlinear optimal
+ * control problem give, y' = f(y,z,p), 0 = g(y,z,p,alpha), r(y(t0),y(tf),p)
+ * = 0, by Lobatto IIIA collocation and a damped Newton method with mesh
+ * refinement: the Newton inner loop of UW-OCP/Collocation-Solver-CUDA,
+ * re-designed for one GB300 (sm_103a), FP64, with many instances per launch.
+ *
+ * The reference has no FFI: its boundary is a set of Python stage functions
+ * that take numpy arrays and allocate device memory per call.  Each entry
+ * point below names the reference function(s) it replaces
+ * (collocation_solver_parallel_2d_shared.py = CS, solve_babd_system.py = SB).
+ *
+ * Conventions: every function returns CS_OK (0) or an error code and never
+ * throws; cs_last_error() gives the message of the calling thread's last
+ * error.  Host arrays are packed per instance in instance order: for node
+ * arrays, instance b's rows start after the sum of N[0..b-1] rows.  One batch
+ * is used by one host thread at a time; calls are ordered on the batch's
+ * stream and return after it has finished.
+ */
+#ifndef CS_GB300_H
+#define CS_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CS_OK 0
+#define CS_ERR_INVALID 1   /* bad argument or size */
+#define CS_ERR_CUDA 2      /* CUDA runtime/driver failure */
+#define CS_ERR_NVRTC 3     /* run-time compilation of the problem failed */
+#define CS_ERR_NOMEM 4     /* device allocation failed */
+#define CS_ERR_STATE 5     /* call not valid in the batch's current state */
+
+/* per-instance status after cs_solve (matches the device state machine) */
+#define CS_STATUS_DONE 3
+#define CS_STATUS_FAIL 4
+
+typedef struct cs_module cs_module;
+typedef struct cs_batch cs_batch;
+
+/* A compiled problem for one number of collocation points m.  problem_src
+ * holds the CUDA device functions cs_f, cs_g, cs_Df, cs_Dg, cs_r, cs_Dr
+ * (emitted from the OCP derivation); the tables are the Lobatto IIIA tableau
+ * and the mesh-error quadrature for this m.
+ * Replaces: the numba JIT of the generated bvp_problem.py functions
+ * (OCP2ABVP.py:203-327) and of every CS/SB kernel. */
+typedef struct cs_module_desc {
+  const char* problem_src;
+  int ny, nz, np;       /* sizes of y, z, p */
+  int np_eff;           /* leading parameters that f, g depend on */
+  int n_theta;          /* instance constants */
+  int m;                /* collocation points, 2..10 */
+  const double* lobatto_A;  /* m*m */
+  const double* lobatto_b;  /* m */
+  const double* lobatto_c;  /* m */
+  const double* gauss_w;    /* m+1 */
+  const double* gauss_L;    /* (m+1)*m: L_k at the Gauss points */
+  const double* gauss_I;    /* (m+1)*m: integral of L_k at the Gauss points */
+  const double* L0;         /* m: L_k(0) */
+  const double* L1;         /* m: L_k(1) */
+  const char* cache_dir;    /* compiled-code cache directory, or NULL */
+} cs_module_desc;
+
+/* Compile (or load from the cache) and load the module on the current device. */
+int cs_module_load(const cs_module_desc* desc, cs_module** out);
+void cs_module_free(cs_module* mod);
+
+/* Solver options; the defaults (cs_opts_default) are the reference's
+ * (CS:58-76): alpha0 = 0.1, beta = 0.9, 20 line-search halvings, min 3 nodes. */
+typedef struct cs_opts {
+  double tol;            /* BvpDae.tolerance */
+  int max_iter;          /* BvpDae.maximum_newton_iterations */
+  int max_mesh;          /* BvpDae.maximum_mesh_refinements */
+  int max_nodes;         /* BvpDae.maximum_nodes */
+  int min_nodes;
+  int max_linesearch;
+  double alpha0;         /* initial continuation parameter */
+  double alpha_m;        /* final continuation parameter (0.1, or 1e-6 with inequalities) */
+  double beta;           /* continuation factor */
+  int check_every;       /* Newton super-steps between host checks for completion */
+} cs_opts;
+
+void cs_opts_default(cs_opts* o);
+
+/* Per-instance counters after a solve (the reference's benchmark counts). */
+typedef struct cs_stats {
+  int status;            /* CS_STATUS_DONE or CS_STATUS_FAIL */
+  int N;                 /* final number of nodes */
+  int newton_steps;      /* Jacobian evaluations ("Jacobian counts") */
+  int residual_evals;    /* "Residual counts" */
+  int segment_evals;     /* "Segment Residual counts" */
+  int remeshes;
+  int continuation_steps;
+  int singular;          /* singular pivots met */
+  int fail_reason;
+  double alpha;          /* final continuation parameter */
+  double max_residual;   /* last maximum segment residual */
+  double last_norm;      /* last residual infinity norm */
+} cs_stats;
+
+/* Device workspace for `batch` instances and up to node_capacity node slots
+ * in total (grown on demand by remeshing).  stream: a cudaStream_t, or NULL
+ * for a new stream owned by the batch. */
+int cs_batch_create(cs_module* mod, int batch, long long node_capacity, void* stream, cs_batch** out);
+void cs_batch_free(cs_batch* bt);
+
+/* Initial guess from HOST arrays: N[b] nodes, t (sum N), y (sum N x ny),
+ * z (sum N x nz) at the nodes, p (batch x np), theta (batch x n_theta, may be
+ * NULL when n_theta = 0); then forms the stage values (y' = f at the linearly
+ * interpolated stage points).
+ * Replaces: BvpDae.T0/Y0/Z0/P0 + form_initial_input_parallel (CS:287-356). */
+int cs_batch_set_guess(cs_batch* bt, const int* N, const double* t, const double* y, const double* z,
+                       const double* p, const double* theta);
+
+/* Full iterate from HOST arrays: nodes as in cs_batch_set_guess, and the
+ * stage values ydot ((N[b]-1) x m x ny per instance, packed) and zt
+ * ((N[b]-1) x m x nz per instance, packed), used as they are.
+ * Replaces: the (y, y_dot, z_tilde, p) arguments the reference passes to each
+ * stage function (e.g. compute_f_q_parallel, CS:399). */
+int cs_batch_set_state(cs_batch* bt, const int* N, const double* t, const double* y, const double* ydot,
+                       const double* zt, const double* p, const double* theta);
+
+/* Full solve of every instance: continuation, Newton with line search,
+ * segment residual, remesh.
+ * Replaces: collocation_solver_parallel (CS:36-251). */
+int cs_solve(cs_batch* bt, const cs_opts* opts);
+
+/* Current node counts (batch ints) and total node slots. */
+int cs_batch_sizes(cs_batch* bt, int* N_out, long long* total_out);
+
+/* Solution to HOST arrays sized by the current node counts (z recovered at the
+ * nodes); any pointer may be NULL.  stats: batch entries or NULL.
+ * Replaces: recover_solution_parallel (CS:2034-2075) and the arrays handed to
+ * bvpdae_write_data (CS:233-237). */
+int cs_get_solution(cs_batch* bt, double* t, double* y, double* z, double* p, cs_stats* stats);
+
+/* ---- stage entry points (one stage on the current iterate; host outputs) ---- */
+
+/* Residual at the current iterate: per-instance infinity norm; optionally the
+ * pieces f_a (slots x m(ny+nz)) and f_b (slots x ny), slot = node slot of the
+ * interval's left node.
+ * Replaces: compute_f_q_parallel (CS:399-512) + np.linalg.norm (CS:116). */
+int cs_stage_residual(cs_batch* bt, double alpha, double* norms, double* f_a, double* f_b);
+
+/* Newton direction at the current iterate: condensed blocks (slots x
+ * ny*(2ny+np_eff+1): A | C | H | b column-major, may be NULL), dy (nodes x
+ * ny), dydot (slots x m x ny), dzt (slots x m x nz), dp (batch x np).
+ * Replaces: construct_jacobian_parallel, reduce_jacobian_parallel (CS:611-1001),
+ * SB.partition_factorization_parallel, construct_babd_mshoot, qr_decomposition,
+ * backward_substitution, partition_backward_substitution_parallel (SB:93-572),
+ * recover_delta_k_parallel (CS:1580-1650). */
+int cs_stage_newton_direction(cs_batch* bt, double alpha, double* rows, double* dy, double* dydot, double* dzt,
+                              double* dp);
+
+/* Segment residual per node slot (interval residual / tol; the last node of
+ * each instance holds |r|_inf / tol) and the per-instance maximum.
+ * Replaces: compute_segment_residual_parallel (CS:1770-1892). */
+int cs_stage_segment_residual(cs_batch* bt, double alpha, double tol, double* res, double* max_res);
+
+/* Remesh every instance with the given per-node residuals (host, node
+ * slots), then re-form the stage values; N_new receives the new node counts.
+ * Replaces: recover_solution_parallel + remesh + form_initial_input_parallel
+ * (CS:194-198, 2034-2311). */
+int cs_stage_remesh(cs_batch* bt, const double* res, int* N_new);
+
+/* Current iterate to host: t, y (nodes), ydot, z~ (slots), z at nodes, p. */
+int cs_get_state(cs_batch* bt, double* t, double* y, double* ydot, double* zt, double* z_nodes, double* p);
+
+/* Message of this thread's last error ("" if none). */
+int cs_last_error(char* buf, size_t len);
+
+/* Time one launch of the condensation kernel on the current iterate, in
+ * milliseconds, with CUDA events on the batch's stream (for roofline figures). */
+int cs_time_condense(cs_batch* bt, int reps, double* ms);
+
+/* FP64 FMA throughput of this GPU, measured by a register-resident DFMA loop
+ * (TFLOP/s, counting an FMA as 2 flops); the denominator of FP64 roofline
+ * fractions. */
+int cs_measure_fp64_peak(double* tflops);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CS_GB300_H */

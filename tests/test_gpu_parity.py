@@ -1,0 +1,171 @@
+"""GPU parity: the CUDA path (through the C ABI) against the oracle and the
+golden fixtures of the reference.
+
+Tolerances: stage residual pieces and segment residuals 1e-12 relative (same
+formulas, different summation order); condensed blocks 1e-9 and Newton
+directions 1e-8 (different but stable factorizations: LU of the stage system
+is the same, the BABD system uses a tree of Householder merges instead of the
+reference's 8 sequential partitions); end-to-end solutions 1e-8 max-abs with
+identical Newton iteration counts, residual counts and final meshes.
+"""
+import numpy as np
+import pytest
+
+from conftest import golden, load_problem, oracle_problem, pkg
+from oracle import collocation_oracle as O
+
+pytestmark = pytest.mark.gpu
+
+STAGES = [("vdp_n21_m4", "vdp"), ("vdp_n33_m5", "vdp"), ("dint_n33_m3", "dint_param"),
+          ("pend2_n21_m5", "pend2"), ("econ_n17_m3", "eqcon")]
+E2E = [("vdp_cfg1", "vdp"), ("vdp_coarse", "vdp_coarse"), ("dint_param", "dint_param"),
+       ("pend2", "pend2"), ("vdp_ineq", "vdp_ineq")]
+
+
+@pytest.fixture(scope="module")
+def cs():
+    c = pkg()
+    c._lib.load()
+    return c
+
+
+_CP = {}
+
+
+def compiled(cs, name, m):
+    key = (name, m)
+    if key not in _CP:
+        pr = load_problem(name)
+        _CP[key] = cs.CompiledProblem(pr, m)
+    return _CP[key]
+
+
+def _batch_with_state(cs, cp, g):
+    bt = cs.Batch(cp, 1)
+    bt.set_state([(g["t"], g["y"], g["y_dot"], g["z_tilde"])], g["p"].reshape(1, -1))
+    return bt
+
+
+@pytest.mark.parametrize("case,prob", STAGES)
+def test_stage_residual(cs, case, prob):
+    g = golden("stage_" + case)
+    m, N = int(g["m"]), int(g["N"])
+    cp = compiled(cs, prob, m)
+    bt = _batch_with_state(cs, cp, g)
+    norms, fa, fb = bt.stage_residual(float(g["alpha"]), pieces=True)
+    P = oracle_problem(prob)
+    f_q, _, f_a, f_b, r_bc = O.compute_f_q(P, m, N, cs.tables.lobatto(m), g["t"], g["y"], g["y_dot"],
+                                           g["z_tilde"], g["p"], float(g["alpha"]))
+    np.testing.assert_allclose(fa[:N - 1], f_a, rtol=1e-12, atol=1e-12)
+    np.testing.assert_allclose(fb[:N - 1], f_b, rtol=1e-12, atol=1e-12)
+    assert abs(norms[0] - np.abs(f_q).max()) <= 1e-12 * max(1.0, np.abs(f_q).max())
+    # and the reference's own numbers
+    np.testing.assert_allclose(fa[:N - 1], g["f_a"], rtol=1e-11, atol=1e-11)
+
+
+@pytest.mark.parametrize("case,prob", STAGES)
+def test_stage_newton_direction(cs, case, prob):
+    g = golden("stage_" + case)
+    m, N = int(g["m"]), int(g["N"])
+    cp = compiled(cs, prob, m)
+    bt = _batch_with_state(cs, cp, g)
+    out = bt.stage_newton_direction(float(g["alpha"]))
+    ny, npe = cp.ny, cp.np_eff
+    rows = out["rows"][:N - 1].reshape(N - 1, 2 * ny + npe + 1, ny)  # column-major blocks
+    A = np.transpose(rows[:, :ny, :], (0, 2, 1))
+    C = np.transpose(rows[:, ny:2 * ny, :], (0, 2, 1))
+    H = np.transpose(rows[:, 2 * ny:2 * ny + npe, :], (0, 2, 1))
+    b = rows[:, 2 * ny + npe, :]
+    gA = g["A"].reshape(N - 1, ny, ny)
+    gH = g["H"].reshape(N - 1, ny, -1)
+    np.testing.assert_allclose(A, gA, rtol=1e-9, atol=1e-9)
+    np.testing.assert_allclose(C, np.broadcast_to(np.eye(ny), C.shape), atol=0)
+    np.testing.assert_allclose(H, gH[:, :, :npe], rtol=1e-9, atol=1e-9)
+    assert np.all(gH[:, :, npe:] == 0)
+    np.testing.assert_allclose(b, g["b"], rtol=1e-9, atol=1e-9)
+    # full Newton direction against the reference's (partitioned QR + recovery)
+    scale = max(1.0, np.abs(g["delta_y"]).max())
+    np.testing.assert_allclose(out["dy"][:N], g["delta_y"], rtol=0, atol=1e-8 * scale)
+    np.testing.assert_allclose(out["dp"][0], g["delta_p"], rtol=0, atol=1e-8 * scale)
+    dyd = out["dydot"][:N - 1].reshape((N - 1) * m, ny)
+    np.testing.assert_allclose(dyd, g["delta_y_dot"], rtol=0, atol=1e-8 * max(1.0, np.abs(g["delta_y_dot"]).max()))
+    if cp.nz:
+        dzt = out["dzt"][:N - 1].reshape((N - 1) * m, cp.nz)
+        np.testing.assert_allclose(dzt, g["delta_z_tilde"], rtol=0,
+                                   atol=1e-8 * max(1.0, np.abs(g["delta_z_tilde"]).max()))
+
+
+@pytest.mark.parametrize("case,prob", STAGES)
+def test_stage_segment_residual_and_remesh(cs, case, prob):
+    g = golden("stage_" + case)
+    m, N = int(g["m"]), int(g["N"])
+    cp = compiled(cs, prob, m)
+    bt = _batch_with_state(cs, cp, g)
+    res, mx = bt.stage_segment_residual(float(g["alpha"]), float(g["tol"]))
+    np.testing.assert_allclose(res[:N], g["seg_residual"], rtol=1e-11, atol=1e-12)
+    assert abs(mx[0] - float(g["seg_max"])) <= 1e-11 * abs(float(g["seg_max"]))
+    # remesh with the synthetic residual of the fixture: exact node arithmetic
+    Nn = bt.stage_remesh(g["remesh_residual"])
+    assert int(Nn[0]) == int(g["remesh_N"])
+    st = bt.state()
+    n = int(Nn[0])
+    np.testing.assert_array_equal(st["t"][:n], g["remesh_t"])
+    np.testing.assert_array_equal(st["y"][:n], g["remesh_y"])
+    # stage values formed on the new mesh (y' = f at interpolated points)
+    P = oracle_problem(prob)
+    _, yd, zt = O.form_initial_input(P, m, n, g["remesh_y"], g["remesh_z"], g["p"], cs.tables.lobatto(m))
+    np.testing.assert_allclose(st["ydot"][:n - 1].reshape(-1, cp.ny), yd, rtol=1e-12, atol=1e-12)
+    if cp.nz:
+        np.testing.assert_allclose(st["zt"][:n - 1].reshape(-1, cp.nz), zt, rtol=1e-12, atol=1e-12)
+
+
+@pytest.mark.parametrize("case,prob", E2E)
+def test_end_to_end_matches_reference(cs, case, prob):
+    g = golden("e2e_" + case)
+    m = int(g["m"])
+    pr = load_problem(prob)
+    sol = cs.solver.solve_single(pr, m)
+    assert sol["success"] == bool(g["success"])
+    assert sol["N"] == g["t"].shape[0]
+    assert sol["newton_steps"] == int(g["jacobian_counts"])
+    assert sol["residual_evals"] == int(g["residual_counts"])
+    assert sol["remeshes"] == len(g["nodes_after_remesh"])
+    np.testing.assert_array_equal(sol["t"], g["t"])
+    np.testing.assert_allclose(sol["y"], g["y"], atol=1e-8, rtol=0)
+    np.testing.assert_allclose(sol["z"], g["z"], atol=1e-8, rtol=0)
+    np.testing.assert_allclose(sol["p"], g["p"], atol=1e-8, rtol=0)
+    assert abs(sol["max_residual"] - float(g["max_residual"])) <= 1e-6 * max(1.0, float(g["max_residual"]))
+
+
+def test_batch_equals_independent_solves(cs):
+    """Instances of one batch (different initial conditions through the
+    constants, different meshes and final times) give the same results as the
+    oracle run on each instance alone."""
+    pr = load_problem("vdp_family")
+    m = 4
+    cp = compiled(cs, "vdp_family", m)
+    rng = np.random.default_rng(5)
+    B = 6
+    meshes, thetas = [], []
+    for b in range(B):
+        N = int(rng.integers(20, 60))
+        T = float(rng.uniform(2, 6))
+        t = np.linspace(0.0, T, N)
+        meshes.append((t, np.zeros((N, cp.ny)), np.zeros((N, cp.nz))))
+        thetas.append([rng.uniform(-1.5, 1.5), rng.uniform(-1.5, 1.5), float(np.exp(rng.uniform(np.log(0.3), np.log(3))))])
+    thetas = np.array(thetas)
+    bt = cs.Batch(cp, B)
+    bt.set_guess(meshes, np.ones((B, cp.np)), thetas)
+    bt.solve(cs.default_opts(pr, max_nodes=20000))
+    sols = bt.solution()
+    P = oracle_problem("vdp_family")
+    P.maximum_nodes = 20000
+    for b in range(B):
+        P.theta = thetas[b]
+        ref = O.solve(P, m, cs.tables.lobatto(m), cs.tables.segment_tables(m), T0=meshes[b][0], Y0=meshes[b][1],
+                      Z0=meshes[b][2], P0=np.ones(cp.np))
+        s = sols[b]
+        assert s["success"] == ref.success
+        assert s["N"] == ref.N and s["newton_steps"] == ref.jacobian_count and s["residual_evals"] == ref.residual_count
+        assert np.abs(s["y"] - ref.y).max() < 1e-8
+        assert np.abs(s["z"] - ref.z).max() < 1e-8
