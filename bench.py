@@ -1,0 +1,391 @@
+"""Benchmark: batched collocation solves per second to a 1e-6 residual on one
+GB300 (FP64), with the CPU oracle timed beside it.
+
+Workload (one "step"): the seeded Van der Pol batch — 4096 instances with
+x0 ~ U[-2,2]^2, T ~ U[2,8], r ~ logU[0.1,10], N ~ U{32..2048} intervals,
+m ~ U{3,4,5}, zero initial guess, tol 1e-6 — solved to completion (Newton,
+line search, segment residual, remesh) in one batch per m.
+
+  value  solves/s with the initial guesses resident in HBM (cs_batch_reset)
+  e2e    solves/s through the C ABI from pinned host buffers: initial guesses
+         H2D, solve, solutions D2H, every step inside the timed region
+
+Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+Under torchrun each rank solves its own batch (seed 1 + rank; weak scaling)
+and rank 0 prints one JSON line.
+"""
+import argparse
+import importlib
+import json
+import multiprocessing as mp
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+PKG = "collocation-solver-cuda_gb300"
+METRIC = "solves/sec to 1e-6 residual: NN-warm-started batched vs plain GPU, same GB300"
+BATCH = 4096
+SEED = 1
+
+
+def _pkg():
+    return importlib.import_module(PKG)
+
+
+# ------------------------------------------------------------ CPU oracle ---
+def _oracle_worker(args):
+    """Solve one instance with the CPU oracle (runs in a spawned process)."""
+    x0, T, r, intervals, m = args
+    os.environ.setdefault("OMP_NUM_THREADS", "1")
+    cs = _pkg()
+    from oracle import collocation_oracle as O
+    pr = cs.workloads.vdp_family_problem()
+
+    class P:
+        pass
+
+    op = P()
+    op.__dict__.update(pr.__dict__)
+    op.ny, op.nz, op.np = pr.size_y, pr.size_z, pr.size_p
+    nf = cs.codegen.NumpyProblem(cs.codegen.ProblemCode(pr.sym))
+    for k in ("f", "g", "Df", "Dg", "r", "Dr"):
+        setattr(op, k, getattr(nf, k))
+    op.theta = np.array([x0[0], x0[1], r])
+    inst = cs.workloads.VdpInstance(np.array(x0), T, r, intervals, m)
+    t, y, z, p = inst.guess()
+    res = O.solve(op, m, cs.tables.lobatto(m), cs.tables.segment_tables(m), T0=t, Y0=y, Z0=z, P0=p)
+    return res.success, res.N
+
+
+def cpu_oracle_rate(instances, procs, target_s=20.0, min_n=None):
+    """Solves/s of the oracle on a bounded sample, with `procs` processes."""
+    ctx = mp.get_context("spawn")
+    args = [(tuple(i.x0), i.T, i.r, i.intervals, i.m) for i in instances]
+    n = min_n or procs
+    with ctx.Pool(procs) as pool:
+        pool.map(_oracle_worker, args[:procs])  # import / codegen warm-up
+        t0 = time.time()
+        done = 0
+        while True:
+            chunk = args[done:done + n]
+            if not chunk:
+                break
+            pool.map(_oracle_worker, chunk)
+            done += len(chunk)
+            if time.time() - t0 > target_s:
+                break
+        dt = time.time() - t0
+    return done / dt, done, dt
+
+
+# --------------------------------------------------------------- clocks ---
+class ClockSampler:
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu=0):
+        self.gpu = gpu
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.QUERY,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([v.strip() for v in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in self.rows if len(r) > 8 and r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if len(r) > 8 and r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in self.rows:
+            for k, nm in enumerate(names):
+                if len(r) > 5 + k and r[5 + k].lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(self.rows)}
+
+
+# ------------------------------------------------------------ GPU batch ---
+class Workload:
+    """The batch split by m, one compiled problem and one Batch per group."""
+
+    def __init__(self, cs, instances):
+        self.cs = cs
+        self.problem = cs.workloads.vdp_family_problem()
+        self.groups = []
+        for m in sorted(set(i.m for i in instances)):
+            insts = [i for i in instances if i.m == m]
+            cp = cs.CompiledProblem(self.problem, m)
+            N, t, y, z, p, th = cs.workloads.pack_vdp(insts)
+            bt = cs.Batch(cp, len(insts), node_capacity=int(N.sum() * 2))
+            host = {}
+            for k, a in (("N", N), ("t", t), ("y", y), ("z", z), ("p", p), ("th", th)):
+                pa = cs.module.PinnedArray(a.shape, a.dtype)
+                pa.array[...] = a
+                host[k] = pa
+            cap = int(N.sum() * 4)
+            out = {k: cs.module.PinnedArray(shape) for k, shape in
+                   (("t", (cap,)), ("y", (cap, cp.ny)), ("z", (cap, max(cp.nz, 1))), ("p", (len(insts), cp.np)))}
+            bt.set_guess_packed(host["N"].array, host["t"].array, host["y"].array, host["z"].array,
+                                host["p"].array, host["th"].array)
+            self.groups.append(dict(m=m, insts=insts, cp=cp, bt=bt, host=host, out=out))
+        self.opts = cs.default_opts(self.problem, max_nodes=20000)
+        self.n = len(instances)
+
+    def _run_groups(self, fn):
+        errs = []
+
+        def wrap(g):
+            try:
+                fn(g)
+            except Exception as e:  # noqa: BLE001
+                errs.append(e)
+
+        ths = [threading.Thread(target=wrap, args=(g,)) for g in self.groups]
+        for t in ths:
+            t.start()
+        for t in ths:
+            t.join()
+        if errs:
+            raise errs[0]
+
+    def step_resident(self):
+        def f(g):
+            g["bt"].reset()
+            g["bt"].solve(self.opts)
+        self._run_groups(f)
+
+    def step_e2e(self):
+        def f(g):
+            h, o, bt = g["host"], g["out"], g["bt"]
+            bt.set_guess_packed(h["N"].array, h["t"].array, h["y"].array, h["z"].array, h["p"].array, h["th"].array)
+            bt.solve(self.opts)
+            N, T = bt.sizes()
+            if T > o["t"].array.shape[0]:
+                raise RuntimeError("solution larger than the pinned output buffers")
+            st = (self.cs._lib.Stats * bt.B)()
+            self.cs._lib.check(bt._lib.cs_get_solution(bt.handle, self.cs._lib.dptr(o["t"].array),
+                                                       self.cs._lib.dptr(o["y"].array), self.cs._lib.dptr(o["z"].array),
+                                                       self.cs._lib.dptr(o["p"].array), st), "cs_get_solution")
+            g["last_T"] = T
+            g["last_stats"] = st
+        self._run_groups(f)
+
+    def h2d_bytes(self):
+        return int(sum(sum(h.array.nbytes for h in g["host"].values()) for g in self.groups))
+
+    def d2h_bytes(self):
+        tot = 0
+        for g in self.groups:
+            T = g.get("last_T", 0)
+            cp = g["cp"]
+            tot += 8 * T * (1 + cp.ny + cp.nz) + 8 * g["bt"].B * cp.np + g["bt"].B * 64
+        return int(tot)
+
+    def results(self):
+        succ, newton, N = 0, 0, 0
+        for g in self.groups:
+            for s in g["bt"].solution():
+                succ += int(s["success"])
+                newton += s["newton_steps"]
+                N += s["N"]
+        return succ, newton, N
+
+
+def flops_per_interval(m, ny=4, nz=1, npe=0):
+    """Algorithmic FP64 flops of condensing one interval: (2/3) s^3 + 2 s^2 r,
+    s = m (ny + nz), r = ny + np_eff + 1 (LU of the stage system with r
+    right-hand sides and their back substitution)."""
+    s = m * (ny + nz)
+    r = ny + npe + 1
+    return 2.0 / 3.0 * s ** 3 + 2.0 * s * s * r
+
+
+def bytes_per_interval(m, ny=4, nz=1, npe=0):
+    """Algorithmic HBM bytes of condensing one interval: read t, y_i, y_{i+1},
+    y', z~; write X = W^-1 [J V f_a] and the block row [A C H b]."""
+    s = m * (ny + nz)
+    r = ny + npe + 1
+    return 8 * (2 + 2 * ny + m * (ny + nz) + r * s + ny * (2 * ny + npe + 1))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--batch", type=int, default=BATCH)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    cs = _pkg()
+    instances = cs.workloads.vdp_batch(args.batch, seed=SEED + rank)
+    cfg = {"workload": "Van der Pol batch: %d instances, x0~U[-2,2]^2, T~U[2,8], r~logU[0.1,10], N~U{32..2048} "
+                       "intervals, m~U{3,4,5}, zero guess, tol 1e-6 (seed %d + rank)" % (args.batch, SEED),
+           "batch_per_gpu": args.batch, "warm_start": "plain (zero initial guess)", "precision": "fp64",
+           "l2": "working set %s GB per step, larger than L2 (129 MB)"}
+    cores = os.cpu_count() or 1
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        # the reference's own CPU implementation of this path is Python; its
+        # restatement (oracle/collocation_oracle.py) runs here on all host cores
+        procs = cores
+        sample = instances[:]
+        rng = np.random.default_rng(7)
+        rng.shuffle(sample)
+        per_step = 2 * procs
+        ctx = mp.get_context("spawn")
+        a = [(tuple(i.x0), i.T, i.r, i.intervals, i.m) for i in sample]
+        with ctx.Pool(procs) as pool:
+            pool.map(_oracle_worker, a[:procs])
+            pos = 0
+            for _ in range(args.warmup):
+                pool.map(_oracle_worker, a[pos:pos + per_step])
+                pos += per_step
+            t0 = time.time()
+            for _ in range(args.steps):
+                pool.map(_oracle_worker, a[pos:pos + per_step])
+                pos += per_step
+            dt = time.time() - t0
+        v = args.steps * per_step / dt
+        cfg["l2"] = "n/a (CPU)"
+        line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "solves/s", "n_gpus": args.gpus,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * dt / args.steps,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic", "config": cfg,
+                "cpu_baseline": {"value": v, "unit": "solves/s", "cores": procs, "kind": "port",
+                                 "sample": "%d random instances of the batch per step, one per process" % per_step},
+                "e2e": {"value": v, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+
+    # CPU baseline first: its spawned pool starts before any GPU call
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        rng = np.random.default_rng(3)
+        idx = rng.permutation(len(instances))
+        sample = [instances[i] for i in idx]
+        rate, n, dt = cpu_oracle_rate(sample, cores, target_s=20.0)
+        cpu = {"value": rate, "unit": "solves/s", "cores": cores, "kind": "port",
+               "sample": "%d random instances of the batch solved by the oracle in %.1f s, one process per core"
+                         % (n, dt)}
+
+    dist = None
+    if world > 1:
+        import torch
+        import torch.distributed as tdist
+        tdist.init_process_group("gloo")
+        dist = tdist
+        os.environ["CUDA_VISIBLE_DEVICES"] = os.environ.get("CUDA_VISIBLE_DEVICES", str(local_rank))
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    def max_over_ranks(x):
+        if dist is None:
+            return x
+        import torch
+        t = torch.tensor([x], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    cs.build.build_library()
+    cs._lib.load()
+    fp64_peak = cs.module.measure_fp64_peak()
+    W = Workload(cs, instances)
+    ws_gb = sum(g["bt"].sizes()[1] for g in W.groups) * 8 * 300 / 1e9
+    cfg["l2"] = cfg["l2"] % ("%.1f" % ws_gb)
+
+    for _ in range(args.warmup):
+        W.step_resident()
+    for g in W.groups:
+        g["bt"].profile_reset(timing=True)
+    barrier()
+    with ClockSampler(local_rank) as clk:
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            W.step_resident()
+        dt = time.perf_counter() - t0
+    dt = max_over_ranks(dt)
+    succ, newton, nodes = W.results()
+    profs = [(g["m"], g["bt"].profile()) for g in W.groups]
+    value = world * args.steps * W.n / dt
+
+    # roofline of the dominant kernel (condensation), from the events of the timed region
+    flops = sum(p["intervals_condensed"] * flops_per_interval(m) for m, p in profs)
+    cbytes = sum(p["intervals_condensed"] * bytes_per_interval(m) for m, p in profs)
+    cms = sum(p["condense_ms"] for _, p in profs)
+    claunch = sum(p["condense_launches"] for _, p in profs)
+    launches = sum(p["launches"] for _, p in profs)
+    achieved = flops / (cms * 1e-3) / 1e12 if cms > 0 else 0.0
+    roof = {"bound": "fp64", "kernel": "k_condense", "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
+            "frac": achieved / fp64_peak if fp64_peak else None, "traffic": None,
+            "peak_source": "DFMA microbenchmark (cs_measure_fp64_peak) in this run; FP64 is absent from "
+                           "MEASURED_PEAKS.json",
+            "flops_per_launch": flops / max(claunch, 1), "ms_per_launch": cms / max(claunch, 1),
+            "hbm_gbs": cbytes / (cms * 1e-3) / 1e9 if cms > 0 else None,
+            "kernel_share": {"condense_ms": cms, "babd_ms": sum(p["babd_ms"] for _, p in profs),
+                             "residual_ms": sum(p["residual_ms"] for _, p in profs),
+                             "timed_region_ms": 1000 * dt}}
+
+    # end to end through the C ABI with pinned host buffers
+    for g in W.groups:
+        g["bt"].profile_reset(timing=False)
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        W.step_e2e()
+    dte = max_over_ranks(time.perf_counter() - t0)
+    e2e = {"value": world * args.steps * W.n / dte, "unit": "solves/s", "h2d_bytes_per_step": W.h2d_bytes(),
+           "d2h_bytes_per_step": W.d2h_bytes()}
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": 1000 * dt / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": cfg,
+                "e2e": e2e, "roofline": roof, "cpu_baseline": cpu, "clocks": clk.summary(),
+                "gpu_launches": int(launches),
+                "solve_stats": {"solved": succ, "of": W.n, "newton_steps_per_solve": newton / W.n,
+                                "final_nodes_per_solve": nodes / W.n}}
+        print(json.dumps(line))
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -39,6 +39,14 @@ class Stats(ctypes.Structure):
                 ("alpha", ctypes.c_double), ("max_residual", ctypes.c_double), ("last_norm", ctypes.c_double)]
 
 
+class Profile(ctypes.Structure):
+    _fields_ = [("launches", ctypes.c_longlong), ("super_steps", ctypes.c_longlong),
+                ("intervals_condensed", ctypes.c_longlong), ("systems_solved", ctypes.c_longlong),
+                ("residual_intervals", ctypes.c_longlong), ("condense_launches", ctypes.c_longlong),
+                ("babd_launches", ctypes.c_longlong), ("residual_launches", ctypes.c_longlong),
+                ("condense_ms", ctypes.c_double), ("babd_ms", ctypes.c_double), ("residual_ms", ctypes.c_double)]
+
+
 # every symbol declared in include/cs_gb300.h: name -> (restype, argtypes)
 SIGNATURES = {
     "cs_module_load": (ctypes.c_int, [ctypes.POINTER(ModuleDesc), ctypes.POINTER(ctypes.c_void_p)]),
@@ -60,6 +68,11 @@ SIGNATURES = {
     "cs_last_error": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_size_t]),
     "cs_time_condense": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _dp]),
     "cs_measure_fp64_peak": (ctypes.c_int, [_dp]),
+    "cs_batch_reset": (ctypes.c_int, [ctypes.c_void_p]),
+    "cs_profile_reset": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "cs_profile_get": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Profile)]),
+    "cs_pinned_alloc": (ctypes.c_void_p, [ctypes.c_size_t]),
+    "cs_pinned_free": (None, [ctypes.c_void_p]),
 }
 
 _lib = None

@@ -100,7 +100,8 @@ struct CsBatch {
   double* res;              // [T] segment residual per node
   double* znode;            // [T][NZ] z at nodes (remesh / initial input)
   CsInst* inst;             // [B]
-  int* counters;            // [8]
+  unsigned long long* counters;  // [0] instances in Newton this step, [1] intervals condensed,
+                                 // [2] BABD systems solved, [3] interval residuals evaluated
   double* fa_out;           // optional [T][S]: residual pieces (stage entry point)
   double* fb_out;           // optional [T][NY]
 };
@@ -279,6 +280,7 @@ extern "C" __global__ void k_decide(CsBatch bt, CsConsts c) {
   s.accepted = 0;
   s.need_jac = 0;
   if (s.status == ST_FRESH || s.status == ST_LS) {
+    atomicAdd(&bt.counters[3], (unsigned long long)(bt.N[b] - 1));
     double nt = cs_from_bits(s.norm_bits);
     s.norm_bits = 0ull;
     s.residual_count += 1;
@@ -294,7 +296,11 @@ extern "C" __global__ void k_decide(CsBatch bt, CsConsts c) {
       s.alpha_ls *= 0.5;
       if (s.ls_it >= c.max_ls) cs_iteration_start(s, bt.N[b], c, true);
     }
-    if (s.status == ST_FRESH || s.status == ST_LS || s.need_jac) atomicAdd(&bt.counters[0], 1);
+    if (s.status == ST_FRESH || s.status == ST_LS || s.need_jac) atomicAdd(&bt.counters[0], 1ull);
+    if (s.need_jac) {
+      atomicAdd(&bt.counters[1], (unsigned long long)(bt.N[b] - 1));
+      atomicAdd(&bt.counters[2], 1ull);
+    }
   }
   bt.inst[b] = s;
 }

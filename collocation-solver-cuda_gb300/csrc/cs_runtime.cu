@@ -121,7 +121,7 @@ struct CsBatchDev {
   double* res;
   double* znode;
   CsInst* inst;
-  int* counters;
+  unsigned long long* counters;
   double* fa_out;
   double* fb_out;
 };
@@ -413,6 +413,21 @@ struct cs_batch {
   DBuf inst_of, dy, dydot, dzt, X, rows0, rows1, tree, res;
   std::vector<int> hN, hoff;
   cs_opts opts;
+  // device copy of the last initial guess (cs_batch_reset)
+  DBuf iN, ioff, it, iy, iz, ip;
+  std::vector<int> ihN, ihoff;
+  int iT = 0;
+  // profiling
+  long long launches = 0, super_steps = 0;
+  bool timing = false;
+  struct EvPair {
+    cudaEvent_t a, b;
+    int kind;
+  };
+  std::vector<EvPair> ev_pool;
+  size_t ev_used = 0;
+  double kind_ms[3] = {0, 0, 0};
+  long long kind_launches[3] = {0, 0, 0};
 };
 
 static int dalloc(DBuf& b, size_t bytes) {
@@ -507,14 +522,49 @@ static CsBatchDev devview(cs_batch* bt) {
   v.res = (double*)bt->res.p;
   v.znode = (double*)bt->znode[s].p;
   v.inst = (CsInst*)bt->dinst.p;
-  v.counters = (int*)bt->dcounters.p;
+  v.counters = (unsigned long long*)bt->dcounters.p;
   return v;
 }
 
-static int launch(cs_batch* bt, CUfunction f, unsigned grid, unsigned block, size_t smem, void** args) {
-  if (grid == 0) return CS_OK;
-  CS_CU(g_drv.launchKernel(f, grid, 1, 1, block, 1, 1, (unsigned)smem, (CUstream)bt->stream, args, nullptr));
+static int flush_events(cs_batch* bt) {
+  if (bt->ev_used == 0) return CS_OK;
+  CS_CUDA(cudaStreamSynchronize(bt->stream));
+  for (size_t i = 0; i < bt->ev_used; ++i) {
+    float ms = 0.f;
+    CS_CUDA(cudaEventElapsedTime(&ms, bt->ev_pool[i].a, bt->ev_pool[i].b));
+    bt->kind_ms[bt->ev_pool[i].kind] += ms;
+  }
+  bt->ev_used = 0;
   return CS_OK;
+}
+
+// kind: -1 untimed, 0 condense, 1 babd, 2 residual
+static int launch_k(cs_batch* bt, CUfunction f, unsigned grid, unsigned block, size_t smem, void** args, int kind) {
+  if (grid == 0) return CS_OK;
+  cs_batch::EvPair* ev = nullptr;
+  if (bt->timing && kind >= 0) {
+    if (bt->ev_used == bt->ev_pool.size()) {
+      if (bt->ev_pool.size() >= 3072) CS_TRY(flush_events(bt));
+      if (bt->ev_used == bt->ev_pool.size()) {
+        cs_batch::EvPair e;
+        CS_CUDA(cudaEventCreate(&e.a));
+        CS_CUDA(cudaEventCreate(&e.b));
+        bt->ev_pool.push_back(e);
+      }
+    }
+    ev = &bt->ev_pool[bt->ev_used++];
+    ev->kind = kind;
+    CS_CUDA(cudaEventRecord(ev->a, bt->stream));
+  }
+  CS_CU(g_drv.launchKernel(f, grid, 1, 1, block, 1, 1, (unsigned)smem, (CUstream)bt->stream, args, nullptr));
+  bt->launches += 1;
+  if (kind >= 0) bt->kind_launches[kind] += 1;
+  if (ev) CS_CUDA(cudaEventRecord(ev->b, bt->stream));
+  return CS_OK;
+}
+
+static int launch(cs_batch* bt, CUfunction f, unsigned grid, unsigned block, size_t smem, void** args) {
+  return launch_k(bt, f, grid, block, smem, args, -1);
 }
 
 static unsigned cdiv(long long a, long long b) { return (unsigned)((a + b - 1) / b); }
@@ -530,18 +580,19 @@ static int run_condense(cs_batch* bt, CsBatchDev& v) {
   cs_module* M = bt->M;
   void* args[] = {&v};
   unsigned grid = (M->cgw == 1) ? cdiv(bt->T, M->condense_per_cta) : (unsigned)bt->T;
-  return launch(bt, M->f_condense, grid, M->condense_block, M->condense_smem, args);
+  return launch_k(bt, M->f_condense, grid, M->condense_block, M->condense_smem, args, 0);
 }
 
 static int run_babd(cs_batch* bt, CsBatchDev& v) {
   void* args[] = {&v};
-  return launch(bt, bt->M->f_babd, (unsigned)bt->B, bt->M->babd_block, bt->M->babd_smem, args);
+  return launch_k(bt, bt->M->f_babd, (unsigned)bt->B, bt->M->babd_block, bt->M->babd_smem, args, 1);
 }
 
 static int fill_inst_of(cs_batch* bt) {
   k_fill_inst_of<<<bt->B, 256, 0, bt->stream>>>(bt->B, (const int*)bt->doff.p, (const int*)bt->dN.p,
                                                   (int*)bt->inst_of.p);
   CS_CUDA(cudaGetLastError());
+  bt->launches += 1;
   return CS_OK;
 }
 
@@ -592,8 +643,13 @@ extern "C" void cs_batch_free(cs_batch* bt) {
   if (!bt) return;
   if (bt->stream) cudaStreamSynchronize(bt->stream);
   DBuf* all[] = {&bt->dN, &bt->doff, &bt->doff2, &bt->dp, &bt->dth, &bt->ddp, &bt->dinst, &bt->dcounters,
-                 &bt->inst_of, &bt->dy, &bt->dydot, &bt->dzt, &bt->X, &bt->rows0, &bt->rows1, &bt->tree, &bt->res};
+                 &bt->inst_of, &bt->dy, &bt->dydot, &bt->dzt, &bt->X, &bt->rows0, &bt->rows1, &bt->tree, &bt->res,
+                 &bt->iN, &bt->ioff, &bt->it, &bt->iy, &bt->iz, &bt->ip};
   for (DBuf* b : all) dfree(*b);
+  for (auto& e : bt->ev_pool) {
+    cudaEventDestroy(e.a);
+    cudaEventDestroy(e.b);
+  }
   for (int s = 0; s < 2; ++s) {
     dfree(bt->t[s]); dfree(bt->y[s]); dfree(bt->ydot[s]); dfree(bt->zt[s]); dfree(bt->znode[s]);
   }
@@ -636,6 +692,22 @@ extern "C" int cs_batch_set_guess(cs_batch* bt, const int* N, const double* t, c
   if (M->nz > 0) CS_CUDA(cudaMemcpyAsync(bt->znode[0].p, z, T * M->nz * d, cudaMemcpyHostToDevice, st));
   if (M->np > 0) CS_CUDA(cudaMemcpyAsync(bt->dp.p, p, (size_t)bt->B * M->np * d, cudaMemcpyHostToDevice, st));
   if (M->nth > 0) CS_CUDA(cudaMemcpyAsync(bt->dth.p, theta, (size_t)bt->B * M->nth * d, cudaMemcpyHostToDevice, st));
+  // device copy of the guess for cs_batch_reset
+  CS_TRY(dalloc(bt->iN, bt->B * sizeof(int)));
+  CS_TRY(dalloc(bt->ioff, bt->B * sizeof(int)));
+  CS_TRY(dalloc(bt->it, T * d));
+  CS_TRY(dalloc(bt->iy, T * M->ny * d));
+  CS_TRY(dalloc(bt->iz, T * std::max(M->nz, 1) * d));
+  CS_TRY(dalloc(bt->ip, (size_t)bt->B * std::max(M->np, 1) * d));
+  CS_CUDA(cudaMemcpyAsync(bt->iN.p, bt->dN.p, bt->B * sizeof(int), cudaMemcpyDeviceToDevice, st));
+  CS_CUDA(cudaMemcpyAsync(bt->ioff.p, bt->doff.p, bt->B * sizeof(int), cudaMemcpyDeviceToDevice, st));
+  CS_CUDA(cudaMemcpyAsync(bt->it.p, bt->t[0].p, T * d, cudaMemcpyDeviceToDevice, st));
+  CS_CUDA(cudaMemcpyAsync(bt->iy.p, bt->y[0].p, T * M->ny * d, cudaMemcpyDeviceToDevice, st));
+  if (M->nz > 0) CS_CUDA(cudaMemcpyAsync(bt->iz.p, bt->znode[0].p, T * M->nz * d, cudaMemcpyDeviceToDevice, st));
+  if (M->np > 0) CS_CUDA(cudaMemcpyAsync(bt->ip.p, bt->dp.p, (size_t)bt->B * M->np * d, cudaMemcpyDeviceToDevice, st));
+  bt->ihN = bt->hN;
+  bt->ihoff = bt->hoff;
+  bt->iT = (int)T;
   std::vector<CsInst> hi(bt->B);
   for (auto& s : hi) init_inst(s, bt->opts.alpha0);
   CS_CUDA(cudaMemcpyAsync(bt->dinst.p, hi.data(), hi.size() * sizeof(CsInst), cudaMemcpyHostToDevice, st));
@@ -713,7 +785,11 @@ static int write_inst(cs_batch* bt, const std::vector<CsInst>& hi) {
 static int super_step(cs_batch* bt, const CsConsts& c) {
   CsBatchDev v = devview(bt);
   cs_module* M = bt->M;
-  CS_TRY(run_slots(bt, M->f_residual, v));
+  {
+    void* args[] = {&v};
+    CS_TRY(launch_k(bt, M->f_residual, cdiv(bt->T, 256), 256, 0, args, 2));
+  }
+  bt->super_steps += 1;
   CsConsts cc = c;
   void* dargs[] = {&v, &cc};
   CS_TRY(run_insts(bt, M->f_decide, dargs));
@@ -784,8 +860,8 @@ extern "C" int cs_solve(cs_batch* bt, const cs_opts* opts) {
     s.alpha = o.alpha0;
   }
   CS_TRY(write_inst(bt, hi));
-  int* hcount = nullptr;
-  CS_CUDA(cudaMallocHost(&hcount, sizeof(int)));
+  unsigned long long* hcount = nullptr;
+  CS_CUDA(cudaMallocHost(&hcount, sizeof(unsigned long long)));
   int rc = CS_OK;
   const long long max_super = 1000000;
   long long steps = 0;
@@ -793,7 +869,7 @@ extern "C" int cs_solve(cs_batch* bt, const cs_opts* opts) {
     // ---- Newton phase
     for (;;) {
       for (int k = 0; k < o.check_every && rc == CS_OK; ++k) {
-        if (cudaMemsetAsync(bt->dcounters.p, 0, sizeof(int), bt->stream) != cudaSuccess) {
+        if (cudaMemsetAsync(bt->dcounters.p, 0, sizeof(unsigned long long), bt->stream) != cudaSuccess) {
           rc = set_err(CS_ERR_CUDA, "memset");
           break;
         }
@@ -801,7 +877,7 @@ extern "C" int cs_solve(cs_batch* bt, const cs_opts* opts) {
         ++steps;
       }
       if (rc != CS_OK) break;
-      if (cudaMemcpyAsync(hcount, bt->dcounters.p, sizeof(int), cudaMemcpyDeviceToHost, bt->stream) != cudaSuccess ||
+      if (cudaMemcpyAsync(hcount, bt->dcounters.p, sizeof(unsigned long long), cudaMemcpyDeviceToHost, bt->stream) != cudaSuccess ||
           cudaStreamSynchronize(bt->stream) != cudaSuccess) {
         rc = set_err(CS_ERR_CUDA, std::string("Newton phase: ") + cudaGetErrorString(cudaGetLastError()));
         break;
@@ -1065,6 +1141,83 @@ extern "C" int cs_measure_fp64_peak(double* tflops) {
   const double flops = 2.0 * 8.0 * iters * (double)grid * block;
   *tflops = flops / (t * 1e-3) / 1e12;
   return CS_OK;
+}
+
+extern "C" int cs_batch_reset(cs_batch* bt) {
+  if (!bt || !bt->have_guess || bt->iT == 0) return set_err(CS_ERR_STATE, "cs_batch_reset: no initial guess to restore");
+  cs_module* M = bt->M;
+  const size_t d = sizeof(double);
+  const long long T = bt->iT;
+  if (T > bt->cap) CS_TRY(alloc_slots(bt, T, false));
+  cudaStream_t st = bt->stream;
+  bt->cur = 0;
+  bt->T = (int)T;
+  bt->hN = bt->ihN;
+  bt->hoff = bt->ihoff;
+  CS_CUDA(cudaMemcpyAsync(bt->dN.p, bt->iN.p, bt->B * sizeof(int), cudaMemcpyDeviceToDevice, st));
+  CS_CUDA(cudaMemcpyAsync(bt->doff.p, bt->ioff.p, bt->B * sizeof(int), cudaMemcpyDeviceToDevice, st));
+  CS_CUDA(cudaMemcpyAsync(bt->t[0].p, bt->it.p, T * d, cudaMemcpyDeviceToDevice, st));
+  CS_CUDA(cudaMemcpyAsync(bt->y[0].p, bt->iy.p, T * M->ny * d, cudaMemcpyDeviceToDevice, st));
+  if (M->nz > 0) CS_CUDA(cudaMemcpyAsync(bt->znode[0].p, bt->iz.p, T * M->nz * d, cudaMemcpyDeviceToDevice, st));
+  if (M->np > 0) CS_CUDA(cudaMemcpyAsync(bt->dp.p, bt->ip.p, (size_t)bt->B * M->np * d, cudaMemcpyDeviceToDevice, st));
+  std::vector<CsInst> hi(bt->B);
+  for (auto& s : hi) init_inst(s, bt->opts.alpha0);
+  CS_CUDA(cudaMemcpyAsync(bt->dinst.p, hi.data(), hi.size() * sizeof(CsInst), cudaMemcpyHostToDevice, st));
+  CS_TRY(fill_inst_of(bt));
+  CsBatchDev v = devview(bt);
+  int only = -1;
+  void* args[] = {&v, &only};
+  CS_TRY(launch(bt, M->f_form_initial, cdiv(bt->T, 256), 256, 0, args));
+  CS_CUDA(cudaStreamSynchronize(st));
+  return CS_OK;
+}
+
+extern "C" int cs_profile_reset(cs_batch* bt, int timing) {
+  if (!bt) return set_err(CS_ERR_INVALID, "cs_profile_reset: null batch");
+  CS_TRY(flush_events(bt));
+  bt->launches = bt->super_steps = 0;
+  for (int k = 0; k < 3; ++k) {
+    bt->kind_ms[k] = 0;
+    bt->kind_launches[k] = 0;
+  }
+  bt->timing = timing != 0;
+  CS_CUDA(cudaMemsetAsync(bt->dcounters.p, 0, 8 * sizeof(unsigned long long), bt->stream));
+  CS_CUDA(cudaStreamSynchronize(bt->stream));
+  return CS_OK;
+}
+
+extern "C" int cs_profile_get(cs_batch* bt, cs_profile* out) {
+  if (!bt || !out) return set_err(CS_ERR_INVALID, "cs_profile_get: null argument");
+  CS_TRY(flush_events(bt));
+  unsigned long long c[8];
+  CS_CUDA(cudaMemcpyAsync(c, bt->dcounters.p, sizeof(c), cudaMemcpyDeviceToHost, bt->stream));
+  CS_CUDA(cudaStreamSynchronize(bt->stream));
+  out->launches = bt->launches;
+  out->super_steps = bt->super_steps;
+  out->intervals_condensed = (long long)c[1];
+  out->systems_solved = (long long)c[2];
+  out->residual_intervals = (long long)c[3];
+  out->condense_launches = bt->kind_launches[0];
+  out->babd_launches = bt->kind_launches[1];
+  out->residual_launches = bt->kind_launches[2];
+  out->condense_ms = bt->kind_ms[0];
+  out->babd_ms = bt->kind_ms[1];
+  out->residual_ms = bt->kind_ms[2];
+  return CS_OK;
+}
+
+extern "C" void* cs_pinned_alloc(size_t bytes) {
+  if (ensure_context() != CS_OK) return nullptr;
+  void* p = nullptr;
+  if (cudaMallocHost(&p, bytes ? bytes : 8) != cudaSuccess) {
+    set_err(CS_ERR_NOMEM, "cudaMallocHost failed");
+    return nullptr;
+  }
+  return p;
+}
+
+extern "C" void cs_pinned_free(void* p) {
+  if (p) cudaFreeHost(p);
 }
 
 extern "C" int cs_last_error(char* buf, size_t len) {

@@ -170,6 +170,18 @@ class Batch:
         _lib.check(self._lib.cs_batch_set_state(self.handle, _lib.iptr(N), _lib.dptr(t), _lib.dptr(y), _lib.dptr(yd),
                                                 _lib.dptr(zt), _lib.dptr(p), _lib.dptr(th)), "cs_batch_set_state")
 
+    def reset(self):
+        """Back to the last initial guess (device copy, no host transfer)."""
+        _lib.check(self._lib.cs_batch_reset(self.handle), "cs_batch_reset")
+
+    def profile_reset(self, timing=False):
+        _lib.check(self._lib.cs_profile_reset(self.handle, int(bool(timing))), "cs_profile_reset")
+
+    def profile(self):
+        pr = _lib.Profile()
+        _lib.check(self._lib.cs_profile_get(self.handle, ctypes.byref(pr)), "cs_profile_get")
+        return {k: getattr(pr, k) for k, _ in _lib.Profile._fields_}
+
     # ---- solve
     def solve(self, opts=None):
         o = opts if opts is not None else default_opts(self.cp.problem)
@@ -265,6 +277,28 @@ class Batch:
         ms = ctypes.c_double()
         _lib.check(self._lib.cs_time_condense(self.handle, int(reps), ctypes.byref(ms)), "cs_time_condense")
         return ms.value
+
+
+class PinnedArray:
+    """numpy array over page-locked host memory (freed with the object)."""
+
+    def __init__(self, shape, dtype=np.float64):
+        lib = _lib.load()
+        self._lib = lib
+        n = int(np.prod(shape)) * np.dtype(dtype).itemsize
+        self.ptr = lib.cs_pinned_alloc(max(n, 8))
+        if not self.ptr:
+            raise _lib.CsError("pinned allocation failed: " + _lib.last_error())
+        buf = (ctypes.c_char * max(n, 8)).from_address(self.ptr)
+        self.array = np.frombuffer(buf, dtype=dtype, count=int(np.prod(shape))).reshape(shape)
+
+    def __del__(self):
+        try:
+            if self.ptr:
+                self._lib.cs_pinned_free(self.ptr)
+                self.ptr = None
+        except Exception:  # noqa: BLE001
+            pass
 
 
 def measure_fp64_peak():

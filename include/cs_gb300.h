@@ -170,6 +170,31 @@ int cs_stage_remesh(cs_batch* bt, const double* res, int* N_new);
 /* Current iterate to host: t, y (nodes), ydot, z~ (slots), z at nodes, p. */
 int cs_get_state(cs_batch* bt, double* t, double* y, double* ydot, double* zt, double* z_nodes, double* p);
 
+/* Restore the initial guess given to the last cs_batch_set_guess from its
+ * device copy (no host transfer) and re-form the stage values: lets a caller
+ * re-solve the same batch with inputs already resident in HBM. */
+int cs_batch_reset(cs_batch* bt);
+
+/* Work and timing counters of a batch since the last cs_profile_reset.
+ * With timing on, the condensation, BABD and residual launches are bracketed
+ * by CUDA events on the batch's stream. */
+typedef struct cs_profile {
+  long long launches;             /* kernel launches issued by the library */
+  long long super_steps;          /* Newton super-steps */
+  long long intervals_condensed;  /* interval condensations (units of k_condense) */
+  long long systems_solved;       /* BABD solves (units of k_babd) */
+  long long residual_intervals;   /* interval residual evaluations */
+  long long condense_launches, babd_launches, residual_launches;
+  double condense_ms, babd_ms, residual_ms;  /* summed event times (timing on) */
+} cs_profile;
+
+int cs_profile_reset(cs_batch* bt, int timing);
+int cs_profile_get(cs_batch* bt, cs_profile* out);
+
+/* Page-locked host memory for the host arrays of the calls above. */
+void* cs_pinned_alloc(size_t bytes);
+void cs_pinned_free(void* p);
+
 /* Message of this thread's last error ("" if none). */
 int cs_last_error(char* buf, size_t len);
 
