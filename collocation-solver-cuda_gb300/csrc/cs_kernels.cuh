@@ -32,9 +32,11 @@
 //                    assembly and norm                 collocation_solver_parallel_2d_shared.py:399-559, 116
 //   k_condense       construct_jacobian_kernel + reduce_jacobian_parallel_kernel
 //                                                      collocation_solver_parallel_2d_shared.py:680-1001
-//   k_babd           partition_factorization_kernel, the host reduced solve,
+//   k_tree_level, k_top, k_backsub_level, k_recover
+//                    partition_factorization_kernel, the host reduced solve,
 //                    partition_backward_substitution_kernel, recover_delta_k_kernel
 //                                                      solve_babd_system.py:161-572, collocation_solver_parallel_2d_shared.py:1619-1650
+//   k_lists          (none: compacts the work of the batch every super-step)
 //   k_decide/k_accept  Newton loop and line search    collocation_solver_parallel_2d_shared.py:105-180
 //   k_segres         compute_segment_residual_kernel   collocation_solver_parallel_2d_shared.py:1833-1892
 //   k_remesh_*       recover_solution_kernel + remesh  collocation_solver_parallel_2d_shared.py:2049-2311
@@ -104,7 +106,19 @@ struct CsBatch {
                                  // [2] BABD systems solved, [3] interval residuals evaluated
   double* fa_out;           // optional [T][S]: residual pieces (stage entry point)
   double* fb_out;           // optional [T][NY]
+  // work lists, rebuilt by k_lists every super-step: only the instances that
+  // have work are visited, so a batch whose stragglers are few costs little
+  int* act;                 // [B] instances that need a residual evaluation
+  int* jac;                 // [B] instances that need a Newton direction
+  int* acc;                 // [B] instances whose line-search trial was accepted
+  long long* act_pre;       // [B+1] prefix of their interval counts
+  long long* jac_pre;       // [B+1] prefix of interval counts
+  long long* acc_pre;       // [B+1] prefix of node counts
+  long long* lvl_pre;       // [CS_MAXLVL][B+1] prefix of tree items per level over jac
+  int* nlist;               // [4] nact, njac, nacc, -
 };
+
+#define CS_MAXLVL 32
 
 static constexpr double CS_EPS = 2.220446049250313e-16;
 
@@ -122,6 +136,33 @@ __device__ __forceinline__ void cs_warp_max_atomic(unsigned long long* dst, int 
   const unsigned mlo = __reduce_max_sync(peers, hi == mhi ? lo : 0u);
   const int leader = __ffs(peers) - 1;
   if (active && (int)(threadIdx.x & 31) == leader) atomicMax(dst, ((unsigned long long)mhi << 32) | mlo);
+}
+
+// first k with pre[k] <= w < pre[k+1] (pre ascending, n entries + total)
+__device__ __forceinline__ int cs_find(const long long* pre, int n, long long w) {
+  int lo = 0, hi = n - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (pre[mid] <= w) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+// block rows at tree level l for n0 rows at level 0 (each level halves, rounding up)
+__device__ __forceinline__ int cs_rows_at(int n0, int l) {
+  int n = n0;
+  for (int q = 0; q < l; ++q) n = (n + 1) >> 1;
+  return n;
+}
+__device__ __forceinline__ int cs_levels(int n0) {
+  int L = 0, n = n0;
+  while (n > 1) { n = (n + 1) >> 1; ++L; }
+  return L;
+}
+// items of tree level l: ceil(n_l / 2) (merges plus the carried odd row)
+__device__ __forceinline__ long long cs_level_items(int n0, int l) {
+  int n = cs_rows_at(n0, l);
+  return n > 1 ? (long long)((n + 1) >> 1) : 0ll;
 }
 
 // ------------------------------------------------------------------------
@@ -161,95 +202,102 @@ extern "C" __global__ void k_form_initial(CsBatch bt, int only_status) {
 // (FRESH): collocation update, f_a = [f(y~,z~,p) - y'; g], f_b and, on
 // interval 0, the boundary conditions.
 extern "C" __global__ void k_residual(CsBatch bt) {
-  int slot = blockIdx.x * blockDim.x + threadIdx.x;
-  bool active = slot < bt.T;
-  int b = 0, i = 0;
-  if (active) {
-    b = bt.inst_of[slot];
-    i = slot - bt.off[b];
-    active = i < bt.N[b] - 1;
-  }
-  int st = active ? bt.inst[b].status : -1;
-  active = active && (st == ST_FRESH || st == ST_LS);
-  unsigned long long nb = 0;
-  if (active) {
-    const bool ls = (st == ST_LS);
-    const double a = ls ? bt.inst[b].alpha_ls : 0.0;
-    const double* th = bt.th + (size_t)b * (CS_NTH > 0 ? CS_NTH : 1);
-    double pl[CS_NP > 0 ? CS_NP : 1];
-    for (int k = 0; k < CS_NP; ++k) {
-      double v = bt.p[(size_t)b * CS_NP + k];
-      pl[k] = ls ? fma(a, bt.dp[(size_t)b * CS_NP + k], v) : v;
+  const int nact = bt.nlist[0];
+  const long long total = bt.act_pre[nact];
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long base = (long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < total; base += stride) {
+    const long long w = base + (threadIdx.x & 31);
+    bool active = w < total;
+    int b = 0, i = 0, slot = 0, st = -1;
+    if (active) {
+      const int k = cs_find(bt.act_pre, nact, w);
+      b = bt.act[k];
+      i = (int)(w - bt.act_pre[k]);
+      slot = bt.off[b] + i;
+      st = bt.inst[b].status;
+      active = (st == ST_FRESH || st == ST_LS);
     }
-    double yi[CS_NY], yi1[CS_NY];
-    for (int k = 0; k < CS_NY; ++k) {
-      double v0 = bt.y[(size_t)slot * CS_NY + k], v1 = bt.y[(size_t)(slot + 1) * CS_NY + k];
-      yi[k] = ls ? fma(a, bt.dy[(size_t)slot * CS_NY + k], v0) : v0;
-      yi1[k] = ls ? fma(a, bt.dy[(size_t)(slot + 1) * CS_NY + k], v1) : v1;
-    }
-    double yd[CS_M][CS_NY];
-    for (int j = 0; j < CS_M; ++j)
-      for (int k = 0; k < CS_NY; ++k) {
-        size_t q = ((size_t)slot * CS_M + j) * CS_NY + k;
-        yd[j][k] = ls ? fma(a, bt.dydot[q], bt.ydot[q]) : bt.ydot[q];
+    unsigned long long nb = 0;
+    if (active) {
+      const bool ls = (st == ST_LS);
+      const double a = ls ? bt.inst[b].alpha_ls : 0.0;
+      const double* th = bt.th + (size_t)b * (CS_NTH > 0 ? CS_NTH : 1);
+      double pl[CS_NP > 0 ? CS_NP : 1];
+      for (int k = 0; k < CS_NP; ++k) {
+        double v = bt.p[(size_t)b * CS_NP + k];
+        pl[k] = ls ? fma(a, bt.dp[(size_t)b * CS_NP + k], v) : v;
       }
-    const double h = bt.t[slot + 1] - bt.t[slot];
-    double mx = 0.0;
-    bool nan = false;
-#pragma unroll 1
-    for (int j = 0; j < CS_M; ++j) {
-      double yt[CS_NY], zl[CS_NZ > 0 ? CS_NZ : 1], f[CS_NY];
+      double yi[CS_NY], yi1[CS_NY];
+      for (int k = 0; k < CS_NY; ++k) {
+        double v0 = bt.y[(size_t)slot * CS_NY + k], v1 = bt.y[(size_t)(slot + 1) * CS_NY + k];
+        yi[k] = ls ? fma(a, bt.dy[(size_t)slot * CS_NY + k], v0) : v0;
+        yi1[k] = ls ? fma(a, bt.dy[(size_t)(slot + 1) * CS_NY + k], v1) : v1;
+      }
+      double yd[CS_M][CS_NY];
+      for (int j = 0; j < CS_M; ++j)
+        for (int k = 0; k < CS_NY; ++k) {
+          size_t q = ((size_t)slot * CS_M + j) * CS_NY + k;
+          yd[j][k] = ls ? fma(a, bt.dydot[q], bt.ydot[q]) : bt.ydot[q];
+        }
+      const double h = bt.t[slot + 1] - bt.t[slot];
+      double mx = 0.0;
+      bool nan = false;
+  #pragma unroll 1
+      for (int j = 0; j < CS_M; ++j) {
+        double yt[CS_NY], zl[CS_NZ > 0 ? CS_NZ : 1], f[CS_NY];
+        for (int k = 0; k < CS_NY; ++k) {
+          double s = 0.0;
+          for (int q = 0; q < CS_M; ++q) s += CS_A[j * CS_M + q] * yd[q][k];
+          yt[k] = yi[k] + h * s;
+        }
+        for (int k = 0; k < CS_NZ; ++k) {
+          size_t q = ((size_t)slot * CS_M + j) * CS_NZ + k;
+          zl[k] = ls ? fma(a, bt.dzt[q], bt.zt[q]) : bt.zt[q];
+        }
+        cs_f(yt, zl, pl, th, f);
+        for (int k = 0; k < CS_NY; ++k) {
+          double r = f[k] - yd[j][k];
+          nan |= (r != r);
+          mx = fmax(mx, fabs(r));
+          if (bt.fa_out) bt.fa_out[(size_t)slot * CS_S + j * (CS_NY + CS_NZ) + k] = r;
+        }
+  #if CS_NZ > 0
+        double g[CS_NZ];
+        cs_g(yt, zl, pl, th, bt.inst[b].alpha, g);
+        for (int k = 0; k < CS_NZ; ++k) {
+          nan |= (g[k] != g[k]);
+          mx = fmax(mx, fabs(g[k]));
+          if (bt.fa_out) bt.fa_out[(size_t)slot * CS_S + j * (CS_NY + CS_NZ) + CS_NY + k] = g[k];
+        }
+  #endif
+      }
       for (int k = 0; k < CS_NY; ++k) {
         double s = 0.0;
-        for (int q = 0; q < CS_M; ++q) s += CS_A[j * CS_M + q] * yd[q][k];
-        yt[k] = yi[k] + h * s;
-      }
-      for (int k = 0; k < CS_NZ; ++k) {
-        size_t q = ((size_t)slot * CS_M + j) * CS_NZ + k;
-        zl[k] = ls ? fma(a, bt.dzt[q], bt.zt[q]) : bt.zt[q];
-      }
-      cs_f(yt, zl, pl, th, f);
-      for (int k = 0; k < CS_NY; ++k) {
-        double r = f[k] - yd[j][k];
+        for (int j = 0; j < CS_M; ++j) s += CS_B[j] * yd[j][k];
+        double r = yi1[k] - yi[k] - h * s;
         nan |= (r != r);
         mx = fmax(mx, fabs(r));
-        if (bt.fa_out) bt.fa_out[(size_t)slot * CS_S + j * (CS_NY + CS_NZ) + k] = r;
+        if (bt.fb_out) bt.fb_out[(size_t)slot * CS_NY + k] = r;
       }
-#if CS_NZ > 0
-      double g[CS_NZ];
-      cs_g(yt, zl, pl, th, bt.inst[b].alpha, g);
-      for (int k = 0; k < CS_NZ; ++k) {
-        nan |= (g[k] != g[k]);
-        mx = fmax(mx, fabs(g[k]));
-        if (bt.fa_out) bt.fa_out[(size_t)slot * CS_S + j * (CS_NY + CS_NZ) + CS_NY + k] = g[k];
+      if (i == 0) {
+        int last = bt.off[b] + bt.N[b] - 1;
+        double ya[CS_NY], yb[CS_NY], r[CS_NY + CS_NP];
+        for (int k = 0; k < CS_NY; ++k) {
+          double v0 = bt.y[(size_t)slot * CS_NY + k], v1 = bt.y[(size_t)last * CS_NY + k];
+          ya[k] = ls ? fma(a, bt.dy[(size_t)slot * CS_NY + k], v0) : v0;
+          yb[k] = ls ? fma(a, bt.dy[(size_t)last * CS_NY + k], v1) : v1;
+        }
+        cs_r(ya, yb, pl, th, r);
+        for (int k = 0; k < CS_NY + CS_NP; ++k) {
+          nan |= (r[k] != r[k]);
+          mx = fmax(mx, fabs(r[k]));
+        }
       }
-#endif
+      nb = nan ? 0x7ff8000000000000ull : cs_abs_bits(mx);
     }
-    for (int k = 0; k < CS_NY; ++k) {
-      double s = 0.0;
-      for (int j = 0; j < CS_M; ++j) s += CS_B[j] * yd[j][k];
-      double r = yi1[k] - yi[k] - h * s;
-      nan |= (r != r);
-      mx = fmax(mx, fabs(r));
-      if (bt.fb_out) bt.fb_out[(size_t)slot * CS_NY + k] = r;
-    }
-    if (i == 0) {
-      int last = bt.off[b] + bt.N[b] - 1;
-      double ya[CS_NY], yb[CS_NY], r[CS_NY + CS_NP];
-      for (int k = 0; k < CS_NY; ++k) {
-        double v0 = bt.y[(size_t)slot * CS_NY + k], v1 = bt.y[(size_t)last * CS_NY + k];
-        ya[k] = ls ? fma(a, bt.dy[(size_t)slot * CS_NY + k], v0) : v0;
-        yb[k] = ls ? fma(a, bt.dy[(size_t)last * CS_NY + k], v1) : v1;
-      }
-      cs_r(ya, yb, pl, th, r);
-      for (int k = 0; k < CS_NY + CS_NP; ++k) {
-        nan |= (r[k] != r[k]);
-        mx = fmax(mx, fabs(r[k]));
-      }
-    }
-    nb = nan ? 0x7ff8000000000000ull : cs_abs_bits(mx);
+
+    cs_warp_max_atomic(active ? &bt.inst[b].norm_bits : nullptr, b, nb, active);
   }
-  cs_warp_max_atomic(active ? &bt.inst[b].norm_bits : nullptr, b, nb, active);
 }
 
 // ------------------------------------------------------------------------
@@ -305,27 +353,111 @@ extern "C" __global__ void k_decide(CsBatch bt, CsConsts c) {
   bt.inst[b] = s;
 }
 
-// x += alpha_ls * dx for instances whose trial was accepted
+// x += alpha_ls * dx for instances whose trial was accepted (items: their nodes)
 extern "C" __global__ void k_accept(CsBatch bt) {
-  int slot = blockIdx.x * blockDim.x + threadIdx.x;
-  if (slot >= bt.T) return;
-  int b = bt.inst_of[slot];
-  if (!bt.inst[b].accepted) return;
-  int i = slot - bt.off[b];
-  int N = bt.N[b];
-  double a = bt.inst[b].alpha_ls;
-  for (int k = 0; k < CS_NY; ++k) bt.y[(size_t)slot * CS_NY + k] = fma(a, bt.dy[(size_t)slot * CS_NY + k], bt.y[(size_t)slot * CS_NY + k]);
-  if (i >= N - 1) return;
-  for (int q = 0; q < CS_M * CS_NY; ++q) {
-    size_t o = (size_t)slot * CS_M * CS_NY + q;
-    bt.ydot[o] = fma(a, bt.dydot[o], bt.ydot[o]);
+  const int nacc = bt.nlist[2];
+  const long long total = bt.acc_pre[nacc];
+  for (long long w = (long long)blockIdx.x * blockDim.x + threadIdx.x; w < total; w += (long long)gridDim.x * blockDim.x) {
+    const int k = cs_find(bt.acc_pre, nacc, w);
+    const int b = bt.acc[k];
+    const int i = (int)(w - bt.acc_pre[k]);
+    const int slot = bt.off[b] + i;
+    const int N = bt.N[b];
+    const double a = bt.inst[b].alpha_ls;
+    for (int q = 0; q < CS_NY; ++q) bt.y[(size_t)slot * CS_NY + q] = fma(a, bt.dy[(size_t)slot * CS_NY + q], bt.y[(size_t)slot * CS_NY + q]);
+    if (i >= N - 1) continue;
+    for (int q = 0; q < CS_M * CS_NY; ++q) {
+      size_t o = (size_t)slot * CS_M * CS_NY + q;
+      bt.ydot[o] = fma(a, bt.dydot[o], bt.ydot[o]);
+    }
+    for (int q = 0; q < CS_M * CS_NZ; ++q) {
+      size_t o = (size_t)slot * CS_M * CS_NZ + q;
+      bt.zt[o] = fma(a, bt.dzt[o], bt.zt[o]);
+    }
+    if (i == 0)
+      for (int q = 0; q < CS_NP; ++q) bt.p[(size_t)b * CS_NP + q] = fma(a, bt.dp[(size_t)b * CS_NP + q], bt.p[(size_t)b * CS_NP + q]);
   }
-  for (int q = 0; q < CS_M * CS_NZ; ++q) {
-    size_t o = (size_t)slot * CS_M * CS_NZ + q;
-    bt.zt[o] = fma(a, bt.dzt[o], bt.zt[o]);
+}
+
+// ------------------------------------------------------------------------
+// Work lists.  One CTA of 1024 threads scans the instances:
+//   mode 0: act = instances in FRESH or LS; jac, acc empty
+//   mode 1: (after k_decide) act = FRESH/LS or needing a Jacobian, jac =
+//           needing a Jacobian, acc = accepted trials; plus, for each tree
+//           level l < nlvl, the prefix of that level's items over jac.
+__device__ long long cs_block_scan(long long v, long long* sh, long long* total) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  long long x = v;
+  for (int o = 1; o < 32; o <<= 1) {
+    long long y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
   }
-  if (i == 0)
-    for (int k = 0; k < CS_NP; ++k) bt.p[(size_t)b * CS_NP + k] = fma(a, bt.dp[(size_t)b * CS_NP + k], bt.p[(size_t)b * CS_NP + k]);
+  if (lane == 31) sh[w] = x;
+  __syncthreads();
+  if (w == 0) {
+    long long q = (lane < nw) ? sh[lane] : 0ll;
+    for (int o = 1; o < 32; o <<= 1) {
+      long long y = __shfl_up_sync(0xffffffffu, q, o);
+      if (lane >= o) q += y;
+    }
+    if (lane < nw) sh[lane] = q;
+  }
+  __syncthreads();
+  const long long excl = x - v + (w > 0 ? sh[w - 1] : 0ll);
+  *total = sh[nw - 1];
+  __syncthreads();
+  return excl;
+}
+
+template <typename F, typename Wt>
+__device__ int cs_build_list(int n, F flag, Wt weight, int* list, long long* pre, long long* sh) {
+  long long cpos = 0, cw = 0;
+  for (int base = 0; base < n; base += blockDim.x) {
+    const int b = base + threadIdx.x;
+    const int f = (b < n && flag(b)) ? 1 : 0;
+    const long long wv = f ? weight(b) : 0ll;
+    long long tf, tw;
+    const long long pf = cs_block_scan((long long)f, sh, &tf);
+    const long long pw = cs_block_scan(wv, sh, &tw);
+    if (f) {
+      if (list) list[cpos + pf] = b;
+      pre[cpos + pf] = cw + pw;
+    }
+    cpos += tf;
+    cw += tw;
+  }
+  if (threadIdx.x == 0) pre[cpos] = cw;
+  __syncthreads();
+  return (int)cpos;
+}
+
+extern "C" __global__ void k_lists(CsBatch bt, int mode, int nlvl) {
+  __shared__ long long sh[32];
+  const int B = bt.B;
+  const CsInst* I = bt.inst;
+  const int* N = bt.N;
+  int nact, njac = 0, nacc = 0;
+  if (mode == 0) {
+    nact = cs_build_list(B, [&](int b) { int st = I[b].status; return st == ST_FRESH || st == ST_LS; },
+                         [&](int b) { return (long long)(N[b] - 1); }, bt.act, bt.act_pre, sh);
+    if (threadIdx.x == 0) { bt.jac_pre[0] = 0; bt.acc_pre[0] = 0; }
+  } else {
+    nact = cs_build_list(B, [&](int b) { int st = I[b].status; return st == ST_FRESH || st == ST_LS || I[b].need_jac; },
+                         [&](int b) { return (long long)(N[b] - 1); }, bt.act, bt.act_pre, sh);
+    njac = cs_build_list(B, [&](int b) { return I[b].need_jac != 0; }, [&](int b) { return (long long)(N[b] - 1); },
+                         bt.jac, bt.jac_pre, sh);
+    nacc = cs_build_list(B, [&](int b) { return I[b].accepted != 0; }, [&](int b) { return (long long)N[b]; },
+                         bt.acc, bt.acc_pre, sh);
+    const int* J = bt.jac;
+    for (int l = 0; l < nlvl && l < CS_MAXLVL; ++l)
+      cs_build_list(njac, [&](int k) { return true; }, [&](int k) { return cs_level_items(N[J[k]] - 1, l); },
+                    (int*)nullptr, bt.lvl_pre + (size_t)l * (B + 1), sh);
+  }
+  if (threadIdx.x == 0) {
+    bt.nlist[0] = nact;
+    bt.nlist[1] = njac;
+    bt.nlist[2] = nacc;
+  }
 }
 
 // ------------------------------------------------------------------------
@@ -499,20 +631,27 @@ template <int GW>
 __device__ __forceinline__ void cs_condense_entry(const CsBatch& bt) {
   extern __shared__ double smem[];
   const int per = CS_S * CS_LDW + CS_NY + 2 * GW + 2;
+  const int njac = bt.nlist[1];
+  const long long total = bt.jac_pre[njac];
   if (GW == 1) {
+    const int wpc = blockDim.x >> 5;
     const int w = threadIdx.x >> 5;
-    const int slot = blockIdx.x * (blockDim.x >> 5) + w;
-    if (slot >= bt.T) return;
-    const int b = bt.inst_of[slot];
-    if (slot - bt.off[b] >= bt.N[b] - 1 || !bt.inst[b].need_jac) return;
     double* Wm = smem + (size_t)w * per;
-    cs_condense_group<1>(bt, slot, Wm, Wm + CS_S * CS_LDW);
+    for (long long it = (long long)blockIdx.x * wpc + w; it < total; it += (long long)gridDim.x * wpc) {
+      const int k = cs_find(bt.jac_pre, njac, it);
+      const int b = bt.jac[k];
+      const int slot = bt.off[b] + (int)(it - bt.jac_pre[k]);
+      cs_condense_group<1>(bt, slot, Wm, Wm + CS_S * CS_LDW);
+      __syncwarp();
+    }
   } else {
-    const int slot = blockIdx.x;
-    if (slot >= bt.T) return;
-    const int b = bt.inst_of[slot];
-    if (slot - bt.off[b] >= bt.N[b] - 1 || !bt.inst[b].need_jac) return;
-    cs_condense_group<GW>(bt, slot, smem, smem + CS_S * CS_LDW);
+    for (long long it = blockIdx.x; it < total; it += gridDim.x) {
+      const int k = cs_find(bt.jac_pre, njac, it);
+      const int b = bt.jac[k];
+      const int slot = bt.off[b] + (int)(it - bt.jac_pre[k]);
+      cs_condense_group<GW>(bt, slot, smem, smem + CS_S * CS_LDW);
+      __syncthreads();
+    }
   }
 }
 
@@ -625,52 +764,59 @@ __device__ void cs_backsub_warp(const double* rec, const double* yl, const doubl
   __syncwarp();
 }
 
-extern "C" __global__ void k_babd(CsBatch bt) {
+// One tree level for every instance that needs a Newton direction: warp per
+// item; item mi < merges eliminates node (2 mi + 1) 2^l between rows 2 mi and
+// 2 mi + 1, the last item of an odd level carries its row up unchanged.
+extern "C" __global__ void k_tree_level(CsBatch bt, int l) {
   extern __shared__ double smem[];
-  const int b = blockIdx.x;
-  if (b >= bt.B) return;
-  if (!bt.inst[b].need_jac) return;
-  const int nw = blockDim.x >> 5;
-  const int w = threadIdx.x >> 5;
-  const int lane = threadIdx.x & 31;
-  const int N = bt.N[b];
-  const int off = bt.off[b];
-  const int n0 = N - 1;  // block rows at level 0
+  const int wpc = blockDim.x >> 5, w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   double* Qw = smem + (size_t)w * CS_QLD * CS_QC;
-  double* top = smem + (size_t)nw * CS_QLD * CS_QC;   // CS_NT x (CS_NT+1), column-major, ld CS_TLD
-  double* dpv = top + (size_t)CS_TLD * (CS_NT + 1);    // [NP]
-  // ---- tree reduction
-  double* src = bt.rows0 + (size_t)off * CS_ROWSZ;
-  double* dst = bt.rows1 + (size_t)off * CS_ROWSZ;
-  int n = n0, stride = 1, levels = 0;
-  while (n > 1) {
-    const int merges = n >> 1;
-    for (int mi = w; mi < merges; mi += nw) {
-      const int mid = (2 * mi + 1) * stride;
+  const int njac = bt.nlist[1];
+  const long long* pre = bt.lvl_pre + (size_t)l * (bt.B + 1);
+  const long long total = pre[njac];
+  double* srcb = (l & 1) ? bt.rows1 : bt.rows0;
+  double* dstb = (l & 1) ? bt.rows0 : bt.rows1;
+  for (long long it = (long long)blockIdx.x * wpc + w; it < total; it += (long long)gridDim.x * wpc) {
+    const int k = cs_find(pre, njac, it);
+    const int b = bt.jac[k];
+    const int mi = (int)(it - pre[k]);
+    const int off = bt.off[b];
+    const int nl = cs_rows_at(bt.N[b] - 1, l);
+    const int merges = nl >> 1;
+    const double* src = srcb + (size_t)off * CS_ROWSZ;
+    double* dst = dstb + (size_t)off * CS_ROWSZ;
+    if (mi < merges) {
+      const int mid = (2 * mi + 1) << l;
       cs_merge_warp(src + (size_t)(2 * mi) * CS_ROWSZ, src + (size_t)(2 * mi + 1) * CS_ROWSZ,
                     dst + (size_t)mi * CS_ROWSZ, bt.tree + (size_t)(off + mid) * CS_TREESZ, Qw);
+    } else {
+      const double* sr = src + (size_t)(nl - 1) * CS_ROWSZ;
+      double* dr = dst + (size_t)merges * CS_ROWSZ;
+      for (int q = lane; q < CS_ROWSZ; q += 32) dr[q] = sr[q];
     }
-    if (n & 1) {
-      const double* s = src + (size_t)(n - 1) * CS_ROWSZ;
-      double* d = dst + (size_t)merges * CS_ROWSZ;
-      for (int q = threadIdx.x; q < CS_ROWSZ; q += blockDim.x) d[q] = s[q];
-    }
-    __syncthreads();
-    double* tmp = src; src = dst; dst = tmp;
-    n = (n + 1) >> 1;
-    stride <<= 1;
-    levels += 1;
+    __syncwarp();
   }
-  // ---- top system: [At Ct Ht 0; B0 Bn Vn] [y0; yN; p] = [bt; -r]
-  if (w == 0) {
-    const double* row = src;  // the single remaining block row
+}
+
+// Top of the tree, warp per instance: the remaining block row with the
+// boundary conditions, [At Ct Ht 0; B_0 B_n V_n] [y_0; y_N; p] = [bt; -r],
+// by Householder QR (the reference: final block QR + np.linalg.solve,
+// solve_babd_system.py:366-423).  Sets the line search going (alpha = 1).
+extern "C" __global__ void k_top(CsBatch bt) {
+  extern __shared__ double smem[];
+  const int wpc = blockDim.x >> 5, w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  double* top = smem + (size_t)w * CS_TLD * (CS_NT + 1);
+  const int njac = bt.nlist[1];
+  for (int k = blockIdx.x * wpc + w; k < njac; k += gridDim.x * wpc) {
+    const int b = bt.jac[k];
+    const int N = bt.N[b], off = bt.off[b];
+    const int L = cs_levels(N - 1);
+    const double* row = ((L & 1) ? bt.rows1 : bt.rows0) + (size_t)off * CS_ROWSZ;
     for (int c = lane; c < CS_NT + 1; c += 32) {
       double* col = top + (size_t)c * CS_TLD;
       for (int r = 0; r < CS_NY; ++r) {
         double v;
-        if (c < CS_NY) v = row[c * CS_NY + r];
-        else if (c < 2 * CS_NY) v = row[c * CS_NY + r];
-        else if (c < 2 * CS_NY + CS_NPE) v = row[c * CS_NY + r];
+        if (c < 2 * CS_NY + CS_NPE) v = row[c * CS_NY + r];
         else if (c < CS_NT) v = 0.0;
         else v = row[(2 * CS_NY + CS_NPE) * CS_NY + r];
         col[r] = v;
@@ -680,26 +826,25 @@ extern "C" __global__ void k_babd(CsBatch bt) {
       const double* th = bt.th + (size_t)b * (CS_NTH > 0 ? CS_NTH : 1);
       double ya[CS_NY], yb[CS_NY], pl[CS_NP > 0 ? CS_NP : 1], r[CS_NY + CS_NP];
       double Dr[(CS_NY + CS_NP) * (2 * CS_NY + CS_NP)];
-      for (int k = 0; k < CS_NY; ++k) { ya[k] = bt.y[(size_t)off * CS_NY + k]; yb[k] = bt.y[(size_t)(off + N - 1) * CS_NY + k]; }
-      for (int k = 0; k < CS_NP; ++k) pl[k] = bt.p[(size_t)b * CS_NP + k];
+      for (int q = 0; q < CS_NY; ++q) { ya[q] = bt.y[(size_t)off * CS_NY + q]; yb[q] = bt.y[(size_t)(off + N - 1) * CS_NY + q]; }
+      for (int q = 0; q < CS_NP; ++q) pl[q] = bt.p[(size_t)b * CS_NP + q];
       cs_r(ya, yb, pl, th, r);
       cs_Dr(ya, yb, pl, th, Dr);
       for (int q = 0; q < CS_NY + CS_NP; ++q) {
-        for (int c = 0; c < CS_NY; ++c) top[(size_t)c * CS_TLD + CS_NY + q] = Dr[q * (2 * CS_NY + CS_NP) + c];            // B_0
-        for (int c = 0; c < CS_NY; ++c) top[(size_t)(CS_NY + c) * CS_TLD + CS_NY + q] = Dr[q * (2 * CS_NY + CS_NP) + CS_NY + c];  // B_n
+        for (int c = 0; c < CS_NY; ++c) top[(size_t)c * CS_TLD + CS_NY + q] = Dr[q * (2 * CS_NY + CS_NP) + c];
+        for (int c = 0; c < CS_NY; ++c) top[(size_t)(CS_NY + c) * CS_TLD + CS_NY + q] = Dr[q * (2 * CS_NY + CS_NP) + CS_NY + c];
         for (int c = 0; c < CS_NP; ++c) top[(size_t)(2 * CS_NY + c) * CS_TLD + CS_NY + q] = Dr[q * (2 * CS_NY + CS_NP) + 2 * CS_NY + c];
         top[(size_t)CS_NT * CS_TLD + CS_NY + q] = -r[q];
       }
     }
     __syncwarp();
-    // Householder QR of the NT x NT system with its right-hand side
 #pragma unroll 1
-    for (int k = 0; k < CS_NT; ++k) {
-      const double* vk = top + (size_t)k * CS_TLD;
+    for (int kk = 0; kk < CS_NT; ++kk) {
+      const double* vk = top + (size_t)kk * CS_TLD;
       double ss = 0.0;
-      for (int r = k + lane; r < CS_NT; r += 32) ss += vk[r] * vk[r];
+      for (int r = kk + lane; r < CS_NT; r += 32) ss += vk[r] * vk[r];
       for (int o = 16; o > 0; o >>= 1) ss += __shfl_xor_sync(0xffffffffu, ss, o);
-      const double x0 = vk[k];
+      const double x0 = vk[kk];
       const double sgn = (x0 >= 0.0) ? 1.0 : -1.0;
       const double g = -sgn * sqrt(ss);
       const double v0 = x0 - g;
@@ -707,19 +852,19 @@ extern "C" __global__ void k_babd(CsBatch bt) {
       __syncwarp();
       if (vs < CS_EPS) continue;
       const double beta = -2.0 / vs;
-      for (int c = k + 1 + lane; c < CS_NT + 1; c += 32) {
+      for (int c = kk + 1 + lane; c < CS_NT + 1; c += 32) {
         double* col = top + (size_t)c * CS_TLD;
-        double wv = v0 * col[k];
-        for (int r = k + 1; r < CS_NT; ++r) wv += vk[r] * col[r];
+        double wv = v0 * col[kk];
+        for (int r = kk + 1; r < CS_NT; ++r) wv += vk[r] * col[r];
         const double bw = beta * wv;
-        col[k] = fma(bw, v0, col[k]);
-        for (int r = k + 1; r < CS_NT; ++r) col[r] = fma(bw, vk[r], col[r]);
+        col[kk] = fma(bw, v0, col[kk]);
+        for (int r = kk + 1; r < CS_NT; ++r) col[r] = fma(bw, vk[r], col[r]);
       }
       __syncwarp();
       if (lane == 0) {
-        double* col = top + (size_t)k * CS_TLD;
-        col[k] = g;
-        for (int r = k + 1; r < CS_NT; ++r) col[r] = 0.0;
+        double* col = top + (size_t)kk * CS_TLD;
+        col[kk] = g;
+        for (int r = kk + 1; r < CS_NT; ++r) col[r] = 0.0;
       }
       __syncwarp();
     }
@@ -729,7 +874,7 @@ extern "C" __global__ void k_babd(CsBatch bt) {
       for (int r = CS_NT - 1; r >= 0; --r) {
         double v = rhs[r];
         for (int c = r + 1; c < CS_NT; ++c) v -= top[(size_t)c * CS_TLD + r] * rhs[c];
-        double d = top[(size_t)r * CS_TLD + r];
+        const double d = top[(size_t)r * CS_TLD + r];
         if (d == 0.0) sing = true;
         rhs[r] = (d != 0.0) ? v / d : 0.0;
       }
@@ -737,35 +882,56 @@ extern "C" __global__ void k_babd(CsBatch bt) {
         for (int r = 0; r < CS_NT; ++r) rhs[r] = 0.0;
         bt.inst[b].singular += 1;
       }
-      for (int k = 0; k < CS_NY; ++k) {
-        bt.dy[(size_t)off * CS_NY + k] = rhs[k];
-        bt.dy[(size_t)(off + N - 1) * CS_NY + k] = rhs[CS_NY + k];
+      for (int q = 0; q < CS_NY; ++q) {
+        bt.dy[(size_t)off * CS_NY + q] = rhs[q];
+        bt.dy[(size_t)(off + N - 1) * CS_NY + q] = rhs[CS_NY + q];
       }
-      for (int k = 0; k < CS_NP; ++k) { dpv[k] = rhs[2 * CS_NY + k]; bt.dp[(size_t)b * CS_NP + k] = rhs[2 * CS_NY + k]; }
+      for (int q = 0; q < CS_NP; ++q) bt.dp[(size_t)b * CS_NP + q] = rhs[2 * CS_NY + q];
+      bt.inst[b].status = ST_LS;
+      bt.inst[b].alpha_ls = 1.0;
+      bt.inst[b].ls_it = 0;
     }
+    __syncwarp();
   }
-  __syncthreads();
-  // ---- back substitution down the tree
-  for (int l = levels - 1; l >= 0; --l) {
-    int nl = n0;
-    for (int q = 0; q < l; ++q) nl = (nl + 1) >> 1;
-    const int st = 1 << l;
-    const int merges = nl >> 1;
-    for (int mi = w; mi < merges; mi += nw) {
-      const int mid = (2 * mi + 1) * st;
-      const int left = 2 * mi * st;
-      int right = (2 * mi + 2) * st;
-      if (right > n0) right = n0;
-      cs_backsub_warp(bt.tree + (size_t)(off + mid) * CS_TREESZ, bt.dy + (size_t)(off + left) * CS_NY,
-                      bt.dy + (size_t)(off + right) * CS_NY, dpv, bt.dy + (size_t)(off + mid) * CS_NY);
-    }
-    __syncthreads();
+}
+
+// Back substitution of one tree level (top-down), warp per merge.
+extern "C" __global__ void k_backsub_level(CsBatch bt, int l) {
+  const int wpc = blockDim.x >> 5, w = threadIdx.x >> 5;
+  const int njac = bt.nlist[1];
+  const long long* pre = bt.lvl_pre + (size_t)l * (bt.B + 1);
+  const long long total = pre[njac];
+  for (long long it = (long long)blockIdx.x * wpc + w; it < total; it += (long long)gridDim.x * wpc) {
+    const int k = cs_find(pre, njac, it);
+    const int b = bt.jac[k];
+    const int mi = (int)(it - pre[k]);
+    const int n0 = bt.N[b] - 1;
+    const int merges = cs_rows_at(n0, l) >> 1;
+    if (mi >= merges) continue;
+    const int off = bt.off[b];
+    const int mid = (2 * mi + 1) << l;
+    const int left = (2 * mi) << l;
+    int right = (2 * mi + 2) << l;
+    if (right > n0) right = n0;
+    cs_backsub_warp(bt.tree + (size_t)(off + mid) * CS_TREESZ, bt.dy + (size_t)(off + left) * CS_NY,
+                    bt.dy + (size_t)(off + right) * CS_NY, bt.dp + (size_t)b * CS_NP, bt.dy + (size_t)(off + mid) * CS_NY);
   }
-  // ---- recovery: dk = -(X_f + X_J dy_i + X_V dp), lanes over stage rows
-  for (int iv = w; iv < n0; iv += nw) {
-    const int slot = off + iv;
+}
+
+// Stage steps: dk = -(X_f + X_J dy_i + X_V dp), warp per interval, lanes
+// over stage rows (the reference re-factorises W instead,
+// collocation_solver_parallel_2d_shared.py:1619-1650).
+extern "C" __global__ void k_recover(CsBatch bt) {
+  const int wpc = blockDim.x >> 5, w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int njac = bt.nlist[1];
+  const long long total = bt.jac_pre[njac];
+  for (long long it = (long long)blockIdx.x * wpc + w; it < total; it += (long long)gridDim.x * wpc) {
+    const int k = cs_find(bt.jac_pre, njac, it);
+    const int b = bt.jac[k];
+    const int slot = bt.off[b] + (int)(it - bt.jac_pre[k]);
     const double* X = bt.X + (size_t)slot * CS_NRHS * CS_S;
     const double* dyi = bt.dy + (size_t)slot * CS_NY;
+    const double* dpv = bt.dp + (size_t)b * CS_NP;
     for (int r = lane; r < CS_S; r += 32) {
       double v = X[(size_t)(CS_NY + CS_NPE) * CS_S + r];
       for (int q = 0; q < CS_NY; ++q) v = fma(X[(size_t)q * CS_S + r], dyi[q], v);
@@ -774,11 +940,6 @@ extern "C" __global__ void k_babd(CsBatch bt) {
       if (a < CS_NY) bt.dydot[((size_t)slot * CS_M + j) * CS_NY + a] = -v;
       else bt.dzt[((size_t)slot * CS_M + j) * CS_NZ + (a - CS_NY)] = -v;
     }
-  }
-  if (threadIdx.x == 0) {
-    bt.inst[b].status = ST_LS;
-    bt.inst[b].alpha_ls = 1.0;
-    bt.inst[b].ls_it = 0;
   }
 }
 

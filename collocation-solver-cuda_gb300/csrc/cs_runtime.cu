@@ -124,7 +124,17 @@ struct CsBatchDev {
   unsigned long long* counters;
   double* fa_out;
   double* fb_out;
+  int* act;
+  int* jac;
+  int* acc;
+  long long* act_pre;
+  long long* jac_pre;
+  long long* acc_pre;
+  long long* lvl_pre;
+  int* nlist;
 };
+
+static const int CS_MAXLVL = 32;
 
 enum { ST_FRESH = 0, ST_LS = 1, ST_SEG = 2, ST_DONE = 3, ST_FAIL = 4, ST_REMESH = 5 };
 enum { FAIL_NONE = 0, FAIL_ITER = 1, FAIL_NODES = 2, FAIL_MESH = 3 };
@@ -209,12 +219,15 @@ struct cs_module {
   int ny, nz, np, npe, nth, m, s, nrhs, cgw;
   size_t rowsz, treesz;
   CUmodule mod = nullptr;
-  CUfunction f_form_initial, f_residual, f_decide, f_accept, f_condense, f_babd, f_segres, f_mesh_decide,
-      f_remesh_count, f_remesh_write, f_repack, f_znodes;
+  CUfunction f_form_initial, f_residual, f_decide, f_accept, f_condense, f_segres, f_mesh_decide,
+      f_remesh_count, f_remesh_write, f_repack, f_znodes, f_lists, f_tree_level, f_top, f_backsub_level, f_recover;
   int condense_block, condense_per_cta;
   size_t condense_smem;
-  int babd_block;
-  size_t babd_smem;
+  size_t tree_smem;   // per CTA of 4 warps
+  int top_wpc;
+  size_t top_smem;
+  int sms = 1;
+  int condense_grid = 1;
 };
 
 static std::string build_source(const cs_module_desc* d, int cgw) {
@@ -320,15 +333,18 @@ extern "C" int cs_module_load(const cs_module_desc* d, cs_module** out) {
     M->condense_block = 32 * cgw;
     M->condense_smem = per;
   }
-  // BABD: one CTA per instance, 8 warps, a merge matrix per warp + the top system
-  M->babd_block = 256;
+  // BABD tree: a merge matrix per warp (4 warps per CTA); top: one system per warp
   const int qld = (2 * M->ny) | 1, qc = 3 * M->ny + M->npe + 1;
   const int nt = 2 * M->ny + M->np, tld = nt | 1;
-  M->babd_smem = ((size_t)8 * qld * qc + (size_t)tld * (nt + 1) + M->np + 2) * sizeof(double);
-  if (M->babd_smem > (size_t)smem_optin) {
+  M->tree_smem = (size_t)4 * qld * qc * sizeof(double);
+  const size_t top_per = (size_t)tld * (nt + 1) * sizeof(double);
+  if (M->tree_smem > (size_t)smem_optin || top_per > (size_t)smem_optin) {
     delete M;
     return set_err(CS_ERR_INVALID, "cs_module_load: BABD blocks do not fit in shared memory");
   }
+  M->top_wpc = (int)std::max<size_t>(1, std::min<size_t>(4, (size_t)smem_optin / top_per));
+  M->top_smem = top_per * M->top_wpc;
+  CS_CUDA(cudaDeviceGetAttribute(&M->sms, cudaDevAttrMultiProcessorCount, dev));
 
   std::string src = build_source(d, cgw);
   std::string cache = d->cache_dir ? d->cache_dir : "";
@@ -351,10 +367,13 @@ extern "C" int cs_module_load(const cs_module_desc* d, cs_module** out) {
     CUfunction* f;
     const char* name;
   } fns[] = {{&M->f_form_initial, "k_form_initial"}, {&M->f_residual, "k_residual"},   {&M->f_decide, "k_decide"},
-             {&M->f_accept, "k_accept"},             {&M->f_condense, "k_condense"},   {&M->f_babd, "k_babd"},
+             {&M->f_accept, "k_accept"},             {&M->f_condense, "k_condense"},
              {&M->f_segres, "k_segres"},             {&M->f_mesh_decide, "k_mesh_decide"},
              {&M->f_remesh_count, "k_remesh_count"}, {&M->f_remesh_write, "k_remesh_write"},
-             {&M->f_repack, "k_repack"},             {&M->f_znodes, "k_znodes"}};
+             {&M->f_repack, "k_repack"},             {&M->f_znodes, "k_znodes"},
+             {&M->f_lists, "k_lists"},               {&M->f_tree_level, "k_tree_level"},
+             {&M->f_top, "k_top"},                   {&M->f_backsub_level, "k_backsub_level"},
+             {&M->f_recover, "k_recover"}};
   for (auto& e : fns) {
     CUresult rr = g_drv.moduleGetFunction(e.f, M->mod, e.name);
     if (rr != CUDA_SUCCESS) {
@@ -365,8 +384,16 @@ extern "C" int cs_module_load(const cs_module_desc* d, cs_module** out) {
   }
   if (M->condense_smem > 48 * 1024)
     CS_CU(g_drv.funcSetAttribute(M->f_condense, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, (int)M->condense_smem));
-  if (M->babd_smem > 48 * 1024)
-    CS_CU(g_drv.funcSetAttribute(M->f_babd, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, (int)M->babd_smem));
+  if (M->tree_smem > 48 * 1024)
+    CS_CU(g_drv.funcSetAttribute(M->f_tree_level, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, (int)M->tree_smem));
+  if (M->top_smem > 48 * 1024)
+    CS_CU(g_drv.funcSetAttribute(M->f_top, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, (int)M->top_smem));
+  {
+    // resident CTAs of the condensation kernel per SM, for its persistent grid
+    int per_sm = std::max<int>(1, (int)((size_t)smem_optin / std::max<size_t>(M->condense_smem, 1)));
+    per_sm = std::min(per_sm, 2048 / M->condense_block);
+    M->condense_grid = M->sms * per_sm;
+  }
   *out = M;
   return CS_OK;
 }
@@ -413,6 +440,14 @@ struct cs_batch {
   DBuf inst_of, dy, dydot, dzt, X, rows0, rows1, tree, res;
   std::vector<int> hN, hoff;
   cs_opts opts;
+  // work lists
+  DBuf l_act, l_jac, l_acc, l_actp, l_jacp, l_accp, l_lvlp, l_n;
+  int* h_n = nullptr;  // pinned copy of nlist
+  // captured super-step
+  cudaGraphExec_t graph = nullptr;
+  int graph_nlvl = -1;
+  CsBatchDev graph_view;
+  CsConsts graph_consts;
   // device copy of the last initial guess (cs_batch_reset)
   DBuf iN, ioff, it, iy, iz, ip;
   std::vector<int> ihN, ihoff;
@@ -523,6 +558,14 @@ static CsBatchDev devview(cs_batch* bt) {
   v.znode = (double*)bt->znode[s].p;
   v.inst = (CsInst*)bt->dinst.p;
   v.counters = (unsigned long long*)bt->dcounters.p;
+  v.act = (int*)bt->l_act.p;
+  v.jac = (int*)bt->l_jac.p;
+  v.acc = (int*)bt->l_acc.p;
+  v.act_pre = (long long*)bt->l_actp.p;
+  v.jac_pre = (long long*)bt->l_jacp.p;
+  v.acc_pre = (long long*)bt->l_accp.p;
+  v.lvl_pre = (long long*)bt->l_lvlp.p;
+  v.nlist = (int*)bt->l_n.p;
   return v;
 }
 
@@ -579,13 +622,44 @@ static int run_insts(cs_batch* bt, CUfunction f, void** args) { return launch(bt
 static int run_condense(cs_batch* bt, CsBatchDev& v) {
   cs_module* M = bt->M;
   void* args[] = {&v};
-  unsigned grid = (M->cgw == 1) ? cdiv(bt->T, M->condense_per_cta) : (unsigned)bt->T;
-  return launch_k(bt, M->f_condense, grid, M->condense_block, M->condense_smem, args, 0);
+  return launch_k(bt, M->f_condense, (unsigned)M->condense_grid, M->condense_block, M->condense_smem, args, 0);
 }
 
-static int run_babd(cs_batch* bt, CsBatchDev& v) {
-  void* args[] = {&v};
-  return launch_k(bt, bt->M->f_babd, (unsigned)bt->B, bt->M->babd_block, bt->M->babd_smem, args, 1);
+static int tree_levels(const cs_batch* bt) {
+  int mx = 1;
+  for (int n : bt->hN) mx = std::max(mx, n - 1);
+  int L = 0, n = mx;
+  while (n > 1) {
+    n = (n + 1) >> 1;
+    ++L;
+  }
+  return L;
+}
+
+static int run_lists(cs_batch* bt, CsBatchDev& v, int mode, int nlvl) {
+  void* args[] = {&v, &mode, &nlvl};
+  return launch(bt, bt->M->f_lists, 1, 1024, 0, args);
+}
+
+// Newton direction for the instances on the jac list: tree levels up, top
+// system, back substitution down, stage recovery.
+static int run_direction(cs_batch* bt, CsBatchDev& v, int nlvl) {
+  cs_module* M = bt->M;
+  const unsigned g = (unsigned)(M->sms * 8);
+  for (int l = 0; l < nlvl; ++l) {
+    void* a[] = {&v, &l};
+    CS_TRY(launch_k(bt, M->f_tree_level, g, 128, M->tree_smem, a, 1));
+  }
+  {
+    void* a[] = {&v};
+    CS_TRY(launch_k(bt, M->f_top, (unsigned)(M->sms * 4), 32 * M->top_wpc, M->top_smem, a, 1));
+  }
+  for (int l = nlvl - 1; l >= 0; --l) {
+    void* a[] = {&v, &l};
+    CS_TRY(launch_k(bt, M->f_backsub_level, g, 128, 0, a, 1));
+  }
+  void* a[] = {&v};
+  return launch_k(bt, M->f_recover, g, 128, 0, a, 1);
 }
 
 static int fill_inst_of(cs_batch* bt) {
@@ -598,6 +672,7 @@ static int fill_inst_of(cs_batch* bt) {
 
 static CsConsts consts_of(const cs_opts& o) {
   CsConsts c;
+  memset(&c, 0, sizeof(c));
   c.tol = o.tol;
   c.alpha_m = o.alpha_m;
   c.beta = o.beta;
@@ -631,7 +706,14 @@ extern "C" int cs_batch_create(cs_module* M, int batch, long long node_capacity,
       (rc = dalloc(bt->doff2, batch * sizeof(int))) || (rc = dalloc(bt->dp, batch * std::max(M->np, 1) * d)) ||
       (rc = dalloc(bt->ddp, batch * std::max(M->np, 1) * d)) ||
       (rc = dalloc(bt->dth, batch * std::max(M->nth, 1) * d)) || (rc = dalloc(bt->dinst, batch * sizeof(CsInst))) ||
-      (rc = dalloc(bt->dcounters, 64)) || (rc = alloc_slots(bt, std::max<long long>(node_capacity, 2 * batch), false))) {
+      (rc = dalloc(bt->dcounters, 64)) || (rc = dalloc(bt->l_act, batch * sizeof(int))) ||
+      (rc = dalloc(bt->l_jac, batch * sizeof(int))) || (rc = dalloc(bt->l_acc, batch * sizeof(int))) ||
+      (rc = dalloc(bt->l_actp, (batch + 1) * sizeof(long long))) ||
+      (rc = dalloc(bt->l_jacp, (batch + 1) * sizeof(long long))) ||
+      (rc = dalloc(bt->l_accp, (batch + 1) * sizeof(long long))) ||
+      (rc = dalloc(bt->l_lvlp, (size_t)CS_MAXLVL * (batch + 1) * sizeof(long long))) ||
+      (rc = dalloc(bt->l_n, 4 * sizeof(int))) ||
+      (rc = alloc_slots(bt, std::max<long long>(node_capacity, 2 * batch), false))) {
     cs_batch_free(bt);
     return rc;
   }
@@ -644,8 +726,11 @@ extern "C" void cs_batch_free(cs_batch* bt) {
   if (bt->stream) cudaStreamSynchronize(bt->stream);
   DBuf* all[] = {&bt->dN, &bt->doff, &bt->doff2, &bt->dp, &bt->dth, &bt->ddp, &bt->dinst, &bt->dcounters,
                  &bt->inst_of, &bt->dy, &bt->dydot, &bt->dzt, &bt->X, &bt->rows0, &bt->rows1, &bt->tree, &bt->res,
-                 &bt->iN, &bt->ioff, &bt->it, &bt->iy, &bt->iz, &bt->ip};
+                 &bt->iN, &bt->ioff, &bt->it, &bt->iy, &bt->iz, &bt->ip, &bt->l_act, &bt->l_jac, &bt->l_acc,
+                 &bt->l_actp, &bt->l_jacp, &bt->l_accp, &bt->l_lvlp, &bt->l_n};
   for (DBuf* b : all) dfree(*b);
+  if (bt->graph) cudaGraphExecDestroy(bt->graph);
+  if (bt->h_n) cudaFreeHost(bt->h_n);
   for (auto& e : bt->ev_pool) {
     cudaEventDestroy(e.a);
     cudaEventDestroy(e.b);
@@ -782,20 +867,57 @@ static int write_inst(cs_batch* bt, const std::vector<CsInst>& hi) {
   return CS_OK;
 }
 
-static int super_step(cs_batch* bt, const CsConsts& c) {
+static int super_step(cs_batch* bt, const CsConsts& c, int nlvl) {
   CsBatchDev v = devview(bt);
   cs_module* M = bt->M;
+  const unsigned g = (unsigned)(M->sms * 8);
   {
     void* args[] = {&v};
-    CS_TRY(launch_k(bt, M->f_residual, cdiv(bt->T, 256), 256, 0, args, 2));
+    CS_TRY(launch_k(bt, M->f_residual, g, 256, 0, args, 2));
   }
   bt->super_steps += 1;
   CsConsts cc = c;
   void* dargs[] = {&v, &cc};
   CS_TRY(run_insts(bt, M->f_decide, dargs));
-  CS_TRY(run_slots(bt, M->f_accept, v));
+  CS_TRY(run_lists(bt, v, 1, nlvl));
+  {
+    void* args[] = {&v};
+    CS_TRY(launch(bt, M->f_accept, g, 256, 0, args));
+  }
   CS_TRY(run_condense(bt, v));
-  CS_TRY(run_babd(bt, v));
+  return run_direction(bt, v, nlvl);
+}
+
+// A CUDA graph of `reps` super-steps for the current layout (re-captured when
+// a remesh changes the buffers).
+static int get_graph(cs_batch* bt, const CsConsts& c, int nlvl, int reps) {
+  const CsBatchDev v = devview(bt);
+  if (bt->graph && bt->graph_nlvl == nlvl && memcmp(&bt->graph_view, &v, sizeof(v)) == 0 &&
+      memcmp(&bt->graph_consts, &c, sizeof(c)) == 0)
+    return CS_OK;
+  if (bt->graph) {
+    cudaGraphExecDestroy(bt->graph);
+    bt->graph = nullptr;
+  }
+  cudaGraph_t g = nullptr;
+  CS_CUDA(cudaStreamBeginCapture(bt->stream, cudaStreamCaptureModeThreadLocal));
+  int rc = CS_OK;
+  const long long l0 = bt->launches, s0 = bt->super_steps;
+  for (int r = 0; r < reps && rc == CS_OK; ++r) rc = super_step(bt, c, nlvl);
+  cudaError_t e = cudaStreamEndCapture(bt->stream, &g);
+  bt->launches = l0;  // captured launches are counted when the graph runs
+  bt->super_steps = s0;
+  if (rc != CS_OK) {
+    if (g) cudaGraphDestroy(g);
+    return rc;
+  }
+  if (e != cudaSuccess) return set_err(CS_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+  e = cudaGraphInstantiate(&bt->graph, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) return set_err(CS_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
+  bt->graph_view = v;
+  bt->graph_consts = c;
+  bt->graph_nlvl = nlvl;
   return CS_OK;
 }
 
@@ -860,29 +982,37 @@ extern "C" int cs_solve(cs_batch* bt, const cs_opts* opts) {
     s.alpha = o.alpha0;
   }
   CS_TRY(write_inst(bt, hi));
-  unsigned long long* hcount = nullptr;
-  CS_CUDA(cudaMallocHost(&hcount, sizeof(unsigned long long)));
+  if (!bt->h_n) CS_CUDA(cudaMallocHost(&bt->h_n, 4 * sizeof(int)));
   int rc = CS_OK;
-  const long long max_super = 1000000;
+  const long long max_super = 10000000;
   long long steps = 0;
+  const int per_launch_steps = 1;
   for (int outer = 0; outer < 1000000 && rc == CS_OK; ++outer) {
-    // ---- Newton phase
+    // ---- Newton phase: device state machine, work lists, graph replays
+    const int nlvl = tree_levels(bt);
+    CsBatchDev v0 = devview(bt);
+    if ((rc = run_lists(bt, v0, 0, nlvl)) != CS_OK) break;
+    const bool use_graph = !bt->timing;
+    if (use_graph && (rc = get_graph(bt, c, nlvl, per_launch_steps)) != CS_OK) break;
     for (;;) {
       for (int k = 0; k < o.check_every && rc == CS_OK; ++k) {
-        if (cudaMemsetAsync(bt->dcounters.p, 0, sizeof(unsigned long long), bt->stream) != cudaSuccess) {
-          rc = set_err(CS_ERR_CUDA, "memset");
-          break;
+        if (use_graph) {
+          cudaError_t e = cudaGraphLaunch(bt->graph, bt->stream);
+          if (e != cudaSuccess) rc = set_err(CS_ERR_CUDA, std::string("graph launch: ") + cudaGetErrorString(e));
+          bt->launches += 9 + 2 * nlvl;
+          bt->super_steps += 1;
+        } else {
+          rc = super_step(bt, c, nlvl);
         }
-        rc = super_step(bt, c);
         ++steps;
       }
       if (rc != CS_OK) break;
-      if (cudaMemcpyAsync(hcount, bt->dcounters.p, sizeof(unsigned long long), cudaMemcpyDeviceToHost, bt->stream) != cudaSuccess ||
+      if (cudaMemcpyAsync(bt->h_n, bt->l_n.p, sizeof(int), cudaMemcpyDeviceToHost, bt->stream) != cudaSuccess ||
           cudaStreamSynchronize(bt->stream) != cudaSuccess) {
         rc = set_err(CS_ERR_CUDA, std::string("Newton phase: ") + cudaGetErrorString(cudaGetLastError()));
         break;
       }
-      if (*hcount == 0) break;
+      if (bt->h_n[0] == 0) break;
       if (steps > max_super) {
         rc = set_err(CS_ERR_STATE, "Newton phase did not terminate");
         break;
@@ -924,7 +1054,6 @@ extern "C" int cs_solve(cs_batch* bt, const cs_opts* opts) {
     }
     if (!any_newton) break;
   }
-  cudaFreeHost(hcount);
   if (rc == CS_OK) CS_CUDA(cudaStreamSynchronize(bt->stream));
   return rc;
 }
@@ -1022,7 +1151,11 @@ extern "C" int cs_stage_residual(cs_batch* bt, double alpha, double* norms, doub
   CsBatchDev v = devview(bt);
   v.fa_out = (double*)fa.p;
   v.fb_out = (double*)fb.p;
-  int rc = run_slots(bt, M->f_residual, v);
+  int rc = run_lists(bt, v, 0, 0);
+  if (rc == CS_OK) {
+    void* args[] = {&v};
+    rc = launch(bt, M->f_residual, (unsigned)(M->sms * 8), 256, 0, args);
+  }
   std::vector<CsInst> hi;
   if (rc == CS_OK) rc = read_inst(bt, hi);
   if (rc == CS_OK && norms)
@@ -1051,11 +1184,13 @@ extern "C" int cs_stage_newton_direction(cs_batch* bt, double alpha, double* row
   cs_module* M = bt->M;
   CS_TRY(set_all_status(bt, ST_FRESH, alpha, 1));
   CsBatchDev v = devview(bt);
+  const int nlvl = tree_levels(bt);
+  CS_TRY(run_lists(bt, v, 1, nlvl));
   CS_TRY(run_condense(bt, v));
   const size_t d = sizeof(double);
   cudaStream_t st = bt->stream;
   if (rows) CS_CUDA(cudaMemcpyAsync(rows, bt->rows0.p, (size_t)bt->T * M->rowsz * d, cudaMemcpyDeviceToHost, st));
-  CS_TRY(run_babd(bt, v));
+  CS_TRY(run_direction(bt, v, nlvl));
   if (dy) CS_CUDA(cudaMemcpyAsync(dy, bt->dy.p, (size_t)bt->T * M->ny * d, cudaMemcpyDeviceToHost, st));
   if (dydot) CS_CUDA(cudaMemcpyAsync(dydot, bt->dydot.p, (size_t)bt->T * M->m * M->ny * d, cudaMemcpyDeviceToHost, st));
   if (dzt && M->nz > 0) CS_CUDA(cudaMemcpyAsync(dzt, bt->dzt.p, (size_t)bt->T * M->m * M->nz * d, cudaMemcpyDeviceToHost, st));
@@ -1100,6 +1235,7 @@ extern "C" int cs_time_condense(cs_batch* bt, int reps, double* ms) {
   if (!bt || !bt->have_guess || !ms || reps < 1) return set_err(CS_ERR_INVALID, "cs_time_condense: bad argument");
   CS_TRY(set_all_status(bt, ST_FRESH, bt->opts.alpha0, 1));
   CsBatchDev v = devview(bt);
+  CS_TRY(run_lists(bt, v, 1, 0));
   CS_TRY(run_condense(bt, v));
   cudaEvent_t e0, e1;
   CS_CUDA(cudaEventCreate(&e0));
