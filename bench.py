@@ -245,7 +245,20 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--batch", type=int, default=BATCH)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile-case", action="store_true",
+                    help="small case for ncu: 512 instances, one full-batch condensation per m group, one solve")
     args = ap.parse_args()
+    if args.profile_case:
+        cs = _pkg()
+        cs.build.build_library()
+        W = Workload(cs, cs.workloads.vdp_batch(512, seed=SEED))
+        for g in W.groups:
+            g["bt"].reset()
+            ms = g["bt"].time_condense(reps=1)
+            print("m=%d condense %.3f ms over %d intervals" % (g["m"], ms, g["bt"].sizes()[1] - g["bt"].B))
+        W.step_resident()
+        print("profile case ok", W.results())
+        return
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))

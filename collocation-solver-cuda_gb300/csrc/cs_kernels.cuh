@@ -475,23 +475,38 @@ struct CsGroup {
   }
 };
 
+// Shared memory of one condensation group (doubles):
+//   Wm    [S][LDW]                 augmented matrix [W | J | V_eff | f_a]
+//   Jy    [M][NY+NZ][NY+NZ+NPE]    stage Jacobian rows [h_y h_z h_p ; g_y g_z g_p]
+//   fa    [M][NY+NZ]               stage residuals
+//   hA    [M][M]                   h * A
+//   fb    [NY]                     f_b
+//   inv   [S]                      reciprocal pivots
+//   red   [2 GW]                   cross-warp pivot search (GW > 1)
+#define CS_JYC (CS_NY + CS_NZ + CS_NPE)
+#define CS_GRP_DBL(GW) (CS_S * CS_LDW + CS_M * (CS_NY + CS_NZ) * CS_JYC + CS_M * (CS_NY + CS_NZ) + CS_M * CS_M + CS_NY + CS_S + 2 * (GW) + 2)
+
 template <int GW>
-__device__ void cs_condense_group(const CsBatch& bt, int slot, double* Wm, double* aux) {
+__device__ void cs_condense_group(const CsBatch& bt, int slot, double* Wm) {
   typedef CsGroup<GW> G;
+  constexpr int NT = G::NT;
+  constexpr int RB = CS_NY + CS_NZ;  // rows per stage block
   const int tid = G::tid();
+  double* Jy = Wm + CS_S * CS_LDW;
+  double* fa = Jy + CS_M * RB * CS_JYC;
+  double* hA = fa + CS_M * RB;
+  double* fb = hA + CS_M * CS_M;
+  double* inv = fb + CS_NY;
+  double* red = inv + CS_S;
   const int b = bt.inst_of[slot];
-  const int i = slot - bt.off[b];
   const double h = bt.t[slot + 1] - bt.t[slot];
   const double* th = bt.th + (size_t)b * (CS_NTH > 0 ? CS_NTH : 1);
-  double* fb = aux;                       // [NY]
-  int* piv = (int*)(aux + CS_NY);         // [GW] partial argmax rows (GW > 1)
-  double* pvv = aux + CS_NY + GW;         // [GW] partial max values
-  // ---- build rows of stage j on thread j (stage Jacobians at y~_j)
-  for (int j = tid; j < CS_M; j += G::NT) {
+  const double* yi = bt.y + (size_t)slot * CS_NY;
+  const double* yd = bt.ydot + (size_t)slot * CS_M * CS_NY;
+  // ---- stage Jacobians and residuals: thread j handles stage j
+  for (int j = tid; j < CS_M; j += NT) {
     double pl[CS_NP > 0 ? CS_NP : 1];
     for (int k = 0; k < CS_NP; ++k) pl[k] = bt.p[(size_t)b * CS_NP + k];
-    const double* yi = bt.y + (size_t)slot * CS_NY;
-    const double* yd = bt.ydot + (size_t)slot * CS_M * CS_NY;
     double yt[CS_NY], zl[CS_NZ > 0 ? CS_NZ : 1];
     for (int k = 0; k < CS_NY; ++k) {
       double s = 0.0;
@@ -503,16 +518,11 @@ __device__ void cs_condense_group(const CsBatch& bt, int slot, double* Wm, doubl
     double Df[CS_NY * CS_NFG];
     cs_f(yt, zl, pl, th, f);
     cs_Df(yt, zl, pl, th, Df);
+    double* J = Jy + (size_t)j * RB * CS_JYC;
     for (int a = 0; a < CS_NY; ++a) {
-      double* row = Wm + (size_t)(j * (CS_NY + CS_NZ) + a) * CS_LDW;
-      for (int k = 0; k < CS_M; ++k) {
-        double hA = h * CS_A[j * CS_M + k];
-        for (int q = 0; q < CS_NY; ++q) row[k * (CS_NY + CS_NZ) + q] = hA * Df[a * CS_NFG + q] - ((k == j && q == a) ? 1.0 : 0.0);
-        for (int q = 0; q < CS_NZ; ++q) row[k * (CS_NY + CS_NZ) + CS_NY + q] = (k == j) ? Df[a * CS_NFG + CS_NY + q] : 0.0;
-      }
-      for (int q = 0; q < CS_NY; ++q) row[CS_S + q] = Df[a * CS_NFG + q];
-      for (int q = 0; q < CS_NPE; ++q) row[CS_S + CS_NY + q] = Df[a * CS_NFG + CS_NY + CS_NZ + q];
-      row[CS_S + CS_NY + CS_NPE] = f[a] - yd[j * CS_NY + a];
+      for (int q = 0; q < CS_NY + CS_NZ; ++q) J[a * CS_JYC + q] = Df[a * CS_NFG + q];
+      for (int q = 0; q < CS_NPE; ++q) J[a * CS_JYC + CS_NY + CS_NZ + q] = Df[a * CS_NFG + CS_NY + CS_NZ + q];
+      fa[j * RB + a] = f[a] - yd[j * CS_NY + a];
     }
 #if CS_NZ > 0
     double g[CS_NZ];
@@ -520,117 +530,136 @@ __device__ void cs_condense_group(const CsBatch& bt, int slot, double* Wm, doubl
     cs_g(yt, zl, pl, th, bt.inst[b].alpha, g);
     cs_Dg(yt, zl, pl, th, bt.inst[b].alpha, Dg);
     for (int a = 0; a < CS_NZ; ++a) {
-      double* row = Wm + (size_t)(j * (CS_NY + CS_NZ) + CS_NY + a) * CS_LDW;
-      for (int k = 0; k < CS_M; ++k) {
-        double hA = h * CS_A[j * CS_M + k];
-        for (int q = 0; q < CS_NY; ++q) row[k * (CS_NY + CS_NZ) + q] = hA * Dg[a * CS_NFG + q];
-        for (int q = 0; q < CS_NZ; ++q) row[k * (CS_NY + CS_NZ) + CS_NY + q] = (k == j) ? Dg[a * CS_NFG + CS_NY + q] : 0.0;
-      }
-      for (int q = 0; q < CS_NY; ++q) row[CS_S + q] = Dg[a * CS_NFG + q];
-      for (int q = 0; q < CS_NPE; ++q) row[CS_S + CS_NY + q] = Dg[a * CS_NFG + CS_NY + CS_NZ + q];
-      row[CS_S + CS_NY + CS_NPE] = g[a];
+      for (int q = 0; q < CS_NY + CS_NZ; ++q) J[(CS_NY + a) * CS_JYC + q] = Dg[a * CS_NFG + q];
+      for (int q = 0; q < CS_NPE; ++q) J[(CS_NY + a) * CS_JYC + CS_NY + CS_NZ + q] = Dg[a * CS_NFG + CS_NY + CS_NZ + q];
+      fa[j * RB + CS_NY + a] = g[a];
     }
 #endif
   }
-  if (tid == G::NT - 1 || (G::NT <= CS_M && tid == 0)) {
-    const double* yi = bt.y + (size_t)slot * CS_NY;
-    const double* yd = bt.ydot + (size_t)slot * CS_M * CS_NY;
-    for (int k = 0; k < CS_NY; ++k) {
-      double s = 0.0;
-      for (int j = 0; j < CS_M; ++j) s += CS_B[j] * yd[j * CS_NY + k];
-      fb[k] = yi[CS_NY + k] - yi[k] - h * s;
-    }
+  for (int e = tid; e < CS_M * CS_M; e += NT) hA[e] = h * CS_A[e];
+  for (int k = tid; k < CS_NY; k += NT) {
+    double s = 0.0;
+    for (int j = 0; j < CS_M; ++j) s += CS_B[j] * yd[j * CS_NY + k];
+    fb[k] = yi[CS_NY + k] - yi[k] - h * s;
   }
   G::sync();
-  // ---- LU with partial pivoting on the augmented matrix
+  // ---- fill [W | J | V_eff | f_a], all threads
+  for (int e = tid; e < CS_S * CS_NCOL; e += NT) {
+    const int row = e / CS_NCOL, col = e - row * CS_NCOL;
+    const int j = row / RB, a = row - j * RB;
+    const double* J = Jy + (size_t)(j * RB + a) * CS_JYC;
+    double v;
+    if (col < CS_S) {
+      const int k = col / RB, q = col - k * RB;
+      if (q < CS_NY) v = hA[j * CS_M + k] * J[q] - ((k == j && q == a) ? 1.0 : 0.0);
+      else v = (k == j) ? J[q] : 0.0;
+    } else {
+      const int c = col - CS_S;
+      if (c < CS_NY) v = J[c];
+      else if (c < CS_NY + CS_NPE) v = J[CS_NY + CS_NZ + (c - CS_NY)];
+      else v = fa[row];
+    }
+    Wm[row * CS_LDW + col] = v;
+  }
+  G::sync();
+  // ---- LU with partial pivoting (largest |entry|, first one on ties, as
+  //      matrix_factorization_cuda.py:133-146), trailing update spread over
+  //      all threads of the group
   int singular = 0;
 #pragma unroll 1
   for (int k = 0; k < CS_S; ++k) {
-    // pivot search over rows k..S-1 of column k (first maximum wins)
     double best = -1.0;
     int brow = k;
-    for (int r = k + tid; r < CS_S; r += G::NT) {
-      double v = fabs(Wm[(size_t)r * CS_LDW + k]);
+    for (int r = k + tid; r < CS_S; r += NT) {
+      const double v = fabs(Wm[r * CS_LDW + k]);
       if (v > best) { best = v; brow = r; }
     }
     for (int o = 16; o > 0; o >>= 1) {
-      double ob = __shfl_xor_sync(0xffffffffu, best, o);
-      int orow = __shfl_xor_sync(0xffffffffu, brow, o);
+      const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+      const int orow = __shfl_xor_sync(0xffffffffu, brow, o);
       if (ob > best || (ob == best && orow < brow)) { best = ob; brow = orow; }
     }
     if (GW > 1) {
-      if ((tid & 31) == 0) { pvv[tid >> 5] = best; piv[tid >> 5] = brow; }
+      if ((tid & 31) == 0) { red[tid >> 5] = best; red[GW + (tid >> 5)] = (double)brow; }
       __syncthreads();
-      best = pvv[0]; brow = piv[0];
+      best = red[0];
+      brow = (int)red[GW];
       for (int w = 1; w < GW; ++w) {
-        double ob = pvv[w];
-        int orow = piv[w];
+        const double ob = red[w];
+        const int orow = (int)red[GW + w];
         if (ob > best || (ob == best && orow < brow)) { best = ob; brow = orow; }
       }
       __syncthreads();
     }
     if (brow != k) {
-      for (int c = tid; c < CS_NCOL; c += G::NT) {
-        double tmp = Wm[(size_t)k * CS_LDW + c];
-        Wm[(size_t)k * CS_LDW + c] = Wm[(size_t)brow * CS_LDW + c];
-        Wm[(size_t)brow * CS_LDW + c] = tmp;
+      for (int c = tid; c < CS_NCOL; c += NT) {
+        const double tmp = Wm[k * CS_LDW + c];
+        Wm[k * CS_LDW + c] = Wm[brow * CS_LDW + c];
+        Wm[brow * CS_LDW + c] = tmp;
       }
       G::sync();
     }
-    const double pv = Wm[(size_t)k * CS_LDW + k];
+    const double pv = Wm[k * CS_LDW + k];
     if (fabs(pv) < 10.0 * CS_EPS) {
       singular = 1;
+      if (tid == 0) inv[k] = 1.0 / pv;
       G::sync();
       continue;
     }
-    const double inv = 1.0 / pv;
-    // multipliers
-    for (int r = k + 1 + tid; r < CS_S; r += G::NT) Wm[(size_t)r * CS_LDW + k] *= inv;
+    const double ip = 1.0 / pv;
+    if (tid == 0) inv[k] = ip;
+    for (int r = k + 1 + tid; r < CS_S; r += NT) Wm[r * CS_LDW + k] *= ip;
     G::sync();
-    // trailing update, threads over columns
-    for (int c = k + 1 + tid; c < CS_NCOL; c += G::NT) {
-      const double ukc = Wm[(size_t)k * CS_LDW + c];
-      for (int r = k + 1; r < CS_S; ++r) Wm[(size_t)r * CS_LDW + c] = fma(-Wm[(size_t)r * CS_LDW + k], ukc, Wm[(size_t)r * CS_LDW + c]);
+    const int nc = CS_NCOL - k - 1;
+    const int ne = (CS_S - k - 1) * nc;
+    for (int e = tid; e < ne; e += NT) {
+      const int rr = e / nc;
+      const int r = k + 1 + rr, c = k + 1 + (e - rr * nc);
+      Wm[r * CS_LDW + c] = fma(-Wm[r * CS_LDW + k], Wm[k * CS_LDW + c], Wm[r * CS_LDW + c]);
     }
     G::sync();
   }
-  // ---- back substitution, threads over right-hand-side columns
-  for (int c = CS_S + tid; c < CS_NCOL; c += G::NT) {
-    for (int r = CS_S - 1; r >= 0; --r) {
-      double xr = Wm[(size_t)r * CS_LDW + c] / Wm[(size_t)r * CS_LDW + r];
-      Wm[(size_t)r * CS_LDW + c] = xr;
-      for (int q = 0; q < r; ++q) Wm[(size_t)q * CS_LDW + c] = fma(-Wm[(size_t)q * CS_LDW + r], xr, Wm[(size_t)q * CS_LDW + c]);
+  // ---- back substitution, threads over (row, right-hand side) pairs
+#pragma unroll 1
+  for (int r = CS_S - 1; r >= 0; --r) {
+    if (tid < CS_NRHS) Wm[r * CS_LDW + CS_S + tid] *= inv[r];
+    G::sync();
+    const int ne = r * CS_NRHS;
+    for (int e = tid; e < ne; e += NT) {
+      const int q = e / CS_NRHS, c = e - q * CS_NRHS;
+      Wm[q * CS_LDW + CS_S + c] = fma(-Wm[q * CS_LDW + r], Wm[r * CS_LDW + CS_S + c], Wm[q * CS_LDW + CS_S + c]);
     }
+    G::sync();
   }
-  G::sync();
-  // ---- condensed block row and X
-  double* row = bt.rows0 + (size_t)slot * CS_ROWSZ;
+  // ---- X (column-major [NRHS][S]) and the condensed block row
   double* X = bt.X + (size_t)slot * CS_NRHS * CS_S;
-  for (int c = tid; c < CS_NRHS; c += G::NT) {
+  for (int e = tid; e < CS_NRHS * CS_S; e += NT) {
+    const int c = e / CS_S, r = e - c * CS_S;
+    X[e] = Wm[r * CS_LDW + CS_S + c];
+  }
+  double* row = bt.rows0 + (size_t)slot * CS_ROWSZ;
+  for (int e = tid; e < CS_NRHS * CS_NY; e += NT) {
+    const int c = e / CS_NY, a = e - c * CS_NY;
     const int col = CS_S + c;
-    for (int r = 0; r < CS_S; ++r) X[(size_t)c * CS_S + r] = Wm[(size_t)r * CS_LDW + col];
-    for (int a = 0; a < CS_NY; ++a) {
-      double s = 0.0;
-      for (int j = 0; j < CS_M; ++j) s += CS_B[j] * Wm[(size_t)(j * (CS_NY + CS_NZ) + a) * CS_LDW + col];
-      double dx = h * s;
-      if (c < CS_NY) {
-        row[c * CS_NY + a] = dx - (a == c ? 1.0 : 0.0);                 // A column c
-        row[(CS_NY + c) * CS_NY + a] = (a == c ? 1.0 : 0.0);             // C = I column c
-      } else if (c < CS_NY + CS_NPE) {
-        row[(2 * CS_NY + (c - CS_NY)) * CS_NY + a] = dx;                 // H
-      } else {
-        row[(2 * CS_NY + CS_NPE) * CS_NY + a] = -fb[a] - dx;             // b
-      }
+    double s = 0.0;
+    for (int j = 0; j < CS_M; ++j) s += CS_B[j] * Wm[(j * RB + a) * CS_LDW + col];
+    const double dx = h * s;
+    if (c < CS_NY) {
+      row[c * CS_NY + a] = dx - (a == c ? 1.0 : 0.0);          // A column c
+      row[(CS_NY + c) * CS_NY + a] = (a == c ? 1.0 : 0.0);      // C = I column c
+    } else if (c < CS_NY + CS_NPE) {
+      row[(2 * CS_NY + (c - CS_NY)) * CS_NY + a] = dx;          // H
+    } else {
+      row[(2 * CS_NY + CS_NPE) * CS_NY + a] = -fb[a] - dx;      // b
     }
   }
   if (singular && tid == 0) atomicAdd(&bt.inst[b].singular, 1);
-  (void)i;
 }
 
 template <int GW>
 __device__ __forceinline__ void cs_condense_entry(const CsBatch& bt) {
   extern __shared__ double smem[];
-  const int per = CS_S * CS_LDW + CS_NY + 2 * GW + 2;
+  const int per = CS_GRP_DBL(GW);
   const int njac = bt.nlist[1];
   const long long total = bt.jac_pre[njac];
   if (GW == 1) {
@@ -641,7 +670,7 @@ __device__ __forceinline__ void cs_condense_entry(const CsBatch& bt) {
       const int k = cs_find(bt.jac_pre, njac, it);
       const int b = bt.jac[k];
       const int slot = bt.off[b] + (int)(it - bt.jac_pre[k]);
-      cs_condense_group<1>(bt, slot, Wm, Wm + CS_S * CS_LDW);
+      cs_condense_group<1>(bt, slot, Wm);
       __syncwarp();
     }
   } else {
@@ -649,7 +678,7 @@ __device__ __forceinline__ void cs_condense_entry(const CsBatch& bt) {
       const int k = cs_find(bt.jac_pre, njac, it);
       const int b = bt.jac[k];
       const int slot = bt.off[b] + (int)(it - bt.jac_pre[k]);
-      cs_condense_group<GW>(bt, slot, smem, smem + CS_S * CS_LDW);
+      cs_condense_group<GW>(bt, slot, smem);
       __syncthreads();
     }
   }
@@ -729,6 +758,91 @@ __device__ void cs_merge_warp(const double* ra, const double* rb, double* out_ro
   __syncwarp();
 }
 
+// Small blocks (2 NY x QC doubles fit in registers): one thread per merge,
+// fully unrolled, the same Householder steps as cs_merge_warp.
+#define CS_TREE_THREAD (2 * CS_NY * CS_QC <= 128)
+#if CS_TREE_THREAD
+__device__ __forceinline__ void cs_merge_thread(const double* __restrict__ ra, const double* __restrict__ rb,
+                                                double* __restrict__ out_row, double* __restrict__ rec) {
+  double Q[CS_QC][2 * CS_NY];
+#pragma unroll
+  for (int c = 0; c < CS_QC; ++c)
+#pragma unroll
+    for (int r = 0; r < CS_NY; ++r) {
+      double top, bot;
+      if (c < CS_NY) { top = ra[(CS_NY + c) * CS_NY + r]; bot = rb[c * CS_NY + r]; }
+      else if (c < 2 * CS_NY) { top = ra[(c - CS_NY) * CS_NY + r]; bot = 0.0; }
+      else if (c < 3 * CS_NY) { top = 0.0; bot = rb[(CS_NY + c - 2 * CS_NY) * CS_NY + r]; }
+      else if (c < 3 * CS_NY + CS_NPE) { top = ra[(2 * CS_NY + c - 3 * CS_NY) * CS_NY + r]; bot = rb[(2 * CS_NY + c - 3 * CS_NY) * CS_NY + r]; }
+      else { top = ra[(2 * CS_NY + CS_NPE) * CS_NY + r]; bot = rb[(2 * CS_NY + CS_NPE) * CS_NY + r]; }
+      Q[c][r] = top;
+      Q[c][CS_NY + r] = bot;
+    }
+#pragma unroll
+  for (int k = 0; k < CS_NY; ++k) {
+    double ss = 0.0;
+#pragma unroll
+    for (int r = k; r < 2 * CS_NY; ++r) ss = fma(Q[k][r], Q[k][r], ss);
+    const double x0 = Q[k][k];
+    const double g = (x0 >= 0.0) ? -sqrt(ss) : sqrt(ss);
+    const double v0 = x0 - g;
+    const double vs = ss - x0 * x0 + v0 * v0;
+    if (vs >= CS_EPS) {
+      const double beta = -2.0 / vs;
+#pragma unroll
+      for (int c = k + 1; c < CS_QC; ++c) {
+        double w = v0 * Q[c][k];
+#pragma unroll
+        for (int r = k + 1; r < 2 * CS_NY; ++r) w = fma(Q[k][r], Q[c][r], w);
+        const double bw = beta * w;
+        Q[c][k] = fma(bw, v0, Q[c][k]);
+#pragma unroll
+        for (int r = k + 1; r < 2 * CS_NY; ++r) Q[c][r] = fma(bw, Q[k][r], Q[c][r]);
+      }
+      Q[k][k] = g;
+#pragma unroll
+      for (int r = k + 1; r < 2 * CS_NY; ++r) Q[k][r] = 0.0;
+    }
+  }
+#pragma unroll
+  for (int c = 0; c < CS_QC; ++c) {
+#pragma unroll
+    for (int r = 0; r < CS_NY; ++r) rec[c * CS_NY + r] = Q[c][r];
+    if (c >= CS_NY) {
+#pragma unroll
+      for (int r = 0; r < CS_NY; ++r) out_row[(c - CS_NY) * CS_NY + r] = Q[c][CS_NY + r];
+    }
+  }
+}
+
+__device__ __forceinline__ void cs_backsub_thread(const double* __restrict__ rec, const double* __restrict__ yl,
+                                                  const double* __restrict__ yr, const double* __restrict__ dpv,
+                                                  double* __restrict__ ym) {
+  double v[CS_NY];
+#pragma unroll
+  for (int a = 0; a < CS_NY; ++a) {
+    double s = rec[(3 * CS_NY + CS_NPE) * CS_NY + a];
+#pragma unroll
+    for (int c = 0; c < CS_NY; ++c) s -= rec[(CS_NY + c) * CS_NY + a] * yl[c];
+#pragma unroll
+    for (int c = 0; c < CS_NY; ++c) s -= rec[(2 * CS_NY + c) * CS_NY + a] * yr[c];
+#pragma unroll
+    for (int c = 0; c < CS_NPE; ++c) s -= rec[(3 * CS_NY + c) * CS_NY + a] * dpv[c];
+    v[a] = s;
+  }
+#pragma unroll
+  for (int r = CS_NY - 1; r >= 0; --r) {
+    const double rr = rec[r * CS_NY + r];
+    const double xr = (rr != 0.0) ? v[r] / rr : 0.0;
+    v[r] = xr;
+#pragma unroll
+    for (int a = 0; a < r; ++a) v[a] -= rec[r * CS_NY + a] * xr;
+  }
+#pragma unroll
+  for (int a = 0; a < CS_NY; ++a) ym[a] = v[a];
+}
+#endif
+
 // y_m = R^-1 (d - G y_l - E y_r - J p), one warp, lanes over rows
 __device__ void cs_backsub_warp(const double* rec, const double* yl, const double* yr, const double* dpv, double* ym) {
   const int lane = threadIdx.x & 31;
@@ -768,6 +882,34 @@ __device__ void cs_backsub_warp(const double* rec, const double* yl, const doubl
 // item; item mi < merges eliminates node (2 mi + 1) 2^l between rows 2 mi and
 // 2 mi + 1, the last item of an odd level carries its row up unchanged.
 extern "C" __global__ void k_tree_level(CsBatch bt, int l) {
+#if CS_TREE_THREAD
+  {
+    const int njac = bt.nlist[1];
+    const long long* pre = bt.lvl_pre + (size_t)l * (bt.B + 1);
+    const long long total = pre[njac];
+    const double* srcb = (l & 1) ? bt.rows1 : bt.rows0;
+    double* dstb = (l & 1) ? bt.rows0 : bt.rows1;
+    for (long long it = (long long)blockIdx.x * blockDim.x + threadIdx.x; it < total; it += (long long)gridDim.x * blockDim.x) {
+      const int k = cs_find(pre, njac, it);
+      const int b = bt.jac[k];
+      const int mi = (int)(it - pre[k]);
+      const int off = bt.off[b];
+      const int nl = cs_rows_at(bt.N[b] - 1, l);
+      const int merges = nl >> 1;
+      const double* src = srcb + (size_t)off * CS_ROWSZ;
+      double* dst = dstb + (size_t)off * CS_ROWSZ;
+      if (mi < merges) {
+        cs_merge_thread(src + (size_t)(2 * mi) * CS_ROWSZ, src + (size_t)(2 * mi + 1) * CS_ROWSZ,
+                        dst + (size_t)mi * CS_ROWSZ, bt.tree + (size_t)(off + ((2 * mi + 1) << l)) * CS_TREESZ);
+      } else {
+        const double* sr = src + (size_t)(nl - 1) * CS_ROWSZ;
+        double* dr = dst + (size_t)merges * CS_ROWSZ;
+        for (int q = 0; q < CS_ROWSZ; ++q) dr[q] = sr[q];
+      }
+    }
+    return;
+  }
+#endif
   extern __shared__ double smem[];
   const int wpc = blockDim.x >> 5, w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   double* Qw = smem + (size_t)w * CS_QLD * CS_QC;
@@ -897,6 +1039,29 @@ extern "C" __global__ void k_top(CsBatch bt) {
 
 // Back substitution of one tree level (top-down), warp per merge.
 extern "C" __global__ void k_backsub_level(CsBatch bt, int l) {
+#if CS_TREE_THREAD
+  {
+    const int njac = bt.nlist[1];
+    const long long* pre = bt.lvl_pre + (size_t)l * (bt.B + 1);
+    const long long total = pre[njac];
+    for (long long it = (long long)blockIdx.x * blockDim.x + threadIdx.x; it < total; it += (long long)gridDim.x * blockDim.x) {
+      const int k = cs_find(pre, njac, it);
+      const int b = bt.jac[k];
+      const int mi = (int)(it - pre[k]);
+      const int n0 = bt.N[b] - 1;
+      const int merges = cs_rows_at(n0, l) >> 1;
+      if (mi >= merges) continue;
+      const int off = bt.off[b];
+      const int mid = (2 * mi + 1) << l;
+      const int left = (2 * mi) << l;
+      int right = (2 * mi + 2) << l;
+      if (right > n0) right = n0;
+      cs_backsub_thread(bt.tree + (size_t)(off + mid) * CS_TREESZ, bt.dy + (size_t)(off + left) * CS_NY,
+                        bt.dy + (size_t)(off + right) * CS_NY, bt.dp + (size_t)b * CS_NP, bt.dy + (size_t)(off + mid) * CS_NY);
+    }
+    return;
+  }
+#endif
   const int wpc = blockDim.x >> 5, w = threadIdx.x >> 5;
   const int njac = bt.nlist[1];
   const long long* pre = bt.lvl_pre + (size_t)l * (bt.B + 1);

@@ -310,12 +310,16 @@ extern "C" int cs_module_load(const cs_module_desc* d, cs_module** out) {
   M->nrhs = d->ny + d->np_eff + 1;
   M->rowsz = (size_t)d->ny * (2 * d->ny + d->np_eff + 1);
   M->treesz = (size_t)d->ny * (3 * d->ny + d->np_eff + 1);
-  // condensation: shared memory for one augmented matrix per group
+  // condensation: shared memory of one group (matches CS_GRP_DBL in cs_kernels.cuh)
   const int ldw = (M->s + M->nrhs) | 1;
-  const size_t per_mat = ((size_t)M->s * ldw + M->ny + 2 * 8 + 2) * sizeof(double);
+  const int rb = d->ny + d->nz, jyc = d->ny + d->nz + d->np_eff;
+  auto grp_bytes = [&](int gw) {
+    return ((size_t)M->s * ldw + (size_t)d->m * rb * jyc + (size_t)d->m * rb + (size_t)d->m * d->m + d->ny + M->s +
+            2 * gw + 2) * sizeof(double);
+  };
   int cgw = 1;
   if (M->s > 48) cgw = 8;  // one CTA of 8 warps per interval
-  size_t per = (cgw == 1) ? ((size_t)M->s * ldw + M->ny + 2 * 1 + 2) * sizeof(double) : per_mat;
+  size_t per = grp_bytes(cgw);
   if (per > (size_t)smem_optin) {
     delete M;
     return set_err(CS_ERR_INVALID, "cs_module_load: stage system of size " + std::to_string(M->s) +
