@@ -14,9 +14,6 @@
 //                                                  and its integral I_k at the
 //                                                  (M+1) Gauss points
 //   CS_L0[M], CS_L1[M]    basis at t = 0 and t = 1
-//   CS_CGW                warps per condensation group (1: one warp per
-//                         interval, several intervals per CTA; >1: one CTA
-//                         per interval)
 //
 // Data layout in HBM (batch of B instances, packed by node):
 //   instance b owns node slots off[b] .. off[b]+N[b]-1; interval i of b uses
@@ -466,15 +463,6 @@ extern "C" __global__ void k_lists(CsBatch bt, int mode, int nlvl) {
 // matrix_factorization_cuda.py:133-146), back substitution, then
 //   A = -I + D X_J, H = D X_V, b = -f_b - D X_f  with D = h b_j I on y rows,
 // written as the level-0 block row [A | C=I | H | b]; X kept for recovery.
-template <int GW>
-struct CsGroup {
-  static constexpr int NT = 32 * GW;
-  __device__ static __forceinline__ int tid() { return GW == 1 ? (int)(threadIdx.x & 31) : (int)threadIdx.x; }
-  __device__ static __forceinline__ void sync() {
-    if (GW == 1) __syncwarp(); else __syncthreads();
-  }
-};
-
 // Shared memory of one condensation group (doubles):
 //   Wm    [S][LDW]                 augmented matrix [W | J | V_eff | f_a]
 //   Jy    [M][NY+NZ][NY+NZ+NPE]    stage Jacobian rows [h_y h_z h_p ; g_y g_z g_p]
@@ -482,14 +470,35 @@ struct CsGroup {
 //   hA    [M][M]                   h * A
 //   fb    [NY]                     f_b
 //   inv   [S]                      reciprocal pivots
-//   red   [2 GW]                   cross-warp pivot search (GW > 1)
+//   red   [2 * 8]                  cross-warp pivot search (CTA groups)
 #define CS_JYC (CS_NY + CS_NZ + CS_NPE)
-#define CS_GRP_DBL(GW) (CS_S * CS_LDW + CS_M * (CS_NY + CS_NZ) * CS_JYC + CS_M * (CS_NY + CS_NZ) + CS_M * CS_M + CS_NY + CS_S + 2 * (GW) + 2)
+#define CS_GRP_DBL (CS_S * CS_LDW + CS_M * (CS_NY + CS_NZ) * CS_JYC + CS_M * (CS_NY + CS_NZ) + CS_M * CS_M + CS_NY + CS_S + 18)
 
-template <int GW>
-__device__ void cs_condense_group(const CsBatch& bt, int slot, double* Wm) {
-  typedef CsGroup<GW> G;
-  constexpr int NT = G::NT;
+// A group of GL threads condenses one interval: GL = 8 or 16 (sub-warp:
+// several intervals per warp, so that the per-column work of the
+// elimination -- pivot search, reciprocal -- serves several intervals per
+// warp instruction), 32 (a warp) or 32*k (a CTA).
+template <int GL>
+struct CsGrp {
+  static constexpr bool CTA = GL > 32;
+  __device__ static __forceinline__ int tid() { return CTA ? (int)threadIdx.x : (int)(threadIdx.x & (GL - 1)); }
+  __device__ static __forceinline__ void sync() {
+    if (CTA) __syncthreads(); else __syncwarp();
+  }
+};
+
+// |x| as an integer key: for non-negative doubles the order of the bit
+// patterns is the order of the values, so the pivot search needs no FP64
+// comparisons (the FP64 pipe is the bottleneck of this kernel).
+__device__ __forceinline__ unsigned long long cs_abskey(double v) {
+  return (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffull;
+}
+
+// `active` is false for a filler group of a partly used warp: it computes on a
+// valid interval but writes nothing.
+template <int GL>
+__device__ void cs_condense_group(const CsBatch& bt, int slot, bool active, double* Wm, double* red) {
+  typedef CsGrp<GL> G;
   constexpr int RB = CS_NY + CS_NZ;  // rows per stage block
   const int tid = G::tid();
   double* Jy = Wm + CS_S * CS_LDW;
@@ -497,14 +506,13 @@ __device__ void cs_condense_group(const CsBatch& bt, int slot, double* Wm) {
   double* hA = fa + CS_M * RB;
   double* fb = hA + CS_M * CS_M;
   double* inv = fb + CS_NY;
-  double* red = inv + CS_S;
   const int b = bt.inst_of[slot];
   const double h = bt.t[slot + 1] - bt.t[slot];
   const double* th = bt.th + (size_t)b * (CS_NTH > 0 ? CS_NTH : 1);
   const double* yi = bt.y + (size_t)slot * CS_NY;
   const double* yd = bt.ydot + (size_t)slot * CS_M * CS_NY;
   // ---- stage Jacobians and residuals: thread j handles stage j
-  for (int j = tid; j < CS_M; j += NT) {
+  for (int j = tid; j < CS_M; j += GL) {
     double pl[CS_NP > 0 ? CS_NP : 1];
     for (int k = 0; k < CS_NP; ++k) pl[k] = bt.p[(size_t)b * CS_NP + k];
     double yt[CS_NY], zl[CS_NZ > 0 ? CS_NZ : 1];
@@ -536,23 +544,27 @@ __device__ void cs_condense_group(const CsBatch& bt, int slot, double* Wm) {
     }
 #endif
   }
-  for (int e = tid; e < CS_M * CS_M; e += NT) hA[e] = h * CS_A[e];
-  for (int k = tid; k < CS_NY; k += NT) {
+  for (int e = tid; e < CS_M * CS_M; e += GL) hA[e] = h * CS_A[e];
+  for (int k = tid; k < CS_NY; k += GL) {
     double s = 0.0;
     for (int j = 0; j < CS_M; ++j) s += CS_B[j] * yd[j * CS_NY + k];
     fb[k] = yi[CS_NY + k] - yi[k] - h * s;
   }
   G::sync();
-  // ---- fill [W | J | V_eff | f_a], all threads
-  for (int e = tid; e < CS_S * CS_NCOL; e += NT) {
+  // ---- fill [W | J | V_eff | f_a]
+  for (int e = tid; e < CS_S * CS_NCOL; e += GL) {
     const int row = e / CS_NCOL, col = e - row * CS_NCOL;
     const int j = row / RB, a = row - j * RB;
     const double* J = Jy + (size_t)(j * RB + a) * CS_JYC;
     double v;
     if (col < CS_S) {
       const int k = col / RB, q = col - k * RB;
-      if (q < CS_NY) v = hA[j * CS_M + k] * J[q] - ((k == j && q == a) ? 1.0 : 0.0);
-      else v = (k == j) ? J[q] : 0.0;
+      if (q < CS_NY) {
+        v = hA[j * CS_M + k] * J[q];
+        if (k == j && q == a) v -= 1.0;
+      } else {
+        v = (k == j) ? J[q] : 0.0;
+      }
     } else {
       const int c = col - CS_S;
       if (c < CS_NY) v = J[c];
@@ -562,57 +574,58 @@ __device__ void cs_condense_group(const CsBatch& bt, int slot, double* Wm) {
     Wm[row * CS_LDW + col] = v;
   }
   G::sync();
-  // ---- LU with partial pivoting (largest |entry|, first one on ties, as
-  //      matrix_factorization_cuda.py:133-146), trailing update spread over
-  //      all threads of the group
+  // ---- LU with partial pivoting: largest |entry| in the column, the first
+  //      such row on ties (as matrix_factorization_cuda.py:133-146)
   int singular = 0;
 #pragma unroll 1
   for (int k = 0; k < CS_S; ++k) {
-    double best = -1.0;
-    int brow = k;
-    for (int r = k + tid; r < CS_S; r += NT) {
-      const double v = fabs(Wm[r * CS_LDW + k]);
-      if (v > best) { best = v; brow = r; }
+    unsigned long long best = 0ull;
+    int brow = CS_S;  // larger than any row: loses every tie
+    for (int r = k + tid; r < CS_S; r += GL) {
+      const unsigned long long v = cs_abskey(Wm[r * CS_LDW + k]);
+      if (v > best || brow == CS_S) { best = v; brow = r; }
     }
-    for (int o = 16; o > 0; o >>= 1) {
-      const double ob = __shfl_xor_sync(0xffffffffu, best, o);
-      const int orow = __shfl_xor_sync(0xffffffffu, brow, o);
+    constexpr int W = CsGrp<GL>::CTA ? 32 : GL;
+    for (int o = W >> 1; o > 0; o >>= 1) {
+      const unsigned long long ob = __shfl_xor_sync(0xffffffffu, best, o, W);
+      const int orow = __shfl_xor_sync(0xffffffffu, brow, o, W);
       if (ob > best || (ob == best && orow < brow)) { best = ob; brow = orow; }
     }
-    if (GW > 1) {
-      if ((tid & 31) == 0) { red[tid >> 5] = best; red[GW + (tid >> 5)] = (double)brow; }
+    if (CsGrp<GL>::CTA) {
+      constexpr int NW = GL / 32;
+      if ((tid & 31) == 0) {
+        red[tid >> 5] = __longlong_as_double((long long)best);
+        red[NW + (tid >> 5)] = (double)brow;
+      }
       __syncthreads();
-      best = red[0];
-      brow = (int)red[GW];
-      for (int w = 1; w < GW; ++w) {
-        const double ob = red[w];
-        const int orow = (int)red[GW + w];
+      best = (unsigned long long)__double_as_longlong(red[0]);
+      brow = (int)red[NW];
+      for (int w = 1; w < NW; ++w) {
+        const unsigned long long ob = (unsigned long long)__double_as_longlong(red[w]);
+        const int orow = (int)red[NW + w];
         if (ob > best || (ob == best && orow < brow)) { best = ob; brow = orow; }
       }
       __syncthreads();
     }
-    if (brow != k) {
-      for (int c = tid; c < CS_NCOL; c += NT) {
-        const double tmp = Wm[k * CS_LDW + c];
-        Wm[k * CS_LDW + c] = Wm[brow * CS_LDW + c];
-        Wm[brow * CS_LDW + c] = tmp;
-      }
-      G::sync();
+    // swap rows k and brow (a self-swap when the pivot is in place)
+    for (int c = tid; c < CS_NCOL; c += GL) {
+      const double tmp = Wm[k * CS_LDW + c];
+      Wm[k * CS_LDW + c] = Wm[brow * CS_LDW + c];
+      Wm[brow * CS_LDW + c] = tmp;
     }
+    G::sync();
     const double pv = Wm[k * CS_LDW + k];
-    if (fabs(pv) < 10.0 * CS_EPS) {
-      singular = 1;
-      if (tid == 0) inv[k] = 1.0 / pv;
-      G::sync();
-      continue;
-    }
+    // |pv| < 10 eps: the reference leaves this column uneliminated
+    const bool tiny = cs_abskey(pv) < 0x3ce4000000000000ull;  // bits of 10 * 2^-52 = 2.22e-15
+    singular |= tiny;
     const double ip = 1.0 / pv;
     if (tid == 0) inv[k] = ip;
-    for (int r = k + 1 + tid; r < CS_S; r += NT) Wm[r * CS_LDW + k] *= ip;
+    const double mul = tiny ? 0.0 : ip;
+    for (int r = k + 1 + tid; r < CS_S; r += GL) Wm[r * CS_LDW + k] *= mul;
     G::sync();
     const int nc = CS_NCOL - k - 1;
     const int ne = (CS_S - k - 1) * nc;
-    for (int e = tid; e < ne; e += NT) {
+    for (int e = tid; e < ne; e += GL) {
       const int rr = e / nc;
       const int r = k + 1 + rr, c = k + 1 + (e - rr * nc);
       Wm[r * CS_LDW + c] = fma(-Wm[r * CS_LDW + k], Wm[k * CS_LDW + c], Wm[r * CS_LDW + c]);
@@ -622,30 +635,31 @@ __device__ void cs_condense_group(const CsBatch& bt, int slot, double* Wm) {
   // ---- back substitution, threads over (row, right-hand side) pairs
 #pragma unroll 1
   for (int r = CS_S - 1; r >= 0; --r) {
-    if (tid < CS_NRHS) Wm[r * CS_LDW + CS_S + tid] *= inv[r];
+    for (int c = tid; c < CS_NRHS; c += GL) Wm[r * CS_LDW + CS_S + c] *= inv[r];
     G::sync();
     const int ne = r * CS_NRHS;
-    for (int e = tid; e < ne; e += NT) {
+    for (int e = tid; e < ne; e += GL) {
       const int q = e / CS_NRHS, c = e - q * CS_NRHS;
       Wm[q * CS_LDW + CS_S + c] = fma(-Wm[q * CS_LDW + r], Wm[r * CS_LDW + CS_S + c], Wm[q * CS_LDW + CS_S + c]);
     }
     G::sync();
   }
+  if (!active) return;
   // ---- X (column-major [NRHS][S]) and the condensed block row
   double* X = bt.X + (size_t)slot * CS_NRHS * CS_S;
-  for (int e = tid; e < CS_NRHS * CS_S; e += NT) {
+  for (int e = tid; e < CS_NRHS * CS_S; e += GL) {
     const int c = e / CS_S, r = e - c * CS_S;
     X[e] = Wm[r * CS_LDW + CS_S + c];
   }
   double* row = bt.rows0 + (size_t)slot * CS_ROWSZ;
-  for (int e = tid; e < CS_NRHS * CS_NY; e += NT) {
+  for (int e = tid; e < CS_NRHS * CS_NY; e += GL) {
     const int c = e / CS_NY, a = e - c * CS_NY;
     const int col = CS_S + c;
     double s = 0.0;
     for (int j = 0; j < CS_M; ++j) s += CS_B[j] * Wm[(j * RB + a) * CS_LDW + col];
     const double dx = h * s;
     if (c < CS_NY) {
-      row[c * CS_NY + a] = dx - (a == c ? 1.0 : 0.0);          // A column c
+      row[c * CS_NY + a] = (a == c) ? dx - 1.0 : dx;            // A column c
       row[(CS_NY + c) * CS_NY + a] = (a == c ? 1.0 : 0.0);      // C = I column c
     } else if (c < CS_NY + CS_NPE) {
       row[(2 * CS_NY + (c - CS_NY)) * CS_NY + a] = dx;          // H
@@ -656,35 +670,45 @@ __device__ void cs_condense_group(const CsBatch& bt, int slot, double* Wm) {
   if (singular && tid == 0) atomicAdd(&bt.inst[b].singular, 1);
 }
 
-template <int GW>
+// lanes per condensation group, from the size of the stage system
+#define CS_CGL ((CS_S > 48) ? 256 : ((CS_S > 32) ? 16 : 8))
+
 __device__ __forceinline__ void cs_condense_entry(const CsBatch& bt) {
   extern __shared__ double smem[];
-  const int per = CS_GRP_DBL(GW);
+  constexpr int GL = CS_CGL;
   const int njac = bt.nlist[1];
   const long long total = bt.jac_pre[njac];
-  if (GW == 1) {
+  if (total == 0) return;
+  if (GL <= 32) {
+    constexpr int GPW = 32 / GL;                  // groups per warp
     const int wpc = blockDim.x >> 5;
     const int w = threadIdx.x >> 5;
-    double* Wm = smem + (size_t)w * per;
-    for (long long it = (long long)blockIdx.x * wpc + w; it < total; it += (long long)gridDim.x * wpc) {
+    const int gi = (threadIdx.x & 31) / GL;       // group within the warp
+    double* Wm = smem + (size_t)(w * GPW + gi) * CS_GRP_DBL;
+    for (long long base = ((long long)blockIdx.x * wpc + w) * GPW; base < total;
+         base += (long long)gridDim.x * wpc * GPW) {
+      long long it = base + gi;
+      const bool active = it < total;
+      if (!active) it = total - 1;
       const int k = cs_find(bt.jac_pre, njac, it);
       const int b = bt.jac[k];
       const int slot = bt.off[b] + (int)(it - bt.jac_pre[k]);
-      cs_condense_group<1>(bt, slot, Wm);
+      cs_condense_group<GL>(bt, slot, active, Wm, nullptr);
       __syncwarp();
     }
   } else {
+    double* red = smem + CS_GRP_DBL;
     for (long long it = blockIdx.x; it < total; it += gridDim.x) {
       const int k = cs_find(bt.jac_pre, njac, it);
       const int b = bt.jac[k];
       const int slot = bt.off[b] + (int)(it - bt.jac_pre[k]);
-      cs_condense_group<GW>(bt, slot, smem);
+      cs_condense_group<GL>(bt, slot, true, smem, red);
       __syncthreads();
     }
   }
 }
 
-extern "C" __global__ void k_condense(CsBatch bt) { cs_condense_entry<CS_CGW>(bt); }
+extern "C" __global__ void k_condense(CsBatch bt) { cs_condense_entry(bt); }
 
 // ------------------------------------------------------------------------
 // BABD solve, one CTA per instance: tree of pairwise QR eliminations over

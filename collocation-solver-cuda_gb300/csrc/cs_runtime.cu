@@ -230,12 +230,11 @@ struct cs_module {
   int condense_grid = 1;
 };
 
-static std::string build_source(const cs_module_desc* d, int cgw) {
+static std::string build_source(const cs_module_desc* d) {
   std::ostringstream o;
   o << "// generated prelude\n";
   o << "#define CS_NY " << d->ny << "\n#define CS_NZ " << d->nz << "\n#define CS_NP " << d->np << "\n";
   o << "#define CS_NPE " << d->np_eff << "\n#define CS_NTH " << d->n_theta << "\n#define CS_M " << d->m << "\n";
-  o << "#define CS_CGW " << cgw << "\n";
   const int m = d->m;
   o << "__constant__ double CS_A[" << m * m << "] = {" << fmt_array(d->lobatto_A, m * m) << "};\n";
   o << "__constant__ double CS_B[" << m << "] = {" << fmt_array(d->lobatto_b, m) << "};\n";
@@ -310,32 +309,33 @@ extern "C" int cs_module_load(const cs_module_desc* d, cs_module** out) {
   M->nrhs = d->ny + d->np_eff + 1;
   M->rowsz = (size_t)d->ny * (2 * d->ny + d->np_eff + 1);
   M->treesz = (size_t)d->ny * (3 * d->ny + d->np_eff + 1);
-  // condensation: shared memory of one group (matches CS_GRP_DBL in cs_kernels.cuh)
+  // condensation: shared memory of one group (CS_GRP_DBL in cs_kernels.cuh) and
+  // lanes per group (CS_GL): 8 lanes for small stage systems (4 intervals per
+  // warp), a warp for medium, a CTA of 256 threads for large ones
   const int ldw = (M->s + M->nrhs) | 1;
   const int rb = d->ny + d->nz, jyc = d->ny + d->nz + d->np_eff;
-  auto grp_bytes = [&](int gw) {
-    return ((size_t)M->s * ldw + (size_t)d->m * rb * jyc + (size_t)d->m * rb + (size_t)d->m * d->m + d->ny + M->s +
-            2 * gw + 2) * sizeof(double);
-  };
-  int cgw = 1;
-  if (M->s > 48) cgw = 8;  // one CTA of 8 warps per interval
-  size_t per = grp_bytes(cgw);
-  if (per > (size_t)smem_optin) {
+  const size_t grp = ((size_t)M->s * ldw + (size_t)d->m * rb * jyc + (size_t)d->m * rb + (size_t)d->m * d->m + d->ny +
+                      M->s + 18) * sizeof(double);
+  const int ncol = M->s + M->nrhs;
+  const int gl = (M->s > 48) ? 256 : ((M->s > 32) ? 16 : 8);
+  (void)ncol;
+  if (grp + (gl > 32 ? 16 * sizeof(double) : 0) > (size_t)smem_optin) {
     delete M;
     return set_err(CS_ERR_INVALID, "cs_module_load: stage system of size " + std::to_string(M->s) +
                                        " does not fit in shared memory");
   }
-  M->cgw = cgw;
-  if (cgw == 1) {
-    int per_cta = (int)std::min<size_t>(4, (size_t)smem_optin / per);
-    if (per_cta < 1) per_cta = 1;
-    M->condense_per_cta = per_cta;
-    M->condense_block = 32 * per_cta;
-    M->condense_smem = per * per_cta;
+  M->cgw = gl;
+  if (gl <= 32) {
+    const int gpw = 32 / gl;
+    int wpc = (int)std::min<size_t>(4, (size_t)smem_optin / (grp * gpw));
+    if (wpc < 1) wpc = 1;
+    M->condense_per_cta = wpc * gpw;
+    M->condense_block = 32 * wpc;
+    M->condense_smem = grp * gpw * wpc;
   } else {
     M->condense_per_cta = 1;
-    M->condense_block = 32 * cgw;
-    M->condense_smem = per;
+    M->condense_block = gl;
+    M->condense_smem = grp + 16 * sizeof(double);
   }
   // BABD tree: a merge matrix per warp (4 warps per CTA); top: one system per warp
   const int qld = (2 * M->ny) | 1, qc = 3 * M->ny + M->npe + 1;
@@ -350,7 +350,7 @@ extern "C" int cs_module_load(const cs_module_desc* d, cs_module** out) {
   M->top_smem = top_per * M->top_wpc;
   CS_CUDA(cudaDeviceGetAttribute(&M->sms, cudaDevAttrMultiProcessorCount, dev));
 
-  std::string src = build_source(d, cgw);
+  std::string src = build_source(d);
   std::string cache = d->cache_dir ? d->cache_dir : "";
   if (cache.empty()) {
     const char* env = getenv("CS_GB300_CACHE");

@@ -10,6 +10,7 @@ instances in HBM.
 """
 import ctypes
 import os
+import sys
 
 import numpy as np
 
@@ -34,15 +35,12 @@ def kernel_program_text(problem, m):
     compile checks; the library builds the same text at run time)."""
     pc = ProblemCode(problem.sym)
     t = _tables(m)
-    s = m * (pc.ny + pc.nz)
-    cgw = 8 if s > 48 else 1
 
     def arr(name, a):
         return "__constant__ double %s[%d] = {%s};\n" % (name, a.size, ",".join("%.17e" % v for v in a) or "0.0")
 
     out = "#define CS_NY %d\n#define CS_NZ %d\n#define CS_NP %d\n#define CS_NPE %d\n#define CS_NTH %d\n#define CS_M %d\n" % (
         pc.ny, pc.nz, pc.np, pc.np_eff, pc.nth, m)
-    out += "#define CS_CGW %d\n" % cgw
     out += arr("CS_A", t["A"]) + arr("CS_B", t["b"]) + arr("CS_C", t["c"]) + arr("CS_GW", t["gw"])
     out += arr("CS_GL", t["gL"]) + arr("CS_GI", t["gI"]) + arr("CS_L0", t["L0"]) + arr("CS_L1", t["L1"])
     out += cuda_problem_source(pc)
@@ -78,6 +76,8 @@ class CompiledProblem:
         self._lib = lib
 
     def __del__(self):
+        if sys.is_finalizing():  # the CUDA runtime may already be gone
+            return
         try:
             if getattr(self, "handle", None):
                 self._lib.cs_module_free(self.handle)
@@ -116,6 +116,8 @@ class Batch:
         self._lib = lib
 
     def __del__(self):
+        if sys.is_finalizing():
+            return
         try:
             if getattr(self, "handle", None):
                 self._lib.cs_batch_free(self.handle)
@@ -293,6 +295,8 @@ class PinnedArray:
         self.array = np.frombuffer(buf, dtype=dtype, count=int(np.prod(shape))).reshape(shape)
 
     def __del__(self):
+        if sys.is_finalizing():
+            return
         try:
             if self.ptr:
                 self._lib.cs_pinned_free(self.ptr)
