@@ -463,16 +463,36 @@ extern "C" __global__ void k_lists(CsBatch bt, int mode, int nlvl) {
 // matrix_factorization_cuda.py:133-146), back substitution, then
 //   A = -I + D X_J, H = D X_V, b = -f_b - D X_f  with D = h b_j I on y rows,
 // written as the level-0 block row [A | C=I | H | b]; X kept for recovery.
+// Structure used by the condensation: Lobatto IIIA has A[0][:] = 0 (the first
+// stage is the left node), so the stage-0 block row of W is
+//   [ -I  h_z0 | 0 ... 0 ]
+//   [  0  g_z0 | 0 ... 0 ]
+// and W is block lower triangular with that block first.  The stage-0
+// unknowns are solved directly (an NZ x NZ solve with g_z0), their coupling
+// W10 (= h A[j][0] [h_y; g_y] of the later stages, y-columns only) is moved
+// to the right-hand side, and partial-pivot LU runs on the remaining
+// S1 = (M-1)(NY+NZ) rows only.  The reference factorises the whole W
+// (collocation_solver_parallel_2d_shared.py:887-1001); the solution is the
+// same up to rounding.
+//
 // Shared memory of one condensation group (doubles):
-//   Wm    [S][LDW]                 augmented matrix [W | J | V_eff | f_a]
+//   Wm    [S1][LDW1]               reduced augmented matrix [W11 | R1']
 //   Jy    [M][NY+NZ][NY+NZ+NPE]    stage Jacobian rows [h_y h_z h_p ; g_y g_z g_p]
 //   fa    [M][NY+NZ]               stage residuals
 //   hA    [M][M]                   h * A
 //   fb    [NY]                     f_b
-//   inv   [S]                      reciprocal pivots
-//   red   [2 * 8]                  cross-warp pivot search (CTA groups)
+//   X0    [NY+NZ][NRHS]            stage-0 rows of X = W^-1 [J V f_a]
+//   inv   [S1]                     reciprocal pivots
+//   red   [16]                     cross-warp pivot search (CTA groups)
+#define CS_RB (CS_NY + CS_NZ)
+#define CS_S1 ((CS_M - 1) * CS_RB)
+#define CS_NCOL1 (CS_S1 + CS_NRHS)
+#define CS_LDW1 (CS_NCOL1 | 1)
 #define CS_JYC (CS_NY + CS_NZ + CS_NPE)
-#define CS_GRP_DBL (CS_S * CS_LDW + CS_M * (CS_NY + CS_NZ) * CS_JYC + CS_M * (CS_NY + CS_NZ) + CS_M * CS_M + CS_NY + CS_S + 18)
+#define CS_GRP_RAW (CS_S1 * CS_LDW1 + CS_M * CS_RB * CS_JYC + CS_M * CS_RB + CS_M * CS_M + CS_NY + CS_RB * CS_NRHS + CS_S1 + 16)
+// group stride padded to 8 (mod 16) doubles: the groups of one warp then
+// start on alternate halves of the shared-memory banks
+#define CS_GRP_DBL (((CS_GRP_RAW + 7) / 16) * 16 + 8)
 
 // A group of GL threads condenses one interval: GL = 8 or 16 (sub-warp:
 // several intervals per warp, so that the per-column work of the
@@ -494,18 +514,26 @@ __device__ __forceinline__ unsigned long long cs_abskey(double v) {
   return (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffull;
 }
 
+// right-hand-side column c of stage row (j, a): J, then V_eff, then f_a
+__device__ __forceinline__ double cs_rhs(const double* J, const double* fa, int j, int a, int c) {
+  if (c < CS_NY) return J[c];
+  if (c < CS_NY + CS_NPE) return J[CS_NY + CS_NZ + (c - CS_NY)];
+  return fa[j * CS_RB + a];
+}
+
 // `active` is false for a filler group of a partly used warp: it computes on a
 // valid interval but writes nothing.
 template <int GL>
 __device__ void cs_condense_group(const CsBatch& bt, int slot, bool active, double* Wm, double* red) {
   typedef CsGrp<GL> G;
-  constexpr int RB = CS_NY + CS_NZ;  // rows per stage block
+  constexpr int RB = CS_RB;
   const int tid = G::tid();
-  double* Jy = Wm + CS_S * CS_LDW;
+  double* Jy = Wm + CS_S1 * CS_LDW1;
   double* fa = Jy + CS_M * RB * CS_JYC;
   double* hA = fa + CS_M * RB;
   double* fb = hA + CS_M * CS_M;
-  double* inv = fb + CS_NY;
+  double* X0 = fb + CS_NY;
+  double* inv = X0 + RB * CS_NRHS;
   const int b = bt.inst_of[slot];
   const double h = bt.t[slot + 1] - bt.t[slot];
   const double* th = bt.th + (size_t)b * (CS_NTH > 0 ? CS_NTH : 1);
@@ -551,14 +579,56 @@ __device__ void cs_condense_group(const CsBatch& bt, int slot, bool active, doub
     fb[k] = yi[CS_NY + k] - yi[k] - h * s;
   }
   G::sync();
-  // ---- fill [W | J | V_eff | f_a]
-  for (int e = tid; e < CS_S * CS_NCOL; e += GL) {
-    const int row = e / CS_NCOL, col = e - row * CS_NCOL;
-    const int j = row / RB, a = row - j * RB;
+  // ---- stage 0: [-I h_z0; 0 g_z0] X0 = R0, one thread per right-hand side
+  for (int c = tid; c < CS_NRHS; c += GL) {
+    const double* J0 = Jy;  // stage 0 rows
+#if CS_NZ > 0
+    double gz[CS_NZ][CS_NZ], xz[CS_NZ];
+    for (int a = 0; a < CS_NZ; ++a) {
+      for (int q = 0; q < CS_NZ; ++q) gz[a][q] = J0[(CS_NY + a) * CS_JYC + CS_NY + q];
+      xz[a] = cs_rhs(J0 + (CS_NY + a) * CS_JYC, fa, 0, CS_NY + a, c);
+    }
+    // partial-pivot elimination on g_z0 (NZ x NZ)
+    for (int kk = 0; kk < CS_NZ; ++kk) {
+      int pr = kk;
+      for (int r = kk + 1; r < CS_NZ; ++r)
+        if (cs_abskey(gz[r][kk]) > cs_abskey(gz[pr][kk])) pr = r;
+      if (pr != kk) {
+        for (int q = 0; q < CS_NZ; ++q) { const double t = gz[kk][q]; gz[kk][q] = gz[pr][q]; gz[pr][q] = t; }
+        const double t = xz[kk]; xz[kk] = xz[pr]; xz[pr] = t;
+      }
+      const double ip = 1.0 / gz[kk][kk];
+      for (int r = kk + 1; r < CS_NZ; ++r) {
+        const double l = gz[r][kk] * ip;
+        for (int q = kk + 1; q < CS_NZ; ++q) gz[r][q] = fma(-l, gz[kk][q], gz[r][q]);
+        xz[r] = fma(-l, xz[kk], xz[r]);
+      }
+    }
+    for (int r = CS_NZ - 1; r >= 0; --r) {
+      double v = xz[r];
+      for (int q = r + 1; q < CS_NZ; ++q) v = fma(-gz[r][q], xz[q], v);
+      xz[r] = v / gz[r][r];
+    }
+    for (int a = 0; a < CS_NZ; ++a) X0[(CS_NY + a) * CS_NRHS + c] = xz[a];
+#endif
+    // -x_y + h_z0 x_z = r_y  ->  x_y = h_z0 x_z - r_y
+    for (int a = 0; a < CS_NY; ++a) {
+      double v = -cs_rhs(J0 + a * CS_JYC, fa, 0, a, c);
+#if CS_NZ > 0
+      for (int q = 0; q < CS_NZ; ++q) v = fma(J0[a * CS_JYC + CS_NY + q], xz[q], v);
+#endif
+      X0[a * CS_NRHS + c] = v;
+    }
+  }
+  G::sync();
+  // ---- fill the reduced system [W11 | R1 - W10 X0] (stages 1..M-1)
+  for (int e = tid; e < CS_S1 * CS_NCOL1; e += GL) {
+    const int row = e / CS_NCOL1, col = e - row * CS_NCOL1;
+    const int j = 1 + row / RB, a = row - (j - 1) * RB;
     const double* J = Jy + (size_t)(j * RB + a) * CS_JYC;
     double v;
-    if (col < CS_S) {
-      const int k = col / RB, q = col - k * RB;
+    if (col < CS_S1) {
+      const int k = 1 + col / RB, q = col - (k - 1) * RB;
       if (q < CS_NY) {
         v = hA[j * CS_M + k] * J[q];
         if (k == j && q == a) v -= 1.0;
@@ -566,24 +636,24 @@ __device__ void cs_condense_group(const CsBatch& bt, int slot, bool active, doub
         v = (k == j) ? J[q] : 0.0;
       }
     } else {
-      const int c = col - CS_S;
-      if (c < CS_NY) v = J[c];
-      else if (c < CS_NY + CS_NPE) v = J[CS_NY + CS_NZ + (c - CS_NY)];
-      else v = fa[row];
+      const int c = col - CS_S1;
+      double w = 0.0;
+      for (int q = 0; q < CS_NY; ++q) w = fma(J[q], X0[q * CS_NRHS + c], w);
+      v = fma(-hA[j * CS_M], w, cs_rhs(J, fa, j, a, c));
     }
-    Wm[row * CS_LDW + col] = v;
+    Wm[row * CS_LDW1 + col] = v;
   }
   G::sync();
   // ---- LU with partial pivoting: largest |entry| in the column, the first
   //      such row on ties (as matrix_factorization_cuda.py:133-146)
   int singular = 0;
 #pragma unroll 1
-  for (int k = 0; k < CS_S; ++k) {
+  for (int k = 0; k < CS_S1; ++k) {
     unsigned long long best = 0ull;
-    int brow = CS_S;  // larger than any row: loses every tie
-    for (int r = k + tid; r < CS_S; r += GL) {
-      const unsigned long long v = cs_abskey(Wm[r * CS_LDW + k]);
-      if (v > best || brow == CS_S) { best = v; brow = r; }
+    int brow = CS_S1;  // larger than any row: loses every tie
+    for (int r = k + tid; r < CS_S1; r += GL) {
+      const unsigned long long v = cs_abskey(Wm[r * CS_LDW1 + k]);
+      if (v > best || brow == CS_S1) { best = v; brow = r; }
     }
     constexpr int W = CsGrp<GL>::CTA ? 32 : GL;
     for (int o = W >> 1; o > 0; o >>= 1) {
@@ -608,55 +678,55 @@ __device__ void cs_condense_group(const CsBatch& bt, int slot, bool active, doub
       __syncthreads();
     }
     // swap rows k and brow (a self-swap when the pivot is in place)
-    for (int c = tid; c < CS_NCOL; c += GL) {
-      const double tmp = Wm[k * CS_LDW + c];
-      Wm[k * CS_LDW + c] = Wm[brow * CS_LDW + c];
-      Wm[brow * CS_LDW + c] = tmp;
+    for (int c = tid; c < CS_NCOL1; c += GL) {
+      const double tmp = Wm[k * CS_LDW1 + c];
+      Wm[k * CS_LDW1 + c] = Wm[brow * CS_LDW1 + c];
+      Wm[brow * CS_LDW1 + c] = tmp;
     }
     G::sync();
-    const double pv = Wm[k * CS_LDW + k];
+    const double pv = Wm[k * CS_LDW1 + k];
     // |pv| < 10 eps: the reference leaves this column uneliminated
     const bool tiny = cs_abskey(pv) < 0x3ce4000000000000ull;  // bits of 10 * 2^-52 = 2.22e-15
     singular |= tiny;
     const double ip = 1.0 / pv;
     if (tid == 0) inv[k] = ip;
     const double mul = tiny ? 0.0 : ip;
-    for (int r = k + 1 + tid; r < CS_S; r += GL) Wm[r * CS_LDW + k] *= mul;
+    for (int r = k + 1 + tid; r < CS_S1; r += GL) Wm[r * CS_LDW1 + k] *= mul;
     G::sync();
-    const int nc = CS_NCOL - k - 1;
-    const int ne = (CS_S - k - 1) * nc;
+    const int nc = CS_NCOL1 - k - 1;
+    const int ne = (CS_S1 - k - 1) * nc;
     for (int e = tid; e < ne; e += GL) {
       const int rr = e / nc;
       const int r = k + 1 + rr, c = k + 1 + (e - rr * nc);
-      Wm[r * CS_LDW + c] = fma(-Wm[r * CS_LDW + k], Wm[k * CS_LDW + c], Wm[r * CS_LDW + c]);
+      Wm[r * CS_LDW1 + c] = fma(-Wm[r * CS_LDW1 + k], Wm[k * CS_LDW1 + c], Wm[r * CS_LDW1 + c]);
     }
     G::sync();
   }
   // ---- back substitution, threads over (row, right-hand side) pairs
 #pragma unroll 1
-  for (int r = CS_S - 1; r >= 0; --r) {
-    for (int c = tid; c < CS_NRHS; c += GL) Wm[r * CS_LDW + CS_S + c] *= inv[r];
+  for (int r = CS_S1 - 1; r >= 0; --r) {
+    for (int c = tid; c < CS_NRHS; c += GL) Wm[r * CS_LDW1 + CS_S1 + c] *= inv[r];
     G::sync();
     const int ne = r * CS_NRHS;
     for (int e = tid; e < ne; e += GL) {
       const int q = e / CS_NRHS, c = e - q * CS_NRHS;
-      Wm[q * CS_LDW + CS_S + c] = fma(-Wm[q * CS_LDW + r], Wm[r * CS_LDW + CS_S + c], Wm[q * CS_LDW + CS_S + c]);
+      Wm[q * CS_LDW1 + CS_S1 + c] = fma(-Wm[q * CS_LDW1 + r], Wm[r * CS_LDW1 + CS_S1 + c], Wm[q * CS_LDW1 + CS_S1 + c]);
     }
     G::sync();
   }
   if (!active) return;
-  // ---- X (column-major [NRHS][S]) and the condensed block row
+  // ---- X (column-major [NRHS][S]: stage-0 rows from X0, the others from Wm)
   double* X = bt.X + (size_t)slot * CS_NRHS * CS_S;
   for (int e = tid; e < CS_NRHS * CS_S; e += GL) {
     const int c = e / CS_S, r = e - c * CS_S;
-    X[e] = Wm[r * CS_LDW + CS_S + c];
+    X[e] = (r < RB) ? X0[r * CS_NRHS + c] : Wm[(r - RB) * CS_LDW1 + CS_S1 + c];
   }
+  // ---- condensed block row: D X = h sum_j b_j X[(j, a)]
   double* row = bt.rows0 + (size_t)slot * CS_ROWSZ;
   for (int e = tid; e < CS_NRHS * CS_NY; e += GL) {
     const int c = e / CS_NY, a = e - c * CS_NY;
-    const int col = CS_S + c;
-    double s = 0.0;
-    for (int j = 0; j < CS_M; ++j) s += CS_B[j] * Wm[(j * RB + a) * CS_LDW + col];
+    double s = CS_B[0] * X0[a * CS_NRHS + c];
+    for (int j = 1; j < CS_M; ++j) s += CS_B[j] * Wm[((j - 1) * RB + a) * CS_LDW1 + CS_S1 + c];
     const double dx = h * s;
     if (c < CS_NY) {
       row[c * CS_NY + a] = (a == c) ? dx - 1.0 : dx;            // A column c
@@ -671,7 +741,7 @@ __device__ void cs_condense_group(const CsBatch& bt, int slot, bool active, doub
 }
 
 // lanes per condensation group, from the size of the stage system
-#define CS_CGL ((CS_S > 48) ? 256 : ((CS_S > 32) ? 16 : 8))
+#define CS_CGL ((CS_S1 > 48) ? 256 : ((CS_S1 > 16) ? 16 : 8))
 
 __device__ __forceinline__ void cs_condense_entry(const CsBatch& bt) {
   extern __shared__ double smem[];
@@ -697,7 +767,7 @@ __device__ __forceinline__ void cs_condense_entry(const CsBatch& bt) {
       __syncwarp();
     }
   } else {
-    double* red = smem + CS_GRP_DBL;
+    double* red = smem + CS_GRP_RAW - 16;
     for (long long it = blockIdx.x; it < total; it += gridDim.x) {
       const int k = cs_find(bt.jac_pre, njac, it);
       const int b = bt.jac[k];

@@ -310,32 +310,43 @@ extern "C" int cs_module_load(const cs_module_desc* d, cs_module** out) {
   M->rowsz = (size_t)d->ny * (2 * d->ny + d->np_eff + 1);
   M->treesz = (size_t)d->ny * (3 * d->ny + d->np_eff + 1);
   // condensation: shared memory of one group (CS_GRP_DBL in cs_kernels.cuh) and
-  // lanes per group (CS_GL): 8 lanes for small stage systems (4 intervals per
-  // warp), a warp for medium, a CTA of 256 threads for large ones
-  const int ldw = (M->s + M->nrhs) | 1;
+  // lanes per group (CS_CGL): 8 lanes for small reduced systems (4 intervals
+  // per warp), 16 for medium, a CTA of 256 threads for large ones
   const int rb = d->ny + d->nz, jyc = d->ny + d->nz + d->np_eff;
-  const size_t grp = ((size_t)M->s * ldw + (size_t)d->m * rb * jyc + (size_t)d->m * rb + (size_t)d->m * d->m + d->ny +
-                      M->s + 18) * sizeof(double);
-  const int ncol = M->s + M->nrhs;
-  const int gl = (M->s > 48) ? 256 : ((M->s > 32) ? 16 : 8);
-  (void)ncol;
-  if (grp + (gl > 32 ? 16 * sizeof(double) : 0) > (size_t)smem_optin) {
+  const int s1 = (d->m - 1) * rb;
+  const int ldw1 = (s1 + M->nrhs) | 1;
+  const size_t raw = (size_t)s1 * ldw1 + (size_t)d->m * rb * jyc + (size_t)d->m * rb + (size_t)d->m * d->m + d->ny +
+                     (size_t)rb * M->nrhs + s1 + 16;
+  const size_t grp = (((raw + 7) / 16) * 16 + 8) * sizeof(double);
+  const int gl = (s1 > 48) ? 256 : ((s1 > 16) ? 16 : 8);
+  if (grp > (size_t)smem_optin) {
     delete M;
     return set_err(CS_ERR_INVALID, "cs_module_load: stage system of size " + std::to_string(M->s) +
                                        " does not fit in shared memory");
   }
   M->cgw = gl;
+  int smem_sm = 0;
+  CS_CUDA(cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev));
   if (gl <= 32) {
+    // warps per CTA that maximise resident groups per SM (shared memory bound)
     const int gpw = 32 / gl;
-    int wpc = (int)std::min<size_t>(4, (size_t)smem_optin / (grp * gpw));
-    if (wpc < 1) wpc = 1;
-    M->condense_per_cta = wpc * gpw;
-    M->condense_block = 32 * wpc;
-    M->condense_smem = grp * gpw * wpc;
+    int best_w = 1;
+    long long best_groups = 0;
+    for (int w = 1; w <= 8; ++w) {
+      const size_t cta = grp * gpw * w;
+      if (cta > (size_t)smem_optin) break;
+      long long ctas = (long long)(smem_sm / (cta + 1024));
+      ctas = std::min<long long>(ctas, 64 / w);  // 64 warps per SM
+      const long long groups = ctas * w * gpw;
+      if (groups > best_groups) { best_groups = groups; best_w = w; }
+    }
+    M->condense_per_cta = best_w * gpw;
+    M->condense_block = 32 * best_w;
+    M->condense_smem = grp * gpw * best_w;
   } else {
     M->condense_per_cta = 1;
     M->condense_block = gl;
-    M->condense_smem = grp + 16 * sizeof(double);
+    M->condense_smem = grp;
   }
   // BABD tree: a merge matrix per warp (4 warps per CTA); top: one system per warp
   const int qld = (2 * M->ny) | 1, qc = 3 * M->ny + M->npe + 1;
@@ -394,7 +405,9 @@ extern "C" int cs_module_load(const cs_module_desc* d, cs_module** out) {
     CS_CU(g_drv.funcSetAttribute(M->f_top, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, (int)M->top_smem));
   {
     // resident CTAs of the condensation kernel per SM, for its persistent grid
-    int per_sm = std::max<int>(1, (int)((size_t)smem_optin / std::max<size_t>(M->condense_smem, 1)));
+    int smem_sm2 = 0;
+    CS_CUDA(cudaDeviceGetAttribute(&smem_sm2, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev));
+    int per_sm = std::max<int>(1, (int)((size_t)smem_sm2 / (M->condense_smem + 1024)));
     per_sm = std::min(per_sm, 2048 / M->condense_block);
     M->condense_grid = M->sms * per_sm;
   }
