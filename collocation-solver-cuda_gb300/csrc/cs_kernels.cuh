@@ -339,7 +339,21 @@ extern "C" __global__ void k_decide(CsBatch bt, CsConsts c) {
     } else {
       s.ls_it += 1;
       s.alpha_ls *= 0.5;
-      if (s.ls_it >= c.max_ls) cs_iteration_start(s, bt.N[b], c, true);
+      if (s.ls_it >= c.max_ls) {
+        // No trial accepted: the iterate is unchanged, so every remaining
+        // Newton iteration recomputes the same residual, Jacobian, direction
+        // and rejected trials (the reference loops exactly so until
+        // max_iter, collocation_solver_parallel_2d_shared.py:109-174).  Take
+        // that outcome directly: same state, same counts, then the
+        // iteration-limit failure.
+        const int rem = c.max_iter - s.it;
+        if (rem > 0) {
+          s.residual_count += rem * (1 + c.max_ls);
+          s.jac_count += rem;
+          s.it = c.max_iter;
+        }
+        cs_iteration_start(s, bt.N[b], c, false);
+      }
     }
     if (s.status == ST_FRESH || s.status == ST_LS || s.need_jac) atomicAdd(&bt.counters[0], 1ull);
     if (s.need_jac) {

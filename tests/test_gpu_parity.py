@@ -169,3 +169,28 @@ def test_batch_equals_independent_solves(cs):
         assert s["N"] == ref.N and s["newton_steps"] == ref.jacobian_count and s["residual_evals"] == ref.residual_count
         assert np.abs(s["y"] - ref.y).max() < 1e-8
         assert np.abs(s["z"] - ref.z).max() < 1e-8
+
+
+def test_failing_instances_match_oracle(cs):
+    """Instances of the Van der Pol batch whose Newton iteration does not
+    converge within the iteration limit: same failure, same counts (including
+    the repeated rejected line searches) and same final iterate as the
+    oracle."""
+    from conftest import OracleProblem
+    pr = cs.workloads.vdp_family_problem()
+    insts = cs.workloads.vdp_batch(4096, seed=1)
+    pick = [insts[i] for i in (209, 420, 629, 1125)]
+    P = OracleProblem(pr)
+    P.maximum_newton_iterations = 30
+    for inst in pick:
+        cp = compiled(cs, "vdp_family", inst.m)
+        bt = cs.Batch(cp, 1)
+        t, y, z, p = inst.guess()
+        bt.set_guess([(t, y, z)], p.reshape(1, -1), inst.theta.reshape(1, -1))
+        bt.solve(cs.default_opts(pr, max_iter=30))
+        s = bt.solution()[0]
+        P.theta = inst.theta
+        ref = O.solve(P, inst.m, cs.tables.lobatto(inst.m), cs.tables.segment_tables(inst.m), T0=t, Y0=y, Z0=z, P0=p)
+        assert s["success"] == ref.success
+        assert (s["newton_steps"], s["residual_evals"], s["N"]) == (ref.jacobian_count, ref.residual_count, ref.N)
+        assert np.abs(s["y"] - ref.y).max() < 1e-8
