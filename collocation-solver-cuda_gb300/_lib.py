@@ -73,6 +73,8 @@ SIGNATURES = {
     "cs_profile_get": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Profile)]),
     "cs_pinned_alloc": (ctypes.c_void_p, [ctypes.c_size_t]),
     "cs_pinned_free": (None, [ctypes.c_void_p]),
+    "cs_babd_solve": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int] + [ctypes.c_void_p] * 10 +
+                      [ctypes.POINTER(ctypes.c_int), ctypes.c_void_p]),
 }
 
 _lib = None

@@ -49,13 +49,13 @@ def _stale(target, deps):
 
 def build_library(force=False, verbose=False):
     hdr = _kernels_header()
-    deps = [os.path.join(CSRC, "cs_runtime.cu"), os.path.join(CSRC, "cs_kernels.cuh"),
-            os.path.join(ROOT, "include", "cs_gb300.h"), hdr]
+    sources = [os.path.join(CSRC, "cs_runtime.cu"), os.path.join(CSRC, "cs_babd.cu")]
+    deps = sources + [os.path.join(CSRC, "cs_kernels.cuh"), os.path.join(ROOT, "include", "cs_gb300.h"), hdr]
     if not force and not _stale(LIB, deps):
         return LIB
     cmd = [NVCC, "-O3", "-std=c++17", "-lineinfo", *ARCH, "-shared", "-Xcompiler", "-fPIC",
            "-I", os.path.join(ROOT, "include"), "-I", BUILD, "-I", CSRC,
-           os.path.join(CSRC, "cs_runtime.cu"), "-o", LIB + ".tmp",
+           *sources, "-o", LIB + ".tmp",
            "-L", os.path.join(CUDA_HOME, "lib64"), "-L", os.path.join(CUDA_HOME, "lib64", "stubs"),
            "-lnvrtc"]
     if verbose:

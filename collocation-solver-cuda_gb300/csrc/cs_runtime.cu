@@ -214,6 +214,9 @@ __global__ void k_dfma_peak(double* out, int iters) {
 
 }  // namespace
 
+// error reporting for the other translation units of the library
+int cs_internal_set_error(int code, const char* msg) { return set_err(code, msg ? msg : ""); }
+
 // ============================================================== module ===
 struct cs_module {
   int ny, nz, np, npe, nth, m, s, nrhs, cgw;

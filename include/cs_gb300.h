@@ -167,6 +167,25 @@ int cs_stage_segment_residual(cs_batch* bt, double alpha, double tol, double* re
  * (CS:194-198, 2034-2311). */
 int cs_stage_remesh(cs_batch* bt, const double* res, int* N_new);
 
+/* Solve one BABD system (the linear system of a Newton step after
+ * condensation) given in DEVICE memory, reference layout (row-major):
+ *   A, C: n x ny x ny;  H: n x ny x np;  b: n x ny      (block rows i = 0..n-1:
+ *   A_i dy_i + C_i dy_{i+1} + H_i dp = b_i)
+ *   B0, Bn: (ny+np) x ny;  Vn: (ny+np) x np;  r: ny+np   (B0 dy_0 + Bn dy_n +
+ *   Vn dp = -r)
+ * Outputs dy ((n+1) x ny) and dp (np) in device memory; *singular (host, may
+ * be NULL) is set when the top system was singular (dy_0, dy_n, dp are then 0,
+ * as the reference's LinAlgError fallback).  1 <= ny <= 32, 0 <= np <= 32.
+ * Allocates its scratch (about 8 (2 ny (2ny+np+1) + ny (3ny+np+1)) bytes per
+ * interval) for the duration of the call; ordered on `stream` (a
+ * cudaStream_t or NULL) and returns after it has finished.
+ * Replaces: partition_factorization_parallel, construct_babd_mshoot,
+ * qr_decomposition, backward_substitution, recover_babd_solution and
+ * partition_backward_substitution_parallel (solve_babd_system.py:93-572). */
+int cs_babd_solve(int ny, int np, int n, const double* A, const double* C, const double* H, const double* b,
+                  const double* B0, const double* Bn, const double* Vn, const double* r, double* dy, double* dp,
+                  int* singular, void* stream);
+
 /* Current iterate to host: t, y (nodes), ydot, z~ (slots), z at nodes, p. */
 int cs_get_state(cs_batch* bt, double* t, double* y, double* ydot, double* zt, double* z_nodes, double* p);
 

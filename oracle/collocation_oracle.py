@@ -203,8 +203,8 @@ def partition_factorization(ny, npar, M, N, A, C, H, b):
             d[j], btl = db[:ny], db[ny:]
             R[j] = Rq[:ny]
         At[i], Ct[i], Ht[i], bt[i] = gt, ct, htl, btl
-    return (index, R.reshape(-1, ny), E.reshape(-1, ny), Jr.reshape(-1, npar), G.reshape(-1, ny), d,
-            At.reshape(-1, ny), Ct.reshape(-1, ny), Ht.reshape(-1, npar), bt)
+    return (index, R.reshape(-1, ny), E.reshape(-1, ny), Jr.reshape((N - 1) * ny, npar), G.reshape(-1, ny), d,
+            At.reshape(-1, ny), Ct.reshape(-1, ny), Ht.reshape(M * ny, npar), bt)
 
 
 def _solve_or_zero(Rm, rhs):
