@@ -75,6 +75,8 @@ SIGNATURES = {
     "cs_pinned_free": (None, [ctypes.c_void_p]),
     "cs_babd_solve": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int] + [ctypes.c_void_p] * 10 +
                       [ctypes.POINTER(ctypes.c_int), ctypes.c_void_p]),
+    "cs_babd_solve_noalloc": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int] + [ctypes.c_void_p] * 10 +
+                              [ctypes.POINTER(ctypes.c_int), ctypes.c_void_p]),
 }
 
 _lib = None

@@ -302,7 +302,70 @@ int babd_run(const BabdDims& d, const double* A, const double* C, const double* 
   return CS_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Scratch for cs_babd_solve_noalloc: one array in the device image of this
+// library, so that callers that cannot allocate device memory can still solve
+// a BABD system.  Every GPU that loads the library holds it until the process
+// exits.  Element 0 carries the singular flag; the block rows and tree records
+// start at element 32 (256-byte aligned).
+constexpr size_t kNoallocDoubles = (size_t)4 << 20;  // 32 MiB
+__device__ __align__(256) double cs_babd_scratch[kNoallocDoubles];
+
+std::mutex g_noalloc_mu;
+void* g_noalloc_addr[128] = {nullptr};
+
+// device address of the scratch array on the current device, looked up once
+// per device (host code cannot use the symbol itself as an address)
+int noalloc_scratch(double** out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cs_internal_set_error(CS_ERR_CUDA, cudaGetErrorString(e));
+  if (dev < 0 || dev >= 128) return cs_internal_set_error(CS_ERR_CUDA, "cs_babd_solve_noalloc: device index out of range");
+  std::lock_guard<std::mutex> lk(g_noalloc_mu);
+  if (!g_noalloc_addr[dev]) {
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, cs_babd_scratch);
+    if (e != cudaSuccess || !p)
+      return cs_internal_set_error(CS_ERR_CUDA, (std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e)).c_str());
+    g_noalloc_addr[dev] = p;
+  }
+  *out = (double*)g_noalloc_addr[dev];
+  return CS_OK;
+}
+
 }  // namespace
+
+extern "C" int cs_babd_solve_noalloc(int ny, int np, int n, const double* A, const double* C, const double* H,
+                                     const double* b, const double* B0, const double* Bn, const double* Vn,
+                                     const double* r, double* dy, double* dp, int* singular, void* stream) {
+  int rc = check_sizes(ny, np, n);
+  if (rc != CS_OK) return rc;
+  if (!A || !C || !b || !B0 || !Bn || !r || !dy || (np > 0 && (!H || !Vn || !dp)))
+    return cs_internal_set_error(CS_ERR_INVALID, "cs_babd_solve_noalloc: null pointer");
+  const BabdDims d = dims_of(ny, np, n);
+  const size_t need = 32 + scratch_doubles(d);
+  if (need > kNoallocDoubles)
+    return cs_internal_set_error(
+        CS_ERR_INVALID, ("cs_babd_solve_noalloc: the system needs " + std::to_string(need * sizeof(double)) +
+                         " bytes of scratch, more than the fixed " + std::to_string(kNoallocDoubles * sizeof(double)) +
+                         " bytes; use cs_babd_solve").c_str());
+  double* base = nullptr;
+  rc = noalloc_scratch(&base);
+  if (rc != CS_OK) return rc;
+  cudaStream_t st = (cudaStream_t)stream;
+  // every element read below is written earlier in the same call (packing,
+  // tree levels, top system), so nothing needs clearing between calls
+  int* dsing = (int*)base;
+  rc = babd_run(d, A, C, H, b, B0, Bn, Vn, r, dy, dp, base + 32, dsing, st);
+  int hs = 0;
+  if (rc == CS_OK) {
+    cudaError_t e = cudaMemcpyAsync(&hs, dsing, sizeof(int), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) rc = cs_internal_set_error(CS_ERR_CUDA, cudaGetErrorString(e));
+  }
+  if (singular) *singular = hs;
+  return rc;
+}
 
 extern "C" int cs_babd_solve(int ny, int np, int n, const double* A, const double* C, const double* H,
                              const double* b, const double* B0, const double* Bn, const double* Vn, const double* r,

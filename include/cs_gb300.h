@@ -186,6 +186,24 @@ int cs_babd_solve(int ny, int np, int n, const double* A, const double* C, const
                   const double* B0, const double* Bn, const double* Vn, const double* r, double* dy, double* dp,
                   int* singular, void* stream);
 
+/* cs_babd_solve without any device allocation, for callers that cannot call
+ * cudaMalloc: code that runs inside a memory pool or allocator it must not
+ * re-enter, inside a CUDA graph being built, or under a framework that owns
+ * all device memory.  It has no counterpart in the reference (whose stage
+ * functions allocate device arrays on every call).
+ * Same arguments and results as cs_babd_solve.  Its scratch is a fixed 32 MiB
+ * array compiled into this library, held by every GPU that loads the library
+ * until the process exits; systems needing more (2 n ny (2ny+np+1) +
+ * (n+1) ny (3ny+np+1) doubles, plus 256 bytes) are rejected with
+ * CS_ERR_INVALID.  The first call on each device looks up the array's device
+ * address (cudaGetSymbolAddress); make that first call before any stream
+ * capture.  All calls share the one array: calls that overlap on the GPU
+ * (other streams, other host threads) race and must be serialised by the
+ * caller. */
+int cs_babd_solve_noalloc(int ny, int np, int n, const double* A, const double* C, const double* H,
+                          const double* b, const double* B0, const double* Bn, const double* Vn, const double* r,
+                          double* dy, double* dp, int* singular, void* stream);
+
 /* Current iterate to host: t, y (nodes), ydot, z~ (slots), z at nodes, p. */
 int cs_get_state(cs_batch* bt, double* t, double* y, double* ydot, double* zt, double* z_nodes, double* p);
 
