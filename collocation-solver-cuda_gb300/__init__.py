@@ -12,6 +12,6 @@ Import with importlib (the directory name contains hyphens):
 The GPU path needs libcs_gb300.so (built by build.py) and a CUDA device; there
 is no CPU fallback.
 """
-from . import tables, ocp, codegen, io, _lib, module, solver, build, workloads  # noqa: F401
+from . import tables, ocp, codegen, io, _lib, module, solver, build, workloads, warmstart  # noqa: F401
 from .ocp import Problem  # noqa: F401
 from .module import Batch, CompiledProblem, default_opts  # noqa: F401

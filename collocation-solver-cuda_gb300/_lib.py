@@ -75,6 +75,19 @@ SIGNATURES = {
     "cs_pinned_free": (None, [ctypes.c_void_p]),
     "cs_babd_solve": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int] + [ctypes.c_void_p] * 10 +
                       [ctypes.POINTER(ctypes.c_int), ctypes.c_void_p]),
+    "cs_mlp_create": (ctypes.c_int, [ctypes.c_int] * 4 + [ctypes.c_ulonglong, ctypes.POINTER(ctypes.c_void_p)]),
+    "cs_mlp_free": (None, [ctypes.c_void_p]),
+    "cs_mlp_num_params": (ctypes.c_longlong, [ctypes.c_void_p]),
+    "cs_mlp_set_normalization": (ctypes.c_int, [ctypes.c_void_p] + [ctypes.POINTER(ctypes.c_float)] * 4),
+    "cs_mlp_get_params": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_float)]),
+    "cs_mlp_set_params": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_float)]),
+    "cs_mlp_gradient": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float),
+                                       ctypes.c_int, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_float)]),
+    "cs_mlp_train": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float),
+                                    ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_float, ctypes.c_ulonglong,
+                                    ctypes.POINTER(ctypes.c_double)]),
+    "cs_mlp_predict": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_float), ctypes.c_int,
+                                      ctypes.POINTER(ctypes.c_float)]),
     "cs_babd_solve_noalloc": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int] + [ctypes.c_void_p] * 10 +
                               [ctypes.POINTER(ctypes.c_int), ctypes.c_void_p]),
 }
@@ -119,6 +132,13 @@ def dptr(a):
         return None
     assert a.dtype == np.float64 and a.flags["C_CONTIGUOUS"], "arrays must be C-contiguous float64"
     return a.ctypes.data_as(_dp)
+
+
+def fptr(a):
+    if a is None:
+        return None
+    assert a.dtype == np.float32 and a.flags["C_CONTIGUOUS"], "arrays must be C-contiguous float32"
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
 
 
 def iptr(a):

@@ -1,0 +1,214 @@
+"""Learned warm start: an MLP maps the parameters of an OCP instance to its
+state/costate/control trajectory at fixed normalised-time nodes; the
+prediction, interpolated onto the instance's mesh, is the Newton initial
+guess.  The network is trained and run by the library's own kernels
+(csrc/cs_mlp.cu) on solutions the batched solver produces.
+
+A warm-started solve is accepted only when it meets the tolerance; any
+instance whose warm-started Newton iteration fails is solved again from the
+plain initial guess (fallback).
+"""
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from .module import Batch, CompiledProblem, default_opts
+
+N_NODES = 64
+
+
+class Mlp:
+    """The network (ctypes over cs_mlp_*)."""
+
+    def __init__(self, n_in, n_out, width=256, depth=4, seed=0):
+        self._lib = _lib.load()
+        h = ctypes.c_void_p()
+        _lib.check(self._lib.cs_mlp_create(n_in, width, depth, n_out, seed, ctypes.byref(h)), "cs_mlp_create")
+        self.handle = h
+        self.n_in, self.n_out, self.width, self.depth = n_in, n_out, width, depth
+        self.sizes = [(n_in if l == 0 else width, n_out if l == depth - 1 else width) for l in range(depth)]
+        self.norm = (np.zeros(n_in, np.float32), np.ones(n_in, np.float32), np.zeros(n_out, np.float32),
+                     np.ones(n_out, np.float32))
+
+    def __del__(self):
+        import sys
+        if sys.is_finalizing():
+            return
+        try:
+            if getattr(self, "handle", None):
+                self._lib.cs_mlp_free(self.handle)
+                self.handle = None
+        except Exception:  # noqa: BLE001
+            pass
+
+    @property
+    def n_params(self):
+        return int(self._lib.cs_mlp_num_params(self.handle))
+
+    def set_normalization(self, xm, xs, ym, ys):
+        arrs = [np.ascontiguousarray(a, dtype=np.float32) for a in (xm, xs, ym, ys)]
+        _lib.check(self._lib.cs_mlp_set_normalization(self.handle, *[_lib.fptr(a) for a in arrs]),
+                   "cs_mlp_set_normalization")
+        self.norm = tuple(arrs)
+
+    def fit_normalization(self, X, Y):
+        xs = X.std(axis=0)
+        ys = Y.std(axis=0)
+        self.set_normalization(X.mean(axis=0), np.where(xs > 1e-8, xs, 1.0), Y.mean(axis=0),
+                               np.where(ys > 1e-8, ys, 1.0))
+
+    def params(self):
+        out = np.zeros(self.n_params, np.float32)
+        _lib.check(self._lib.cs_mlp_get_params(self.handle, _lib.fptr(out)), "cs_mlp_get_params")
+        return out
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        assert p.size == self.n_params
+        _lib.check(self._lib.cs_mlp_set_params(self.handle, _lib.fptr(p)), "cs_mlp_set_params")
+
+    def gradient(self, X, Y):
+        X = np.ascontiguousarray(X, dtype=np.float32)
+        Y = np.ascontiguousarray(Y, dtype=np.float32)
+        loss = ctypes.c_double()
+        g = np.zeros(self.n_params, np.float32)
+        _lib.check(self._lib.cs_mlp_gradient(self.handle, _lib.fptr(X), _lib.fptr(Y), X.shape[0], ctypes.byref(loss),
+                                             _lib.fptr(g)), "cs_mlp_gradient")
+        return loss.value, g
+
+    def train(self, X, Y, epochs=200, batch=512, lr=1e-3, seed=0):
+        X = np.ascontiguousarray(X, dtype=np.float32)
+        Y = np.ascontiguousarray(Y, dtype=np.float32)
+        loss = ctypes.c_double()
+        _lib.check(self._lib.cs_mlp_train(self.handle, _lib.fptr(X), _lib.fptr(Y), X.shape[0], epochs, batch,
+                                          ctypes.c_float(lr), seed, ctypes.byref(loss)), "cs_mlp_train")
+        return loss.value
+
+    def predict(self, X):
+        X = np.ascontiguousarray(X, dtype=np.float32)
+        Y = np.zeros((X.shape[0], self.n_out), np.float32)
+        _lib.check(self._lib.cs_mlp_predict(self.handle, _lib.fptr(X), X.shape[0], _lib.fptr(Y)), "cs_mlp_predict")
+        return Y
+
+
+# ------------------------------------------------------- trajectories ---
+def trajectory_vector(t, y, z, p, T, n_nodes=N_NODES):
+    """y and z resampled at n_nodes equispaced normalised times in [0, 1]
+    (linear interpolation of the nodal solution), then p."""
+    s = np.linspace(0.0, 1.0, n_nodes)
+    tau = t / T
+    ys = np.stack([np.interp(s, tau, y[:, k]) for k in range(y.shape[1])], axis=1)
+    zs = np.stack([np.interp(s, tau, z[:, k]) for k in range(z.shape[1])], axis=1) if z.shape[1] else np.zeros((n_nodes, 0))
+    return np.concatenate([ys.ravel(), zs.ravel(), np.asarray(p, float).ravel()])
+
+
+def guess_from_vector(v, t, T, ny, nz, npar, n_nodes=N_NODES):
+    """Initial guess on the mesh t from a trajectory vector."""
+    s = np.linspace(0.0, 1.0, n_nodes)
+    ys = v[:n_nodes * ny].reshape(n_nodes, ny)
+    zs = v[n_nodes * ny:n_nodes * (ny + nz)].reshape(n_nodes, nz)
+    p = v[n_nodes * (ny + nz):n_nodes * (ny + nz) + npar]
+    tau = t / T
+    y = np.stack([np.interp(tau, s, ys[:, k]) for k in range(ny)], axis=1)
+    z = np.stack([np.interp(tau, s, zs[:, k]) for k in range(nz)], axis=1) if nz else np.zeros((len(t), 0))
+    return y, z, p
+
+
+class Family:
+    """An instance family: the OCP problem, instance parameters -> features,
+    constants theta, final time, mesh and plain guess."""
+
+    def __init__(self, problem, features, theta, final_time, plain_guess, name="family"):
+        self.problem = problem
+        self.features = features
+        self.theta = theta
+        self.final_time = final_time
+        self.plain_guess = plain_guess
+        self.name = name
+        self.ny, self.nz, self.np = problem.size_y, problem.size_z, problem.size_p
+        self.n_out = N_NODES * (self.ny + self.nz) + self.np
+
+
+def vdp_family():
+    from .workloads import vdp_family_problem
+    pr = vdp_family_problem()
+    return Family(pr, features=lambda i: np.array([i.x0[0], i.x0[1], i.T, np.log(i.r)]),
+                  theta=lambda i: i.theta, final_time=lambda i: i.T, plain_guess=lambda i: i.guess(), name="vdp")
+
+
+class BatchSolver:
+    """Solves lists of instances of a family in one batch per m; compiled
+    problems are kept per m."""
+
+    def __init__(self, family, opts=None):
+        self.family = family
+        self.compiled = {}
+        self.opts = opts if opts is not None else default_opts(family.problem, max_nodes=20000)
+
+    def cp(self, m):
+        if m not in self.compiled:
+            self.compiled[m] = CompiledProblem(self.family.problem, m)
+        return self.compiled[m]
+
+    def solve(self, instances, guesses=None):
+        """Solve every instance (guesses: list of (y, z, p) on the plain mesh or
+        None for the plain guess).  Returns the solution dicts in input order."""
+        fam = self.family
+        out = [None] * len(instances)
+        for m in sorted(set(i.m for i in instances)):
+            idx = [k for k, i in enumerate(instances) if i.m == m]
+            meshes, ps, ths = [], [], []
+            for k in idx:
+                inst = instances[k]
+                t, y0, z0, p0 = fam.plain_guess(inst)
+                if guesses is not None and guesses[k] is not None:
+                    y0, z0, p0 = guesses[k]
+                meshes.append((t, y0, z0))
+                ps.append(p0)
+                ths.append(fam.theta(inst))
+            bt = Batch(self.cp(m), len(idx))
+            bt.set_guess(meshes, np.array(ps).reshape(len(idx), -1), np.array(ths).reshape(len(idx), -1))
+            bt.solve(self.opts)
+            for k, s in zip(idx, bt.solution()):
+                out[k] = s
+        return out
+
+
+def training_set(family, solver, instances):
+    """(X, Y) from the instances the batched solver solves from the plain guess."""
+    sols = solver.solve(instances)
+    X, Y = [], []
+    for inst, s in zip(instances, sols):
+        if not s["success"]:
+            continue
+        X.append(family.features(inst))
+        Y.append(trajectory_vector(s["t"], s["y"], s["z"], s["p"], family.final_time(inst)))
+    return np.array(X, np.float32), np.array(Y, np.float32), sols
+
+
+def warm_guesses(family, mlp, instances):
+    X = np.array([family.features(i) for i in instances], np.float32)
+    pred = mlp.predict(X).astype(np.float64)
+    out = []
+    for inst, v in zip(instances, pred):
+        t = family.plain_guess(inst)[0]
+        out.append(guess_from_vector(v, t, family.final_time(inst), family.ny, family.nz, family.np))
+    return out
+
+
+def solve_warm(family, solver, mlp, instances):
+    """Warm-started batch solve with fallback: instances whose warm-started
+    solve fails are solved again from the plain guess.  Returns (solutions,
+    fallback indices, warm-start solutions)."""
+    guesses = warm_guesses(family, mlp, instances)
+    warm = solver.solve(instances, guesses)
+    fb = [k for k, s in enumerate(warm) if not s["success"]]
+    final = list(warm)
+    if fb:
+        plain = solver.solve([instances[k] for k in fb])
+        for k, s in zip(fb, plain):
+            s = dict(s)
+            s["fallback"] = True
+            final[k] = s
+    return final, fb, warm

@@ -232,6 +232,28 @@ int cs_profile_get(cs_batch* bt, cs_profile* out);
 void* cs_pinned_alloc(size_t bytes);
 void cs_pinned_free(void* p);
 
+/* ---- learned warm start: a multilayer perceptron trained on solutions ----
+ * depth linear layers n_in -> width -> ... -> width -> n_out, GELU between
+ * them; FP32 master weights, BF16 operands with FP32 accumulation on the
+ * tensor cores, MSE loss on normalised outputs, Adam.  Host arrays are
+ * row-major float32 (one row per sample).  No counterpart in the reference
+ * (its Newton starts from the OCP file's constant estimates). */
+typedef struct cs_mlp cs_mlp;
+int cs_mlp_create(int n_in, int width, int depth, int n_out, unsigned long long seed, cs_mlp** out);
+void cs_mlp_free(cs_mlp* mlp);
+long long cs_mlp_num_params(const cs_mlp* mlp);
+/* inputs and outputs are normalised as (v - mean) / std inside the network */
+int cs_mlp_set_normalization(cs_mlp* mlp, const float* in_mean, const float* in_std, const float* out_mean,
+                             const float* out_std);
+/* all weights and biases, layer by layer (W[out][in] then b[out]) */
+int cs_mlp_get_params(cs_mlp* mlp, float* host);
+int cs_mlp_set_params(cs_mlp* mlp, const float* host);
+/* mean-squared error (normalised outputs) of n samples and its gradient */
+int cs_mlp_gradient(cs_mlp* mlp, const float* X, const float* Y, int n, double* loss, float* grad);
+int cs_mlp_train(cs_mlp* mlp, const float* X, const float* Y, int n, int epochs, int batch, float lr,
+                 unsigned long long seed, double* final_loss);
+int cs_mlp_predict(cs_mlp* mlp, const float* X, int n, float* Y);
+
 /* Message of this thread's last error ("" if none). */
 int cs_last_error(char* buf, size_t len);
 
