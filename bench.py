@@ -1,17 +1,30 @@
-"""Benchmark: batched collocation solves per second to a 1e-6 residual on one
-GB300 (FP64), with the CPU oracle timed beside it.
+"""Benchmark: solves per second to a 1e-6 residual on one GB300 (FP64):
+NN-warm-started batched solves against the plain GPU solver on the same
+batch, with the CPU oracle timed beside them.
 
-Workload (one "step"): the seeded Van der Pol batch — 4096 instances with
-x0 ~ U[-2,2]^2, T ~ U[2,8], r ~ logU[0.1,10], N ~ U{32..2048} intervals,
-m ~ U{3,4,5}, zero initial guess, tol 1e-6 — solved to completion (Newton,
-line search, segment residual, remesh) in one batch per m.
+Default workload (`--workload warm`, the learned-warm-start configuration):
+the Van der Pol family (x0 ~ U[-2,2]^2, T ~ U[2,8], control weight
+r ~ logU[0.1,10]).  Set-up (untimed, reported): 65,536 seeded instances
+(seed 1000, N ~ U{32..256} intervals) solved by the batched solver from the
+plain guess, an MLP (4 layers, width 256, GELU, BF16 operands, FP32
+accumulation) trained on them by the library's kernels.  One "step": the
+8192 held-out instances (seed 7, N ~ U{32..2048} intervals, m ~ U{3,4,5})
+solved to completion in one batch per m: features -> MLP -> trajectories
+interpolated onto each mesh (on the device) -> Newton, line search, segment
+residual, remesh; instances whose warm-started solve fails are solved again
+from the plain guess.
 
-  value  solves/s with the initial guesses resident in HBM (cs_batch_reset)
-  e2e    solves/s through the C ABI from pinned host buffers: initial guesses
-         H2D, solve, solutions D2H, every step inside the timed region
+  value  solves/s (instances reaching the tolerance), inputs resident in HBM
+  e2e    the same through the C ABI from pinned host buffers: features and
+         plain guesses H2D, solutions D2H, inside the timed region
+  plain_batched      the same batch from the plain (zero) guess
+  plain_single_gpu   the plain solver one instance at a time (a random sample)
+
+`--workload plain`: the batched plain solve of 4096 instances (seed 1,
+N ~ U{32..2048}) alone.
 
 Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-Under torchrun each rank solves its own batch (seed 1 + rank; weak scaling)
+Under torchrun each rank solves its own batch (seeds + rank; weak scaling)
 and rank 0 prints one JSON line.
 """
 import argparse
@@ -220,6 +233,12 @@ class Workload:
         return succ, newton, N
 
 
+# DRAM bytes per condensed interval measured by ncu on the m = 3 case
+# (dram__bytes_read.sum + dram__bytes_write.sum = 130.7 MB over 179,417
+# intervals, profiles/k_condense_vdp_batch512_m3.md)
+TRAFFIC_PER_INTERVAL_NCU = 728.5
+
+
 def flops_per_interval(m, ny=4, nz=1, npe=0):
     """Algorithmic FP64 flops of condensing one interval: (2/3) s^3 + 2 s^2 r,
     s = m (ny + nz), r = ny + np_eff + 1 (LU of the stage system with r
@@ -237,13 +256,287 @@ def bytes_per_interval(m, ny=4, nz=1, npe=0):
     return 8 * (2 + 2 * ny + m * (ny + nz) + r * s + ny * (2 * ny + npe + 1))
 
 
+def _dist_setup(world, local_rank):
+    if world <= 1:
+        return None
+    import torch.distributed as tdist
+    tdist.init_process_group("gloo")
+    return tdist
+
+
+def _barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def _max_over_ranks(dist, x):
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def _sum_over_ranks(dist, x):
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+def _roofline(groups, fp64_peak):
+    """Condensation of every interval of each group, timed alone with CUDA
+    events on the batch's stream (one launch per group)."""
+    flops = cbytes = cms = 0.0
+    n_all = 0
+    for m, bt in groups:
+        bt.reset()
+        ms = bt.time_condense(reps=5)
+        n_int = bt.sizes()[1] - bt.B
+        flops += n_int * flops_per_interval(m)
+        cbytes += n_int * bytes_per_interval(m)
+        cms += ms
+        n_all += n_int
+    achieved = flops / (cms * 1e-3) / 1e12
+    return {"bound": "fp64", "kernel": "k_condense", "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
+            "frac": achieved / fp64_peak if fp64_peak else None,
+            "traffic": TRAFFIC_PER_INTERVAL_NCU * n_all / len(groups),
+            "traffic_note": "DRAM bytes per launch: the ncu capture of the m=3 case "
+                            "(profiles/k_condense_vdp_batch512_m3.md, 728.5 B per interval) scaled by the intervals "
+                            "of one launch; algorithmic bytes per interval are in flops_note",
+            "peak_source": "DFMA microbenchmark (cs_measure_fp64_peak) in this run; FP64 is absent from "
+                           "MEASURED_PEAKS.json",
+            "flops_per_launch": flops / len(groups), "ms_per_launch": cms / len(groups),
+            "flops_note": "contract flops per interval (2/3)s^3 + 2 s^2 r, s = m(ny+nz), r = ny+np_eff+1; "
+                          "algorithmic bytes 8(2 + 2ny + m(ny+nz) + r s + ny(2ny+np_eff+1)) per interval",
+            "hbm_gbs": cbytes / (cms * 1e-3) / 1e9}
+
+
+def _cpu_baseline(instances, cores, seed=3):
+    rng = np.random.default_rng(seed)
+    idx = rng.permutation(len(instances))
+    sample = [instances[i] for i in idx]
+    rate, n, dt = cpu_oracle_rate(sample, cores, target_s=20.0)
+    return {"value": rate, "unit": "solves/s", "cores": cores, "kind": "port",
+            "sample": "%d random instances of the batch solved by the oracle from the plain guess in %.1f s, one "
+                      "process per core" % (n, dt)}
+
+
+def run_reference(args, instances, cfg, cores):
+    """The reference's CPU implementation of the path (its Python restated as
+    the oracle), all host cores, bounded sample per step."""
+    procs = cores
+    sample = instances[:]
+    rng = np.random.default_rng(7)
+    rng.shuffle(sample)
+    per_step = 2 * procs
+    ctx = mp.get_context("spawn")
+    a = [(tuple(i.x0), i.T, i.r, i.intervals, i.m) for i in sample]
+    with ctx.Pool(procs) as pool:
+        pool.map(_oracle_worker, a[:procs])
+        pos = 0
+        for _ in range(args.warmup):
+            pool.map(_oracle_worker, a[pos:pos + per_step])
+            pos += per_step
+        t0 = time.time()
+        for _ in range(args.steps):
+            pool.map(_oracle_worker, a[pos:pos + per_step])
+            pos += per_step
+        dt = time.time() - t0
+    v = args.steps * per_step / dt
+    cfg = dict(cfg, l2="n/a (CPU)")
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "solves/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * dt / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": cfg,
+            "cpu_baseline": {"value": v, "unit": "solves/s", "cores": procs, "kind": "port",
+                             "sample": "%d random instances of the batch per step from the plain guess (the "
+                                       "reference has no warm start), one per process" % per_step},
+            "e2e": {"value": v, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def run_warm(args, cs, rank, world, local_rank, cpu, cfg):
+    dist = _dist_setup(world, local_rank)
+    cs.build.build_library()
+    cs._lib.load()
+    ws = cs.warmstart
+    fp64_peak = cs.module.measure_fp64_peak()
+    fam = ws.vdp_family()
+    solver = ws.BatchSolver(fam)
+    # ---- set-up: training data from the batched solver, then training
+    t0 = time.perf_counter()
+    train = cs.workloads.vdp_batch(args.train, seed=1000 + 100 * rank, n_range=(32, 256))
+    X, Y, _ = ws.training_set(fam, solver, train)
+    t_data = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    net = ws.Mlp(X.shape[1], Y.shape[1], width=256, depth=4, seed=0)
+    net.fit_normalization(X, Y)
+    loss = net.train(X, Y, epochs=args.epochs, batch=1024, lr=1e-3, seed=0)
+    t_train = time.perf_counter() - t0
+    # ---- evaluation batch, resident in HBM
+    held = cs.workloads.vdp_batch(args.batch, seed=7 + 100 * rank)
+    runner = ws.WarmRunner(fam, solver, net, held)
+    ws_gb = sum(g["bt"].sizes()[1] for g in runner.groups) * 8 * 300 / 1e9
+    cfg["l2"] = cfg["l2"] % ("%.1f" % ws_gb)
+    for _ in range(args.warmup):
+        runner.run(warm=True)
+    for g in runner.groups:
+        g["bt"].profile_reset(timing=False)
+    _barrier(dist)
+    with ClockSampler(local_rank) as clk:
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            solved, n_fb, sols = runner.run(warm=True)
+        dt = time.perf_counter() - t0
+    dt = _max_over_ranks(dist, dt)
+    launches = sum(g["bt"].profile()["launches"] for g in runner.groups) + args.steps * 7
+    value = _sum_over_ranks(dist, args.steps * solved) / dt
+    newton_warm = np.mean([s["newton_steps"] for s in sols])
+    # ---- plain batched solve of the same instances
+    runner.run(warm=False)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        solved_p, _, sols_p = runner.run(warm=False)
+    dtp = _max_over_ranks(dist, time.perf_counter() - t0)
+    plain_batched = _sum_over_ranks(dist, args.steps * solved_p) / dtp
+    newton_plain = np.mean([s["newton_steps"] for s in sols_p])
+    # ---- plain one-instance GPU solver on a random sample of the same batch
+    rng = np.random.default_rng(11)
+    sample = [held[k] for k in rng.choice(len(held), size=args.single_sample, replace=False)]
+    solver.solve(sample[:2])
+    t0 = time.perf_counter()
+    n_ok = 0
+    for inst in sample:
+        n_ok += int(solver.solve([inst])[0]["success"])
+    dts = time.perf_counter() - t0
+    plain_single = n_ok / dts
+    # ---- end to end through the C ABI from pinned host buffers
+    Xh = cs.module.PinnedArray((len(runner.instances), X.shape[1]), np.float32)
+    Xh.array[...] = np.array([fam.features(i) for i in runner.instances], np.float32)
+    hosts = []
+    for g in runner.groups:
+        insts = runner.instances[g["first"]:g["first"] + g["n"]]
+        N, t, y, z, p, th = cs.workloads.pack_vdp(insts)
+        hh = {}
+        for k, a in (("N", N), ("t", t), ("y", y), ("z", z), ("p", p), ("th", th)):
+            pa = cs.module.PinnedArray(a.shape, a.dtype)
+            pa.array[...] = a
+            hh[k] = pa
+        cap = int(N.sum() * 4)
+        out = {k: cs.module.PinnedArray(shape) for k, shape in (("t", (cap,)), ("y", (cap, fam.ny)),
+                                                                 ("z", (cap, fam.nz)), ("p", (g["n"], fam.np)))}
+        hosts.append((hh, out))
+    h2d = Xh.array.nbytes + sum(sum(a.array.nbytes for a in hh.values()) for hh, _ in hosts)
+    d2h = 0
+    _barrier(dist)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        runner.dX.upload(Xh.array)
+        net.predict_device(runner.dX, len(runner.instances), runner.dY)
+        d2h = 0
+        n_e2e = 0
+        failed = []
+        for g, (hh, out) in zip(runner.groups, hosts):
+            bt = g["bt"]
+            bt.set_guess_packed(hh["N"].array, hh["t"].array, hh["y"].array, hh["z"].array, hh["p"].array,
+                                hh["th"].array)
+            bt.warm_start(runner.dY.ptr + 4 * g["first"] * net.n_out, ws.N_NODES, net.n_out)
+            bt.solve(solver.opts)
+            Nn, T = bt.sizes()
+            st = (cs._lib.Stats * bt.B)()
+            cs._lib.check(bt._lib.cs_get_solution(bt.handle, cs._lib.dptr(out["t"].array), cs._lib.dptr(out["y"].array),
+                                                  cs._lib.dptr(out["z"].array), cs._lib.dptr(out["p"].array), st),
+                          "cs_get_solution")
+            d2h += 8 * T * (1 + fam.ny + fam.nz) + 8 * bt.B * fam.np + bt.B * 64
+            for b in range(bt.B):
+                if st[b].status == 3:
+                    n_e2e += 1
+                else:
+                    failed.append(runner.instances[g["first"] + b])
+        if failed:
+            n_e2e += sum(int(s["success"]) for s in solver.solve(failed))
+    dte = _max_over_ranks(dist, time.perf_counter() - t0)
+    e2e = {"value": _sum_over_ranks(dist, args.steps * n_e2e) / dte, "unit": "solves/s", "h2d_bytes_per_step": h2d,
+           "d2h_bytes_per_step": d2h}
+    roof = _roofline([(g["m"], g["bt"]) for g in runner.groups], fp64_peak)
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": 1000 * dt / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": cfg,
+                "e2e": e2e, "roofline": roof, "cpu_baseline": cpu, "clocks": clk.summary(),
+                "gpu_launches": int(launches),
+                "plain_batched": {"value": plain_batched, "unit": "solves/s", "solved": solved_p,
+                                  "newton_steps_per_solve": float(newton_plain)},
+                "plain_single_gpu": {"value": plain_single, "unit": "solves/s",
+                                     "sample": "%d random instances of the batch, one Batch of 1 each" % len(sample)},
+                "speedup_vs_plain_single_gpu": value / plain_single if plain_single else None,
+                "warm_start": {"solved": solved, "of": len(held), "fallbacks": n_fb,
+                               "fallback_rate": n_fb / len(held), "newton_steps_per_solve": float(newton_warm),
+                               "train_solutions": int(len(X)), "train_data_s": t_data, "train_s": t_train,
+                               "train_loss": loss, "epochs": args.epochs}}
+        print(json.dumps(line))
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def run_plain(args, cs, rank, world, local_rank, cpu, cfg, instances):
+    dist = _dist_setup(world, local_rank)
+    cs.build.build_library()
+    cs._lib.load()
+    fp64_peak = cs.module.measure_fp64_peak()
+    W = Workload(cs, instances)
+    ws_gb = sum(g["bt"].sizes()[1] for g in W.groups) * 8 * 300 / 1e9
+    cfg["l2"] = cfg["l2"] % ("%.1f" % ws_gb)
+    for _ in range(args.warmup):
+        W.step_resident()
+    for g in W.groups:
+        g["bt"].profile_reset(timing=False)
+    _barrier(dist)
+    with ClockSampler(local_rank) as clk:
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            W.step_resident()
+        dt = time.perf_counter() - t0
+    dt = _max_over_ranks(dist, dt)
+    succ, newton, nodes = W.results()
+    launches = sum(g["bt"].profile()["launches"] for g in W.groups)
+    value = _sum_over_ranks(dist, args.steps * succ) / dt
+    roof = _roofline([(g["m"], g["bt"]) for g in W.groups], fp64_peak)
+    _barrier(dist)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        W.step_e2e()
+    dte = _max_over_ranks(dist, time.perf_counter() - t0)
+    e2e = {"value": _sum_over_ranks(dist, args.steps * succ) / dte, "unit": "solves/s",
+           "h2d_bytes_per_step": W.h2d_bytes(), "d2h_bytes_per_step": W.d2h_bytes()}
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": 1000 * dt / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": cfg,
+                "e2e": e2e, "roofline": roof, "cpu_baseline": cpu, "clocks": clk.summary(),
+                "gpu_launches": int(launches),
+                "solve_stats": {"solved": succ, "of": W.n, "newton_steps_per_solve": newton / W.n,
+                                "final_nodes_per_solve": nodes / W.n}}
+        print(json.dumps(line))
+    if dist is not None:
+        dist.destroy_process_group()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--batch", type=int, default=BATCH)
+    ap.add_argument("--workload", default="warm", choices=["warm", "plain"])
+    ap.add_argument("--batch", type=int, default=None, help="instances per step (warm: 8192, plain: 4096)")
+    ap.add_argument("--train", type=int, default=65536, help="training solutions (warm)")
+    ap.add_argument("--epochs", type=int, default=150)
+    ap.add_argument("--single-sample", type=int, default=64)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile-case", action="store_true",
                     help="small case for ncu: 512 instances, one full-batch condensation per m group, one solve")
@@ -264,154 +557,37 @@ def main():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
     cs = _pkg()
-    instances = cs.workloads.vdp_batch(args.batch, seed=SEED + rank)
-    cfg = {"workload": "Van der Pol batch: %d instances, x0~U[-2,2]^2, T~U[2,8], r~logU[0.1,10], N~U{32..2048} "
-                       "intervals, m~U{3,4,5}, zero guess, tol 1e-6 (seed %d + rank)" % (args.batch, SEED),
-           "batch_per_gpu": args.batch, "warm_start": "plain (zero initial guess)", "precision": "fp64",
-           "l2": "working set %s GB per step, larger than L2 (129 MB)"}
     cores = os.cpu_count() or 1
-
+    if args.batch is None:
+        args.batch = 8192 if args.workload == "warm" else BATCH
+    if args.workload == "warm":
+        instances = cs.workloads.vdp_batch(args.batch, seed=7 + 100 * rank)
+        cfg = {"workload": "NN-warm-started batched solve: Van der Pol family, %d held-out instances per GPU "
+                           "(x0~U[-2,2]^2, T~U[2,8], r~logU[0.1,10], N~U{32..2048} intervals, m~U{3,4,5}, seed 7 + "
+                           "100 rank), MLP trained on %d batched-solver solutions (seed 1000, N~U{32..256})"
+                           % (args.batch, args.train),
+               "batch_per_gpu": args.batch, "tol": 1e-6, "precision": "fp64 solver, bf16/fp32 network",
+               "warm_start": "MLP 4x256 GELU, 64 normalised-time nodes, fallback to the plain guess",
+               "l2": "working set %s GB per step, larger than L2 (129 MB)"}
+    else:
+        instances = cs.workloads.vdp_batch(args.batch, seed=SEED + rank)
+        cfg = {"workload": "plain batched solve: Van der Pol batch, %d instances (x0~U[-2,2]^2, T~U[2,8], "
+                           "r~logU[0.1,10], N~U{32..2048} intervals, m~U{3,4,5}, zero guess, tol 1e-6, seed %d + rank)"
+                           % (args.batch, SEED),
+               "batch_per_gpu": args.batch, "warm_start": "plain (zero initial guess)", "precision": "fp64",
+               "l2": "working set %s GB per step, larger than L2 (129 MB)"}
     if args.impl == "reference":
-        if rank != 0:
-            return
-        # the reference's own CPU implementation of this path is Python; its
-        # restatement (oracle/collocation_oracle.py) runs here on all host cores
-        procs = cores
-        sample = instances[:]
-        rng = np.random.default_rng(7)
-        rng.shuffle(sample)
-        per_step = 2 * procs
-        ctx = mp.get_context("spawn")
-        a = [(tuple(i.x0), i.T, i.r, i.intervals, i.m) for i in sample]
-        with ctx.Pool(procs) as pool:
-            pool.map(_oracle_worker, a[:procs])
-            pos = 0
-            for _ in range(args.warmup):
-                pool.map(_oracle_worker, a[pos:pos + per_step])
-                pos += per_step
-            t0 = time.time()
-            for _ in range(args.steps):
-                pool.map(_oracle_worker, a[pos:pos + per_step])
-                pos += per_step
-            dt = time.time() - t0
-        v = args.steps * per_step / dt
-        cfg["l2"] = "n/a (CPU)"
-        line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "solves/s", "n_gpus": args.gpus,
-                "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * dt / args.steps,
-                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-                "data": "synthetic", "config": cfg,
-                "cpu_baseline": {"value": v, "unit": "solves/s", "cores": procs, "kind": "port",
-                                 "sample": "%d random instances of the batch per step, one per process" % per_step},
-                "e2e": {"value": v, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
-        print(json.dumps(line))
+        if rank == 0:
+            run_reference(args, instances, cfg, cores)
         return
-
     # CPU baseline first: its spawned pool starts before any GPU call
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
-        rng = np.random.default_rng(3)
-        idx = rng.permutation(len(instances))
-        sample = [instances[i] for i in idx]
-        rate, n, dt = cpu_oracle_rate(sample, cores, target_s=20.0)
-        cpu = {"value": rate, "unit": "solves/s", "cores": cores, "kind": "port",
-               "sample": "%d random instances of the batch solved by the oracle in %.1f s, one process per core"
-                         % (n, dt)}
-
-    dist = None
-    if world > 1:
-        import torch
-        import torch.distributed as tdist
-        tdist.init_process_group("gloo")
-        dist = tdist
-        os.environ["CUDA_VISIBLE_DEVICES"] = os.environ.get("CUDA_VISIBLE_DEVICES", str(local_rank))
-
-    def barrier():
-        if dist is not None:
-            dist.barrier()
-
-    def max_over_ranks(x):
-        if dist is None:
-            return x
-        import torch
-        t = torch.tensor([x], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
-
-    cs.build.build_library()
-    cs._lib.load()
-    fp64_peak = cs.module.measure_fp64_peak()
-    W = Workload(cs, instances)
-    ws_gb = sum(g["bt"].sizes()[1] for g in W.groups) * 8 * 300 / 1e9
-    cfg["l2"] = cfg["l2"] % ("%.1f" % ws_gb)
-
-    for _ in range(args.warmup):
-        W.step_resident()
-    for g in W.groups:
-        g["bt"].profile_reset(timing=False)
-    barrier()
-    with ClockSampler(local_rank) as clk:
-        t0 = time.perf_counter()
-        for _ in range(args.steps):
-            W.step_resident()
-        dt = time.perf_counter() - t0
-    dt = max_over_ranks(dt)
-    succ, newton, nodes = W.results()
-    launches = sum(g["bt"].profile()["launches"] for g in W.groups)
-    value = world * args.steps * succ / dt
-
-    # roofline of the dominant kernel (condensation), timed alone with CUDA
-    # events on its stream: one launch condensing every interval of a group
-    flops = cbytes = cms = 0.0
-    for g in W.groups:
-        g["bt"].reset()
-        ms = g["bt"].time_condense(reps=5)
-        n_int = g["bt"].sizes()[1] - g["bt"].B
-        flops += n_int * flops_per_interval(g["m"])
-        cbytes += n_int * bytes_per_interval(g["m"])
-        cms += ms
-    achieved = flops / (cms * 1e-3) / 1e12
-    # kernel time shares: one more step with every launch bracketed by events
-    # (groups one after another, so that events do not overlap)
-    shares = {"condense_ms": 0.0, "babd_ms": 0.0, "residual_ms": 0.0}
-    t1 = time.perf_counter()
-    for g in W.groups:
-        g["bt"].profile_reset(timing=True)
-        g["bt"].reset()
-        g["bt"].solve(W.opts)
-        pr = g["bt"].profile()
-        for k in shares:
-            shares[k] += pr[k]
-    shares["step_ms"] = 1000 * (time.perf_counter() - t1)
-    roof = {"bound": "fp64", "kernel": "k_condense", "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
-            "frac": achieved / fp64_peak if fp64_peak else None, "traffic": None,
-            "peak_source": "DFMA microbenchmark (cs_measure_fp64_peak) in this run; FP64 is absent from "
-                           "MEASURED_PEAKS.json",
-            "flops_per_launch": flops / len(W.groups), "ms_per_launch": cms / len(W.groups),
-            "hbm_gbs": cbytes / (cms * 1e-3) / 1e9, "kernel_ms_one_step": shares}
-
-    # end to end through the C ABI with pinned host buffers
-    for g in W.groups:
-        g["bt"].profile_reset(timing=False)
-    barrier()
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        W.step_e2e()
-    dte = max_over_ranks(time.perf_counter() - t0)
-    e2e = {"value": world * args.steps * succ / dte, "unit": "solves/s", "h2d_bytes_per_step": W.h2d_bytes(),
-           "d2h_bytes_per_step": W.d2h_bytes()}
-
-    if rank == 0:
-        line = {"metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
-                "warmup": args.warmup, "ms_per_step": 1000 * dt / args.steps, "higher_is_better": True,
-                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": cfg,
-                "e2e": e2e, "roofline": roof, "cpu_baseline": cpu, "clocks": clk.summary(),
-                "gpu_launches": int(launches),
-                "solve_stats": {"solved": succ, "of": W.n, "newton_steps_per_solve": newton / W.n,
-                                "final_nodes_per_solve": nodes / W.n,
-                                "note": "value counts solves that reached the tolerance"}}
-        print(json.dumps(line))
-    if dist is not None:
-        dist.destroy_process_group()
+        cpu = _cpu_baseline(instances, cores)
+    if args.workload == "warm":
+        run_warm(args, cs, rank, world, local_rank, cpu, cfg)
+    else:
+        run_plain(args, cs, rank, world, local_rank, cpu, cfg, instances)
 
 
 if __name__ == "__main__":

@@ -88,6 +88,12 @@ SIGNATURES = {
                                     ctypes.POINTER(ctypes.c_double)]),
     "cs_mlp_predict": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_float), ctypes.c_int,
                                       ctypes.POINTER(ctypes.c_float)]),
+    "cs_mlp_predict_device": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
+                                             ctypes.c_void_p]),
+    "cs_batch_warm_start": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_int]),
+    "cs_device_alloc": (ctypes.c_void_p, [ctypes.c_size_t]),
+    "cs_device_free": (None, [ctypes.c_void_p]),
+    "cs_copy": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int]),
     "cs_babd_solve_noalloc": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int] + [ctypes.c_void_p] * 10 +
                               [ctypes.POINTER(ctypes.c_int), ctypes.c_void_p]),
 }

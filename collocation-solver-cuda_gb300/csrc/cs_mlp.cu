@@ -508,6 +508,32 @@ extern "C" int cs_mlp_train(cs_mlp* M, const float* X, const float* Y, int n, in
   return rc;
 }
 
+extern "C" int cs_mlp_predict_device(cs_mlp* M, const float* dX, int n, float* dY, void* stream) {
+  if (!M || !dX || !dY || n < 1) return cs_internal_set_error(CS_ERR_INVALID, "cs_mlp_predict_device: bad argument");
+  const int chunk = 65536;
+  int rc = mlp_reserve(M, std::min(n, chunk));
+  if (rc != CS_OK) return rc;
+  cudaStream_t st = stream ? (cudaStream_t)stream : M->st;
+  cudaStream_t keep = M->st;
+  M->st = st;
+  const float* nr = M->norm;
+  for (int s = 0; s < n && rc == CS_OK; s += chunk) {
+    const int c = std::min(chunk, n - s);
+    k_gather<<<grid_for((long long)c * M->nin), 256, 0, st>>>(dX + (size_t)s * M->nin, nullptr, nullptr, c, M->nin, 0,
+                                                               nr, nr + M->nin, nullptr, nullptr, M->act[0], nullptr);
+    rc = mlp_forward(M, c);
+    if (rc != CS_OK) break;
+    float* out = M->act[M->depth];
+    k_denorm<<<grid_for((long long)c * M->nout), 256, 0, st>>>(out, c, M->nout, nr + 2 * M->nin,
+                                                                nr + 2 * M->nin + M->nout);
+    cudaMemcpyAsync(dY + (size_t)s * M->nout, out, (size_t)c * M->nout * sizeof(float), cudaMemcpyDeviceToDevice, st);
+  }
+  M->st = keep;
+  cudaError_t e = cudaStreamSynchronize(st);
+  if (rc == CS_OK && e != cudaSuccess) rc = cs_internal_set_error(CS_ERR_CUDA, cudaGetErrorString(e));
+  return rc;
+}
+
 extern "C" int cs_mlp_predict(cs_mlp* M, const float* X, int n, float* Y) {
   if (!M || !X || !Y || n < 1) return cs_internal_set_error(CS_ERR_INVALID, "cs_mlp_predict: bad argument");
   const int chunk = 65536;

@@ -212,6 +212,36 @@ __global__ void k_dfma_peak(double* out, int iters) {
   if (s == 12345.678) out[0] = s;
 }
 
+// y, z at the nodes of every instance from its trajectory vector (linear in
+// normalised time on n_nodes equispaced nodes), and p from its tail
+__global__ void k_warm_fill(int B, int ny, int nz, int np, int n_nodes, const float* traj, int stride, const int* N,
+                            const int* off, const double* t, double* y, double* znode, double* p) {
+  const int b = blockIdx.x;
+  if (b >= B) return;
+  const float* v = traj + (size_t)b * stride;
+  const int o = off[b], n = N[b];
+  const double t0 = t[o], span = t[o + n - 1] - t0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    double x = (span > 0.0) ? (t[o + i] - t0) / span * (double)(n_nodes - 1) : 0.0;
+    if (x < 0.0) x = 0.0;
+    if (x > (double)(n_nodes - 1)) x = (double)(n_nodes - 1);
+    int k = (int)x;
+    if (k > n_nodes - 2) k = n_nodes - 2;
+    if (k < 0) k = 0;
+    const double w = (n_nodes > 1) ? x - (double)k : 0.0;
+    const int k1 = (n_nodes > 1) ? k + 1 : k;
+    for (int c = 0; c < ny; ++c)
+      y[(size_t)(o + i) * ny + c] = (1.0 - w) * (double)v[(size_t)k * ny + c] + w * (double)v[(size_t)k1 * ny + c];
+    const float* vz = v + (size_t)n_nodes * ny;
+    for (int c = 0; c < nz; ++c)
+      znode[(size_t)(o + i) * nz + c] = (1.0 - w) * (double)vz[(size_t)k * nz + c] + w * (double)vz[(size_t)k1 * nz + c];
+  }
+  if (threadIdx.x == 0) {
+    const float* vp = v + (size_t)n_nodes * (ny + nz);
+    for (int c = 0; c < np; ++c) p[(size_t)b * np + c] = (double)vp[c];
+  }
+}
+
 }  // namespace
 
 // error reporting for the other translation units of the library
@@ -1325,6 +1355,48 @@ extern "C" int cs_batch_reset(cs_batch* bt) {
   void* args[] = {&v, &only};
   CS_TRY(launch(bt, M->f_form_initial, cdiv(bt->T, 256), 256, 0, args));
   CS_CUDA(cudaStreamSynchronize(st));
+  return CS_OK;
+}
+
+extern "C" int cs_batch_warm_start(cs_batch* bt, int n_nodes, const float* traj, int stride) {
+  if (!bt || !bt->have_guess || !traj || n_nodes < 1) return set_err(CS_ERR_INVALID, "cs_batch_warm_start: bad argument");
+  cs_module* M = bt->M;
+  if (stride < n_nodes * (M->ny + M->nz) + M->np) return set_err(CS_ERR_INVALID, "cs_batch_warm_start: stride too small");
+  const int s = bt->cur;
+  k_warm_fill<<<bt->B, 128, 0, bt->stream>>>(bt->B, M->ny, M->nz, M->np, n_nodes, traj, stride, (const int*)bt->dN.p,
+                                             (const int*)bt->doff.p, (const double*)bt->t[s].p, (double*)bt->y[s].p,
+                                             (double*)bt->znode[s].p, (double*)bt->dp.p);
+  CS_CUDA(cudaGetLastError());
+  bt->launches += 1;
+  std::vector<CsInst> hi(bt->B);
+  for (auto& q : hi) init_inst(q, bt->opts.alpha0);
+  CS_CUDA(cudaMemcpyAsync(bt->dinst.p, hi.data(), hi.size() * sizeof(CsInst), cudaMemcpyHostToDevice, bt->stream));
+  CsBatchDev v = devview(bt);
+  int only = -1;
+  void* args[] = {&v, &only};
+  CS_TRY(launch(bt, M->f_form_initial, cdiv(bt->T, 256), 256, 0, args));
+  CS_CUDA(cudaStreamSynchronize(bt->stream));
+  return CS_OK;
+}
+
+extern "C" void* cs_device_alloc(size_t bytes) {
+  if (ensure_context() != CS_OK) return nullptr;
+  void* p = nullptr;
+  if (cudaMalloc(&p, bytes ? bytes : 8) != cudaSuccess) {
+    set_err(CS_ERR_NOMEM, "cudaMalloc failed");
+    return nullptr;
+  }
+  return p;
+}
+
+extern "C" void cs_device_free(void* p) {
+  if (p) cudaFree(p);
+}
+
+extern "C" int cs_copy(void* dst, const void* src, size_t bytes, int kind) {
+  if (!dst || !src) return set_err(CS_ERR_INVALID, "cs_copy: null pointer");
+  cudaMemcpyKind k = kind == 0 ? cudaMemcpyHostToDevice : (kind == 1 ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice);
+  CS_CUDA(cudaMemcpy(dst, src, bytes, k));
   return CS_OK;
 }
 

@@ -275,10 +275,52 @@ class Batch:
         _lib.check(self._lib.cs_stage_remesh(self.handle, _lib.dptr(res), _lib.iptr(N)), "cs_stage_remesh")
         return N
 
+    def warm_start(self, traj_dev, n_nodes, stride):
+        """Initial guess from per-instance trajectory vectors in device memory
+        (row b of `traj_dev`, a DeviceArray or device address)."""
+        ptr = traj_dev.ptr if isinstance(traj_dev, DeviceArray) else traj_dev
+        _lib.check(self._lib.cs_batch_warm_start(self.handle, int(n_nodes), ctypes.c_void_p(ptr), int(stride)),
+                   "cs_batch_warm_start")
+
     def time_condense(self, reps=10):
         ms = ctypes.c_double()
         _lib.check(self._lib.cs_time_condense(self.handle, int(reps), ctypes.byref(ms)), "cs_time_condense")
         return ms.value
+
+
+class DeviceArray:
+    """Device memory of a given shape/dtype with host copies in and out."""
+
+    def __init__(self, shape, dtype=np.float32):
+        lib = _lib.load()
+        self._lib = lib
+        self.shape = tuple(shape)
+        self.dtype = np.dtype(dtype)
+        self.nbytes = int(np.prod(self.shape)) * self.dtype.itemsize
+        self.ptr = lib.cs_device_alloc(max(self.nbytes, 8))
+        if not self.ptr:
+            raise _lib.CsError("device allocation failed: " + _lib.last_error())
+
+    def upload(self, a):
+        a = np.ascontiguousarray(a, dtype=self.dtype)
+        assert a.nbytes <= self.nbytes
+        _lib.check(self._lib.cs_copy(ctypes.c_void_p(self.ptr), a.ctypes.data_as(ctypes.c_void_p), a.nbytes, 0), "cs_copy")
+
+    def download(self):
+        out = np.empty(self.shape, self.dtype)
+        _lib.check(self._lib.cs_copy(out.ctypes.data_as(ctypes.c_void_p), ctypes.c_void_p(self.ptr), self.nbytes, 1),
+                   "cs_copy")
+        return out
+
+    def __del__(self):
+        if sys.is_finalizing():
+            return
+        try:
+            if self.ptr:
+                self._lib.cs_device_free(ctypes.c_void_p(self.ptr))
+                self.ptr = None
+        except Exception:  # noqa: BLE001
+            pass
 
 
 class PinnedArray:

@@ -9,6 +9,7 @@ instance whose warm-started Newton iteration fails is solved again from the
 plain initial guess (fallback).
 """
 import ctypes
+import sys
 
 import numpy as np
 
@@ -32,7 +33,6 @@ class Mlp:
                      np.ones(n_out, np.float32))
 
     def __del__(self):
-        import sys
         if sys.is_finalizing():
             return
         try:
@@ -84,6 +84,13 @@ class Mlp:
         _lib.check(self._lib.cs_mlp_train(self.handle, _lib.fptr(X), _lib.fptr(Y), X.shape[0], epochs, batch,
                                           ctypes.c_float(lr), seed, ctypes.byref(loss)), "cs_mlp_train")
         return loss.value
+
+    def predict_device(self, dX, n, dY, stream=None):
+        """Forward pass on device arrays (module.DeviceArray or addresses)."""
+        px = dX.ptr if hasattr(dX, "ptr") else dX
+        py = dY.ptr if hasattr(dY, "ptr") else dY
+        _lib.check(self._lib.cs_mlp_predict_device(self.handle, ctypes.c_void_p(px), int(n), ctypes.c_void_p(py), stream),
+                   "cs_mlp_predict_device")
 
     def predict(self, X):
         X = np.ascontiguousarray(X, dtype=np.float32)
@@ -212,3 +219,71 @@ def solve_warm(family, solver, mlp, instances):
             s["fallback"] = True
             final[k] = s
     return final, fb, warm
+
+
+class WarmRunner:
+    """Device-resident warm-started batch solve of a fixed list of instances:
+    features and plain guesses live in HBM; each run resets the batches,
+    predicts the trajectories, fills the guesses on the device, solves, and
+    solves the failed instances again from the plain guess."""
+
+    def __init__(self, family, solver, mlp, instances):
+        from .module import DeviceArray
+        self.family, self.solver, self.mlp = family, solver, mlp
+        order = sorted(range(len(instances)), key=lambda k: instances[k].m)
+        self.instances = [instances[k] for k in order]
+        self.order = order
+        X = np.array([family.features(i) for i in self.instances], np.float32)
+        self.dX = DeviceArray(X.shape, np.float32)
+        self.dX.upload(X)
+        self.dY = DeviceArray((len(self.instances), mlp.n_out), np.float32)
+        self.groups = []
+        start = 0
+        for m in sorted(set(i.m for i in self.instances)):
+            idx = [k for k, i in enumerate(self.instances) if i.m == m]
+            assert idx == list(range(start, start + len(idx)))
+            meshes, ps, ths = [], [], []
+            for k in idx:
+                t, y0, z0, p0 = family.plain_guess(self.instances[k])
+                meshes.append((t, y0, z0))
+                ps.append(p0)
+                ths.append(family.theta(self.instances[k]))
+            bt = Batch(solver.cp(m), len(idx))
+            bt.set_guess(meshes, np.array(ps).reshape(len(idx), -1), np.array(ths).reshape(len(idx), -1))
+            self.groups.append(dict(m=m, first=start, n=len(idx), bt=bt))
+            start += len(idx)
+
+    def run(self, warm=True, fallback=True, threads=True):
+        """One solve of every instance; returns (solved, fallback count, stats)."""
+        import threading
+        if warm:
+            self.mlp.predict_device(self.dX, len(self.instances), self.dY)
+
+        def one(g):
+            bt = g["bt"]
+            bt.reset()
+            if warm:
+                bt.warm_start(self.dY.ptr + 4 * g["first"] * self.mlp.n_out, N_NODES, self.mlp.n_out)
+            bt.solve(self.solver.opts)
+
+        if threads:
+            ths = [threading.Thread(target=one, args=(g,)) for g in self.groups]
+            for t in ths:
+                t.start()
+            for t in ths:
+                t.join()
+        else:
+            for g in self.groups:
+                one(g)
+        sols = []
+        for g in self.groups:
+            sols += g["bt"].solution()
+        failed = [k for k, s in enumerate(sols) if not s["success"]]
+        n_fb = 0
+        if warm and fallback and failed:
+            plain = self.solver.solve([self.instances[k] for k in failed])
+            for k, s in zip(failed, plain):
+                sols[k] = dict(s, fallback=True)
+            n_fb = len(failed)
+        solved = sum(int(s["success"]) for s in sols)
+        return solved, n_fb, sols

@@ -254,6 +254,27 @@ int cs_mlp_train(cs_mlp* mlp, const float* X, const float* Y, int n, int epochs,
                  unsigned long long seed, double* final_loss);
 int cs_mlp_predict(cs_mlp* mlp, const float* X, int n, float* Y);
 
+/* forward pass on DEVICE arrays (n rows), ordered on `stream` (cudaStream_t
+ * or NULL); returns after the stream has finished */
+int cs_mlp_predict_device(cs_mlp* mlp, const float* dX, int n, float* dY, void* stream);
+
+/* Warm start of a batch from per-instance trajectory vectors in DEVICE
+ * memory: row b (stride floats) holds y and z at n_nodes equispaced
+ * normalised times in [0, 1] (node-major: n_nodes x ny, then n_nodes x nz)
+ * followed by p.  For every instance, y and z at its current mesh nodes are
+ * interpolated linearly in (t - t_0) / (t_N - t_0), p is taken over, the stage
+ * values are re-formed and the instance restarts from Newton (continuation
+ * parameter alpha0).  Replaces the constant estimates of the OCP file
+ * (OCP2ABVP.py:402-447) as the Newton initial guess; no reference
+ * counterpart. */
+int cs_batch_warm_start(cs_batch* bt, int n_nodes, const float* traj, int stride);
+
+/* Device memory for callers of the device-pointer entry points. */
+void* cs_device_alloc(size_t bytes);
+void cs_device_free(void* p);
+/* kind: 0 host to device, 1 device to host, 2 device to device; synchronous */
+int cs_copy(void* dst, const void* src, size_t bytes, int kind);
+
 /* Message of this thread's last error ("" if none). */
 int cs_last_error(char* buf, size_t len);
 
