@@ -393,6 +393,7 @@ def run_warm(args, cs, rank, world, local_rank, cpu, cfg):
             solved, n_fb, sols = runner.run(warm=True)
         dt = time.perf_counter() - t0
     dt = _max_over_ranks(dist, dt)
+    runner_times = dict(runner.times)
     launches = sum(g["bt"].profile()["launches"] for g in runner.groups) + args.steps * 7
     value = _sum_over_ranks(dist, args.steps * solved) / dt
     newton_warm = np.mean([s["newton_steps"] for s in sols])
@@ -474,7 +475,7 @@ def run_warm(args, cs, rank, world, local_rank, cpu, cfg):
                 "plain_single_gpu": {"value": plain_single, "unit": "solves/s",
                                      "sample": "%d random instances of the batch, one Batch of 1 each" % len(sample)},
                 "speedup_vs_plain_single_gpu": value / plain_single if plain_single else None,
-                "warm_start": {"solved": solved, "of": len(held), "fallbacks": n_fb,
+                "warm_start": {"solved": solved, "of": len(held), "fallbacks": n_fb, "phase_s": runner_times,
                                "fallback_rate": n_fb / len(held), "newton_steps_per_solve": float(newton_warm),
                                "train_solutions": int(len(X)), "train_data_s": t_data, "train_s": t_train,
                                "train_loss": loss, "epochs": args.epochs}}

@@ -254,10 +254,14 @@ class WarmRunner:
             start += len(idx)
 
     def run(self, warm=True, fallback=True, threads=True):
-        """One solve of every instance; returns (solved, fallback count, stats)."""
+        """One solve of every instance; returns (solved, fallback count, stats).
+        self.times holds the seconds of the phases of the last run."""
         import threading
+        import time
+        t0 = time.perf_counter()
         if warm:
             self.mlp.predict_device(self.dX, len(self.instances), self.dY)
+        t1 = time.perf_counter()
 
         def one(g):
             bt = g["bt"]
@@ -275,15 +279,19 @@ class WarmRunner:
         else:
             for g in self.groups:
                 one(g)
+        t2 = time.perf_counter()
         sols = []
         for g in self.groups:
             sols += g["bt"].solution()
         failed = [k for k, s in enumerate(sols) if not s["success"]]
         n_fb = 0
+        t3 = time.perf_counter()
         if warm and fallback and failed:
             plain = self.solver.solve([self.instances[k] for k in failed])
             for k, s in zip(failed, plain):
                 sols[k] = dict(s, fallback=True)
             n_fb = len(failed)
+        t4 = time.perf_counter()
+        self.times = {"predict_s": t1 - t0, "solve_s": t2 - t1, "collect_s": t3 - t2, "fallback_s": t4 - t3}
         solved = sum(int(s["success"]) for s in sols)
         return solved, n_fb, sols
