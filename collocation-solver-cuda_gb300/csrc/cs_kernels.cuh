@@ -1052,97 +1052,100 @@ extern "C" __global__ void k_tree_level(CsBatch bt, int l) {
 // boundary conditions, [At Ct Ht 0; B_0 B_n V_n] [y_0; y_N; p] = [bt; -r],
 // by Householder QR (the reference: final block QR + np.linalg.solve,
 // solve_babd_system.py:366-423).  Sets the line search going (alpha = 1).
-extern "C" __global__ void k_top(CsBatch bt) {
-  extern __shared__ double smem[];
-  const int wpc = blockDim.x >> 5, w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  double* top = smem + (size_t)w * CS_TLD * (CS_NT + 1);
-  const int njac = bt.nlist[1];
-  for (int k = blockIdx.x * wpc + w; k < njac; k += gridDim.x * wpc) {
-    const int b = bt.jac[k];
-    const int N = bt.N[b], off = bt.off[b];
-    const int L = cs_levels(N - 1);
-    const double* row = ((L & 1) ? bt.rows1 : bt.rows0) + (size_t)off * CS_ROWSZ;
-    for (int c = lane; c < CS_NT + 1; c += 32) {
-      double* col = top + (size_t)c * CS_TLD;
-      for (int r = 0; r < CS_NY; ++r) {
-        double v;
-        if (c < 2 * CS_NY + CS_NPE) v = row[c * CS_NY + r];
-        else if (c < CS_NT) v = 0.0;
-        else v = row[(2 * CS_NY + CS_NPE) * CS_NY + r];
-        col[r] = v;
-      }
+// top system of instance b, one warp (top: per-warp shared memory)
+__device__ void cs_top_warp(const CsBatch& bt, int b, double* top) {
+  const int lane = threadIdx.x & 31;
+  const int N = bt.N[b], off = bt.off[b];
+  const int L = cs_levels(N - 1);
+  const double* row = ((L & 1) ? bt.rows1 : bt.rows0) + (size_t)off * CS_ROWSZ;
+  for (int c = lane; c < CS_NT + 1; c += 32) {
+    double* col = top + (size_t)c * CS_TLD;
+    for (int r = 0; r < CS_NY; ++r) {
+      double v;
+      if (c < 2 * CS_NY + CS_NPE) v = row[c * CS_NY + r];
+      else if (c < CS_NT) v = 0.0;
+      else v = row[(2 * CS_NY + CS_NPE) * CS_NY + r];
+      col[r] = v;
     }
-    if (lane == 0) {
-      const double* th = bt.th + (size_t)b * (CS_NTH > 0 ? CS_NTH : 1);
-      double ya[CS_NY], yb[CS_NY], pl[CS_NP > 0 ? CS_NP : 1], r[CS_NY + CS_NP];
-      double Dr[(CS_NY + CS_NP) * (2 * CS_NY + CS_NP)];
-      for (int q = 0; q < CS_NY; ++q) { ya[q] = bt.y[(size_t)off * CS_NY + q]; yb[q] = bt.y[(size_t)(off + N - 1) * CS_NY + q]; }
-      for (int q = 0; q < CS_NP; ++q) pl[q] = bt.p[(size_t)b * CS_NP + q];
-      cs_r(ya, yb, pl, th, r);
-      cs_Dr(ya, yb, pl, th, Dr);
-      for (int q = 0; q < CS_NY + CS_NP; ++q) {
-        for (int c = 0; c < CS_NY; ++c) top[(size_t)c * CS_TLD + CS_NY + q] = Dr[q * (2 * CS_NY + CS_NP) + c];
-        for (int c = 0; c < CS_NY; ++c) top[(size_t)(CS_NY + c) * CS_TLD + CS_NY + q] = Dr[q * (2 * CS_NY + CS_NP) + CS_NY + c];
-        for (int c = 0; c < CS_NP; ++c) top[(size_t)(2 * CS_NY + c) * CS_TLD + CS_NY + q] = Dr[q * (2 * CS_NY + CS_NP) + 2 * CS_NY + c];
-        top[(size_t)CS_NT * CS_TLD + CS_NY + q] = -r[q];
-      }
+  }
+  if (lane == 0) {
+    const double* th = bt.th + (size_t)b * (CS_NTH > 0 ? CS_NTH : 1);
+    double ya[CS_NY], yb[CS_NY], pl[CS_NP > 0 ? CS_NP : 1], r[CS_NY + CS_NP];
+    double Dr[(CS_NY + CS_NP) * (2 * CS_NY + CS_NP)];
+    for (int q = 0; q < CS_NY; ++q) { ya[q] = bt.y[(size_t)off * CS_NY + q]; yb[q] = bt.y[(size_t)(off + N - 1) * CS_NY + q]; }
+    for (int q = 0; q < CS_NP; ++q) pl[q] = bt.p[(size_t)b * CS_NP + q];
+    cs_r(ya, yb, pl, th, r);
+    cs_Dr(ya, yb, pl, th, Dr);
+    for (int q = 0; q < CS_NY + CS_NP; ++q) {
+      for (int c = 0; c < CS_NY; ++c) top[(size_t)c * CS_TLD + CS_NY + q] = Dr[q * (2 * CS_NY + CS_NP) + c];
+      for (int c = 0; c < CS_NY; ++c) top[(size_t)(CS_NY + c) * CS_TLD + CS_NY + q] = Dr[q * (2 * CS_NY + CS_NP) + CS_NY + c];
+      for (int c = 0; c < CS_NP; ++c) top[(size_t)(2 * CS_NY + c) * CS_TLD + CS_NY + q] = Dr[q * (2 * CS_NY + CS_NP) + 2 * CS_NY + c];
+      top[(size_t)CS_NT * CS_TLD + CS_NY + q] = -r[q];
+    }
+  }
+  __syncwarp();
+#pragma unroll 1
+  for (int kk = 0; kk < CS_NT; ++kk) {
+    const double* vk = top + (size_t)kk * CS_TLD;
+    double ss = 0.0;
+    for (int r = kk + lane; r < CS_NT; r += 32) ss += vk[r] * vk[r];
+    for (int o = 16; o > 0; o >>= 1) ss += __shfl_xor_sync(0xffffffffu, ss, o);
+    const double x0 = vk[kk];
+    const double sgn = (x0 >= 0.0) ? 1.0 : -1.0;
+    const double g = -sgn * sqrt(ss);
+    const double v0 = x0 - g;
+    const double vs = ss - x0 * x0 + v0 * v0;
+    __syncwarp();
+    if (vs < CS_EPS) continue;
+    const double beta = -2.0 / vs;
+    for (int c = kk + 1 + lane; c < CS_NT + 1; c += 32) {
+      double* col = top + (size_t)c * CS_TLD;
+      double wv = v0 * col[kk];
+      for (int r = kk + 1; r < CS_NT; ++r) wv += vk[r] * col[r];
+      const double bw = beta * wv;
+      col[kk] = fma(bw, v0, col[kk]);
+      for (int r = kk + 1; r < CS_NT; ++r) col[r] = fma(bw, vk[r], col[r]);
     }
     __syncwarp();
-#pragma unroll 1
-    for (int kk = 0; kk < CS_NT; ++kk) {
-      const double* vk = top + (size_t)kk * CS_TLD;
-      double ss = 0.0;
-      for (int r = kk + lane; r < CS_NT; r += 32) ss += vk[r] * vk[r];
-      for (int o = 16; o > 0; o >>= 1) ss += __shfl_xor_sync(0xffffffffu, ss, o);
-      const double x0 = vk[kk];
-      const double sgn = (x0 >= 0.0) ? 1.0 : -1.0;
-      const double g = -sgn * sqrt(ss);
-      const double v0 = x0 - g;
-      const double vs = ss - x0 * x0 + v0 * v0;
-      __syncwarp();
-      if (vs < CS_EPS) continue;
-      const double beta = -2.0 / vs;
-      for (int c = kk + 1 + lane; c < CS_NT + 1; c += 32) {
-        double* col = top + (size_t)c * CS_TLD;
-        double wv = v0 * col[kk];
-        for (int r = kk + 1; r < CS_NT; ++r) wv += vk[r] * col[r];
-        const double bw = beta * wv;
-        col[kk] = fma(bw, v0, col[kk]);
-        for (int r = kk + 1; r < CS_NT; ++r) col[r] = fma(bw, vk[r], col[r]);
-      }
-      __syncwarp();
-      if (lane == 0) {
-        double* col = top + (size_t)kk * CS_TLD;
-        col[kk] = g;
-        for (int r = kk + 1; r < CS_NT; ++r) col[r] = 0.0;
-      }
-      __syncwarp();
-    }
     if (lane == 0) {
-      double* rhs = top + (size_t)CS_NT * CS_TLD;
-      bool sing = false;
-      for (int r = CS_NT - 1; r >= 0; --r) {
-        double v = rhs[r];
-        for (int c = r + 1; c < CS_NT; ++c) v -= top[(size_t)c * CS_TLD + r] * rhs[c];
-        const double d = top[(size_t)r * CS_TLD + r];
-        if (d == 0.0) sing = true;
-        rhs[r] = (d != 0.0) ? v / d : 0.0;
-      }
-      if (sing) {
-        for (int r = 0; r < CS_NT; ++r) rhs[r] = 0.0;
-        bt.inst[b].singular += 1;
-      }
-      for (int q = 0; q < CS_NY; ++q) {
-        bt.dy[(size_t)off * CS_NY + q] = rhs[q];
-        bt.dy[(size_t)(off + N - 1) * CS_NY + q] = rhs[CS_NY + q];
-      }
-      for (int q = 0; q < CS_NP; ++q) bt.dp[(size_t)b * CS_NP + q] = rhs[2 * CS_NY + q];
-      bt.inst[b].status = ST_LS;
-      bt.inst[b].alpha_ls = 1.0;
-      bt.inst[b].ls_it = 0;
+      double* col = top + (size_t)kk * CS_TLD;
+      col[kk] = g;
+      for (int r = kk + 1; r < CS_NT; ++r) col[r] = 0.0;
     }
     __syncwarp();
   }
+  if (lane == 0) {
+    double* rhs = top + (size_t)CS_NT * CS_TLD;
+    bool sing = false;
+    for (int r = CS_NT - 1; r >= 0; --r) {
+      double v = rhs[r];
+      for (int c = r + 1; c < CS_NT; ++c) v -= top[(size_t)c * CS_TLD + r] * rhs[c];
+      const double d = top[(size_t)r * CS_TLD + r];
+      if (d == 0.0) sing = true;
+      rhs[r] = (d != 0.0) ? v / d : 0.0;
+    }
+    if (sing) {
+      for (int r = 0; r < CS_NT; ++r) rhs[r] = 0.0;
+      bt.inst[b].singular += 1;
+    }
+    for (int q = 0; q < CS_NY; ++q) {
+      bt.dy[(size_t)off * CS_NY + q] = rhs[q];
+      bt.dy[(size_t)(off + N - 1) * CS_NY + q] = rhs[CS_NY + q];
+    }
+    for (int q = 0; q < CS_NP; ++q) bt.dp[(size_t)b * CS_NP + q] = rhs[2 * CS_NY + q];
+    bt.inst[b].status = ST_LS;
+    bt.inst[b].alpha_ls = 1.0;
+    bt.inst[b].ls_it = 0;
+  }
+  __syncwarp();
+}
+
+extern "C" __global__ void k_top(CsBatch bt) {
+  extern __shared__ double smem[];
+  const int wpc = blockDim.x >> 5, w = threadIdx.x >> 5;
+  double* top = smem + (size_t)w * CS_TLD * (CS_NT + 1);
+  const int njac = bt.nlist[1];
+  for (int k = blockIdx.x * wpc + w; k < njac; k += gridDim.x * wpc) cs_top_warp(bt, bt.jac[k], top);
 }
 
 // Back substitution of one tree level (top-down), warp per merge.
@@ -1213,6 +1216,98 @@ extern "C" __global__ void k_recover(CsBatch bt) {
       if (a < CS_NY) bt.dydot[((size_t)slot * CS_M + j) * CS_NY + a] = -v;
       else bt.dzt[((size_t)slot * CS_M + j) * CS_NZ + (a - CS_NY)] = -v;
     }
+  }
+}
+
+// The whole Newton direction of one instance in one CTA: tree levels up,
+// top system, back substitution down, stage recovery, then the line search
+// starts (alpha = 1).  One launch per super-step instead of 2 L + 3, which is
+// what matters when few instances are left; used for batches of small and
+// medium instances (the per-level kernels above serve large single ones).
+extern "C" __global__ void __launch_bounds__(256) k_babd_cta(CsBatch bt) {
+  extern __shared__ double smem[];
+  const int nw = blockDim.x >> 5, w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  double* top = smem;                                  // CS_TLD x (CS_NT + 1)
+  double* Qw = smem + (size_t)CS_TLD * (CS_NT + 1) + (size_t)w * CS_QLD * CS_QC;  // merge matrix per warp
+  const int njac = bt.nlist[1];
+  for (int k = blockIdx.x; k < njac; k += gridDim.x) {
+    const int b = bt.jac[k];
+    const int N = bt.N[b], off = bt.off[b];
+    const int n0 = N - 1;
+    const int L = cs_levels(n0);
+    // ---- tree up
+    for (int l = 0; l < L; ++l) {
+      const int nl = cs_rows_at(n0, l);
+      const int merges = nl >> 1, items = (nl + 1) >> 1;
+      const double* src = ((l & 1) ? bt.rows1 : bt.rows0) + (size_t)off * CS_ROWSZ;
+      double* dst = ((l & 1) ? bt.rows0 : bt.rows1) + (size_t)off * CS_ROWSZ;
+#if CS_TREE_THREAD
+      for (int mi = threadIdx.x; mi < items; mi += blockDim.x) {
+        if (mi < merges) {
+          cs_merge_thread(src + (size_t)(2 * mi) * CS_ROWSZ, src + (size_t)(2 * mi + 1) * CS_ROWSZ,
+                          dst + (size_t)mi * CS_ROWSZ, bt.tree + (size_t)(off + ((2 * mi + 1) << l)) * CS_TREESZ);
+        } else {
+          const double* sr = src + (size_t)(nl - 1) * CS_ROWSZ;
+          double* dr = dst + (size_t)merges * CS_ROWSZ;
+          for (int q = 0; q < CS_ROWSZ; ++q) dr[q] = sr[q];
+        }
+      }
+#else
+      for (int mi = w; mi < items; mi += nw) {
+        if (mi < merges) {
+          cs_merge_warp(src + (size_t)(2 * mi) * CS_ROWSZ, src + (size_t)(2 * mi + 1) * CS_ROWSZ,
+                        dst + (size_t)mi * CS_ROWSZ, bt.tree + (size_t)(off + ((2 * mi + 1) << l)) * CS_TREESZ, Qw);
+        } else {
+          const double* sr = src + (size_t)(nl - 1) * CS_ROWSZ;
+          double* dr = dst + (size_t)merges * CS_ROWSZ;
+          for (int q = lane; q < CS_ROWSZ; q += 32) dr[q] = sr[q];
+        }
+        __syncwarp();
+      }
+#endif
+      __syncthreads();
+    }
+    // ---- top system (warp 0)
+    if (w == 0) cs_top_warp(bt, b, top);
+    __syncthreads();
+    // ---- back substitution down
+    const double* dpv = bt.dp + (size_t)b * CS_NP;
+    for (int l = L - 1; l >= 0; --l) {
+      const int merges = cs_rows_at(n0, l) >> 1;
+#if CS_TREE_THREAD
+      for (int mi = threadIdx.x; mi < merges; mi += blockDim.x) {
+        const int mid = (2 * mi + 1) << l, left = (2 * mi) << l;
+        int right = (2 * mi + 2) << l;
+        if (right > n0) right = n0;
+        cs_backsub_thread(bt.tree + (size_t)(off + mid) * CS_TREESZ, bt.dy + (size_t)(off + left) * CS_NY,
+                          bt.dy + (size_t)(off + right) * CS_NY, dpv, bt.dy + (size_t)(off + mid) * CS_NY);
+      }
+#else
+      for (int mi = w; mi < merges; mi += nw) {
+        const int mid = (2 * mi + 1) << l, left = (2 * mi) << l;
+        int right = (2 * mi + 2) << l;
+        if (right > n0) right = n0;
+        cs_backsub_warp(bt.tree + (size_t)(off + mid) * CS_TREESZ, bt.dy + (size_t)(off + left) * CS_NY,
+                        bt.dy + (size_t)(off + right) * CS_NY, dpv, bt.dy + (size_t)(off + mid) * CS_NY);
+      }
+#endif
+      __syncthreads();
+    }
+    // ---- stage recovery, warp per interval, lanes over stage rows
+    for (int iv = w; iv < n0; iv += nw) {
+      const int slot = off + iv;
+      const double* X = bt.X + (size_t)slot * CS_NRHS * CS_S;
+      const double* dyi = bt.dy + (size_t)slot * CS_NY;
+      for (int r = lane; r < CS_S; r += 32) {
+        double v = X[(size_t)(CS_NY + CS_NPE) * CS_S + r];
+        for (int q = 0; q < CS_NY; ++q) v = fma(X[(size_t)q * CS_S + r], dyi[q], v);
+        for (int q = 0; q < CS_NPE; ++q) v = fma(X[(size_t)(CS_NY + q) * CS_S + r], dpv[q], v);
+        const int j = r / (CS_NY + CS_NZ), a = r % (CS_NY + CS_NZ);
+        if (a < CS_NY) bt.dydot[((size_t)slot * CS_M + j) * CS_NY + a] = -v;
+        else bt.dzt[((size_t)slot * CS_M + j) * CS_NZ + (a - CS_NY)] = -v;
+      }
+    }
+    __syncthreads();
   }
 }
 

@@ -253,7 +253,9 @@ struct cs_module {
   size_t rowsz, treesz;
   CUmodule mod = nullptr;
   CUfunction f_form_initial, f_residual, f_decide, f_accept, f_condense, f_segres, f_mesh_decide,
-      f_remesh_count, f_remesh_write, f_repack, f_znodes, f_lists, f_tree_level, f_top, f_backsub_level, f_recover;
+      f_remesh_count, f_remesh_write, f_repack, f_znodes, f_lists, f_tree_level, f_top, f_backsub_level, f_recover,
+      f_babd_cta;
+  size_t babd_cta_smem;
   int condense_block, condense_per_cta;
   size_t condense_smem;
   size_t tree_smem;   // per CTA of 4 warps
@@ -391,6 +393,7 @@ extern "C" int cs_module_load(const cs_module_desc* d, cs_module** out) {
     return set_err(CS_ERR_INVALID, "cs_module_load: BABD blocks do not fit in shared memory");
   }
   M->top_wpc = (int)std::max<size_t>(1, std::min<size_t>(4, (size_t)smem_optin / top_per));
+  M->babd_cta_smem = top_per + (size_t)8 * qld * qc * sizeof(double);
   M->top_smem = top_per * M->top_wpc;
   CS_CUDA(cudaDeviceGetAttribute(&M->sms, cudaDevAttrMultiProcessorCount, dev));
 
@@ -421,7 +424,7 @@ extern "C" int cs_module_load(const cs_module_desc* d, cs_module** out) {
              {&M->f_repack, "k_repack"},             {&M->f_znodes, "k_znodes"},
              {&M->f_lists, "k_lists"},               {&M->f_tree_level, "k_tree_level"},
              {&M->f_top, "k_top"},                   {&M->f_backsub_level, "k_backsub_level"},
-             {&M->f_recover, "k_recover"}};
+             {&M->f_recover, "k_recover"},           {&M->f_babd_cta, "k_babd_cta"}};
   for (auto& e : fns) {
     CUresult rr = g_drv.moduleGetFunction(e.f, M->mod, e.name);
     if (rr != CUDA_SUCCESS) {
@@ -436,6 +439,9 @@ extern "C" int cs_module_load(const cs_module_desc* d, cs_module** out) {
     CS_CU(g_drv.funcSetAttribute(M->f_tree_level, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, (int)M->tree_smem));
   if (M->top_smem > 48 * 1024)
     CS_CU(g_drv.funcSetAttribute(M->f_top, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, (int)M->top_smem));
+  if (M->babd_cta_smem > (size_t)smem_optin) M->babd_cta_smem = 0;  // per-level kernels only
+  else if (M->babd_cta_smem > 48 * 1024)
+    CS_CU(g_drv.funcSetAttribute(M->f_babd_cta, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, (int)M->babd_cta_smem));
   {
     // resident CTAs of the condensation kernel per SM, for its persistent grid
     int smem_sm2 = 0;
@@ -686,6 +692,16 @@ static int tree_levels(const cs_batch* bt) {
   return L;
 }
 
+// One CTA per instance for the whole Newton direction (one launch), unless a
+// few large instances would leave the GPU idle: then one launch per tree
+// level across the instances.
+static bool use_cta_path(const cs_batch* bt) {
+  if (bt->M->babd_cta_smem == 0) return false;
+  int mx = 0;
+  for (int n : bt->hN) mx = std::max(mx, n);
+  return !(bt->B < 64 && mx > 4096);
+}
+
 static int run_lists(cs_batch* bt, CsBatchDev& v, int mode, int nlvl) {
   void* args[] = {&v, &mode, &nlvl};
   return launch(bt, bt->M->f_lists, 1, 1024, 0, args);
@@ -695,6 +711,10 @@ static int run_lists(cs_batch* bt, CsBatchDev& v, int mode, int nlvl) {
 // system, back substitution down, stage recovery.
 static int run_direction(cs_batch* bt, CsBatchDev& v, int nlvl) {
   cs_module* M = bt->M;
+  if (use_cta_path(bt)) {
+    void* a[] = {&v};
+    return launch_k(bt, M->f_babd_cta, (unsigned)(M->sms * 2), 256, M->babd_cta_smem, a, 1);
+  }
   const unsigned g = (unsigned)(M->sms * 8);
   for (int l = 0; l < nlvl; ++l) {
     void* a[] = {&v, &l};
@@ -929,7 +949,7 @@ static int super_step(cs_batch* bt, const CsConsts& c, int nlvl) {
   CsConsts cc = c;
   void* dargs[] = {&v, &cc};
   CS_TRY(run_insts(bt, M->f_decide, dargs));
-  CS_TRY(run_lists(bt, v, 1, nlvl));
+  CS_TRY(run_lists(bt, v, 1, use_cta_path(bt) ? 0 : nlvl));
   {
     void* args[] = {&v};
     CS_TRY(launch(bt, M->f_accept, g, 256, 0, args));
@@ -1049,7 +1069,7 @@ extern "C" int cs_solve(cs_batch* bt, const cs_opts* opts) {
         if (use_graph) {
           cudaError_t e = cudaGraphLaunch(bt->graph, bt->stream);
           if (e != cudaSuccess) rc = set_err(CS_ERR_CUDA, std::string("graph launch: ") + cudaGetErrorString(e));
-          bt->launches += 9 + 2 * nlvl;
+          bt->launches += use_cta_path(bt) ? 6 : 9 + 2 * nlvl;
           bt->super_steps += 1;
         } else {
           rc = super_step(bt, c, nlvl);
@@ -1235,7 +1255,7 @@ extern "C" int cs_stage_newton_direction(cs_batch* bt, double alpha, double* row
   CS_TRY(set_all_status(bt, ST_FRESH, alpha, 1));
   CsBatchDev v = devview(bt);
   const int nlvl = tree_levels(bt);
-  CS_TRY(run_lists(bt, v, 1, nlvl));
+  CS_TRY(run_lists(bt, v, 1, use_cta_path(bt) ? 0 : nlvl));
   CS_TRY(run_condense(bt, v));
   const size_t d = sizeof(double);
   cudaStream_t st = bt->stream;
