@@ -45,6 +45,7 @@ PKG = "collocation-solver-cuda_gb300"
 METRIC = "solves/sec to 1e-6 residual: NN-warm-started batched vs plain GPU, same GB300"
 BATCH = 4096
 SEED = 1
+BABD_PATH = [0]
 
 
 def _pkg():
@@ -170,7 +171,7 @@ class Workload:
             bt.set_guess_packed(host["N"].array, host["t"].array, host["y"].array, host["z"].array,
                                 host["p"].array, host["th"].array)
             self.groups.append(dict(m=m, insts=insts, cp=cp, bt=bt, host=host, out=out))
-        self.opts = cs.default_opts(self.problem, max_nodes=20000)
+        self.opts = cs.default_opts(self.problem, max_nodes=20000, babd_path=BABD_PATH[0])
         self.n = len(instances)
 
     def _run_groups(self, fn):
@@ -366,7 +367,7 @@ def run_warm(args, cs, rank, world, local_rank, cpu, cfg):
     ws = cs.warmstart
     fp64_peak = cs.module.measure_fp64_peak()
     fam = ws.vdp_family()
-    solver = ws.BatchSolver(fam)
+    solver = ws.BatchSolver(fam, cs.default_opts(fam.problem, max_nodes=20000, babd_path=args.babd_path))
     # ---- set-up: training data from the batched solver, then training
     t0 = time.perf_counter()
     train = cs.workloads.vdp_batch(args.train, seed=1000 + 100 * rank, n_range=(32, 256))
@@ -539,9 +540,11 @@ def main():
     ap.add_argument("--epochs", type=int, default=150)
     ap.add_argument("--single-sample", type=int, default=64)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--babd-path", type=int, default=0, help="0 automatic, 1 one CTA per instance, 2 per level")
     ap.add_argument("--profile-case", action="store_true",
                     help="small case for ncu: 512 instances, one full-batch condensation per m group, one solve")
     args = ap.parse_args()
+    BABD_PATH[0] = args.babd_path
     if args.profile_case:
         cs = _pkg()
         cs.build.build_library()

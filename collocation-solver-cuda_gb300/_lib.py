@@ -29,7 +29,7 @@ class Opts(ctypes.Structure):
     _fields_ = [("tol", ctypes.c_double), ("max_iter", ctypes.c_int), ("max_mesh", ctypes.c_int),
                 ("max_nodes", ctypes.c_int), ("min_nodes", ctypes.c_int), ("max_linesearch", ctypes.c_int),
                 ("alpha0", ctypes.c_double), ("alpha_m", ctypes.c_double), ("beta", ctypes.c_double),
-                ("check_every", ctypes.c_int)]
+                ("check_every", ctypes.c_int), ("babd_path", ctypes.c_int)]
 
 
 class Stats(ctypes.Structure):

@@ -472,6 +472,7 @@ extern "C" void cs_opts_default(cs_opts* o) {
   o->alpha_m = 0.1;
   o->beta = 0.9;
   o->check_every = 4;
+  o->babd_path = 0;
 }
 
 // =============================================================== batch ===
@@ -697,6 +698,8 @@ static int tree_levels(const cs_batch* bt) {
 // level across the instances.
 static bool use_cta_path(const cs_batch* bt) {
   if (bt->M->babd_cta_smem == 0) return false;
+  if (bt->opts.babd_path == 1) return true;
+  if (bt->opts.babd_path == 2) return false;
   int mx = 0;
   for (int n : bt->hN) mx = std::max(mx, n);
   return !(bt->B < 64 && mx > 4096);

@@ -82,6 +82,8 @@ typedef struct cs_opts {
   double alpha_m;        /* final continuation parameter (0.1, or 1e-6 with inequalities) */
   double beta;           /* continuation factor */
   int check_every;       /* Newton super-steps between host checks for completion */
+  int babd_path;         /* Newton direction kernels: 0 automatic, 1 one CTA per instance,
+                            2 one launch per tree level across the instances */
 } cs_opts;
 
 void cs_opts_default(cs_opts* o);
