@@ -693,16 +693,17 @@ static int tree_levels(const cs_batch* bt) {
   return L;
 }
 
-// One CTA per instance for the whole Newton direction (one launch), unless a
-// few large instances would leave the GPU idle: then one launch per tree
-// level across the instances.
+// Newton direction: one launch per tree level across the instances (spreads
+// every level over all SMs; measured faster for batches, also for their
+// stragglers), or one CTA per instance for the whole direction (one launch
+// per super-step; for a few small instances, where launches dominate).
 static bool use_cta_path(const cs_batch* bt) {
   if (bt->M->babd_cta_smem == 0) return false;
   if (bt->opts.babd_path == 1) return true;
   if (bt->opts.babd_path == 2) return false;
   int mx = 0;
   for (int n : bt->hN) mx = std::max(mx, n);
-  return !(bt->B < 64 && mx > 4096);
+  return bt->B <= 8 && mx <= 1024;
 }
 
 static int run_lists(cs_batch* bt, CsBatchDev& v, int mode, int nlvl) {

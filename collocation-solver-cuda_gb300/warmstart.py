@@ -269,6 +269,17 @@ class WarmRunner:
             if warm:
                 bt.warm_start(self.dY.ptr + 4 * g["first"] * self.mlp.n_out, N_NODES, self.mlp.n_out)
             bt.solve(self.solver.opts)
+            g["sols"] = bt.solution()
+            g["fallback"] = []
+            if warm and fallback:
+                # this group's failed instances again from the plain guess,
+                # overlapping with the other groups' solves
+                failed = [k for k, s in enumerate(g["sols"]) if not s["success"]]
+                if failed:
+                    plain = self.solver.solve([self.instances[g["first"] + k] for k in failed])
+                    for k, s in zip(failed, plain):
+                        g["sols"][k] = dict(s, fallback=True)
+                    g["fallback"] = failed
 
         if threads:
             ths = [threading.Thread(target=one, args=(g,)) for g in self.groups]
@@ -281,17 +292,10 @@ class WarmRunner:
                 one(g)
         t2 = time.perf_counter()
         sols = []
-        for g in self.groups:
-            sols += g["bt"].solution()
-        failed = [k for k, s in enumerate(sols) if not s["success"]]
         n_fb = 0
-        t3 = time.perf_counter()
-        if warm and fallback and failed:
-            plain = self.solver.solve([self.instances[k] for k in failed])
-            for k, s in zip(failed, plain):
-                sols[k] = dict(s, fallback=True)
-            n_fb = len(failed)
-        t4 = time.perf_counter()
-        self.times = {"predict_s": t1 - t0, "solve_s": t2 - t1, "collect_s": t3 - t2, "fallback_s": t4 - t3}
+        for g in self.groups:
+            sols += g["sols"]
+            n_fb += len(g["fallback"])
+        self.times = {"predict_s": t1 - t0, "solve_and_fallback_s": t2 - t1}
         solved = sum(int(s["success"]) for s in sols)
         return solved, n_fb, sols
