@@ -22,7 +22,8 @@ class ModuleDesc(ctypes.Structure):
     _fields_ = [("problem_src", ctypes.c_char_p), ("ny", ctypes.c_int), ("nz", ctypes.c_int), ("np", ctypes.c_int),
                 ("np_eff", ctypes.c_int), ("n_theta", ctypes.c_int), ("m", ctypes.c_int),
                 ("lobatto_A", _dp), ("lobatto_b", _dp), ("lobatto_c", _dp), ("gauss_w", _dp), ("gauss_L", _dp),
-                ("gauss_I", _dp), ("L0", _dp), ("L1", _dp), ("cache_dir", ctypes.c_char_p)]
+                ("gauss_I", _dp), ("L0", _dp), ("L1", _dp), ("cache_dir", ctypes.c_char_p),
+                ("layout", ctypes.c_int)]
 
 
 class Opts(ctypes.Structure):

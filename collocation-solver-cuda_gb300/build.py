@@ -65,16 +65,16 @@ def build_library(force=False, verbose=False):
     return LIB
 
 
-def check_kernels(problem_name="vdp", m=4, verbose=False):
+def check_kernels(problem_name="vdp", m=4, verbose=False, big=False):
     """nvcc-compile the kernel program for one problem to a cubin and return
-    the -Xptxas -v report."""
+    the -Xptxas -v report (big: the large-system kernels)."""
     from . import module as _module  # noqa: F401  (package import)
     from .module import kernel_program_text
     from .ocp import Problem
     pr = Problem.from_file(os.path.join(HERE, "problems", problem_name + ".ocp"))
-    text = kernel_program_text(pr, m)
+    text = kernel_program_text(pr, m, big=big)
     os.makedirs(BUILD, exist_ok=True)
-    cu = os.path.join(BUILD, "check_%s_m%d.cu" % (problem_name, m))
+    cu = os.path.join(BUILD, "check_%s_m%d%s.cu" % (problem_name, m, "_big" if big else ""))
     with open(cu, "w") as f:
         f.write(text)
     cmd = [NVCC, "-cubin", "-O3", "-std=c++17", "-lineinfo", "-arch=sm_103a", "-Xptxas", "-v", cu,

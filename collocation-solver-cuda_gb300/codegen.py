@@ -159,6 +159,22 @@ def _cuda_body(exprs, targets, pr):
     return lines
 
 
+def _cuda_matrix(flat, name, pr):
+    """Assignments of a flattened derivative matrix.  Large, mostly
+    structurally zero matrices (pendulum chains: Df, Dr of thousands of
+    entries, a few percent nonzero) are cleared by a loop and only their
+    nonzeros assigned, which keeps the generated code, and its compile time,
+    proportional to the nonzeros."""
+    n = len(flat)
+    nz = [k for k, e in enumerate(flat) if e != 0]
+    if n > 256 and len(nz) < n // 2:
+        lines = ["  for (int cs_k = 0; cs_k < %d; ++cs_k) %s[cs_k] = 0.0;" % (n, name)]
+        if nz:
+            lines += _cuda_body([flat[k] for k in nz], ["%s[%d]" % (name, k) for k in nz], pr)
+        return lines
+    return _cuda_body(flat, ["%s[%d]" % (name, k) for k in range(n)], pr) if flat else []
+
+
 def cuda_problem_source(pc):
     """CUDA C text for the six problem functions of ProblemCode `pc`."""
     pr = _CudaPrinter()
@@ -177,20 +193,17 @@ def cuda_problem_source(pc):
     out += _cuda_body(pc.g, ["g[%d]" % i for i in range(nz)], pr) if nz else []
     out.append("}")
     out.append("%s cs_Df(%s, double* __restrict__ Df) {" % (A, sig_pt))
-    flat = [e for row in pc.Df for e in row]
-    out += _cuda_body(flat, ["Df[%d]" % k for k in range(len(flat))], pr) if flat else []
+    out += _cuda_matrix([e for row in pc.Df for e in row], "Df", pr)
     out.append("}")
     out.append("%s cs_Dg(%s, const double cs_alpha, double* __restrict__ Dg) {" % (A, sig_pt))
     out.append("  (void)cs_alpha;")
-    flat = [e for row in pc.Dg for e in row]
-    out += _cuda_body(flat, ["Dg[%d]" % k for k in range(len(flat))], pr) if flat else []
+    out += _cuda_matrix([e for row in pc.Dg for e in row], "Dg", pr)
     out.append("}")
     out.append("%s cs_r(%s, double* __restrict__ r) {" % (A, sig_bc))
     out += _cuda_body(pc.r, ["r[%d]" % i for i in range(len(pc.r))], pr)
     out.append("}")
     out.append("%s cs_Dr(%s, double* __restrict__ Dr) {" % (A, sig_bc))
-    flat = [e for row in pc.Dr for e in row]
-    out += _cuda_body(flat, ["Dr[%d]" % k for k in range(len(flat))], pr)
+    out += _cuda_matrix([e for row in pc.Dr for e in row], "Dr", pr)
     out.append("}")
     return "\n".join(out) + "\n"
 

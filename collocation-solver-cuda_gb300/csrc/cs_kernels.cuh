@@ -113,7 +113,18 @@ struct CsBatch {
   long long* acc_pre;       // [B+1] prefix of node counts
   long long* lvl_pre;       // [CS_MAXLVL][B+1] prefix of tree items per level over jac
   int* nlist;               // [4] nact, njac, nacc, -
+  // large stage systems (CS_BIG): a slab of global memory per CTA
+  double* wsp;              // [wsp_ctas][wsp_stride]
+  long long wsp_stride;     // doubles per CTA
+  int wsp_ctas, wsp_pad;
 };
+
+#ifndef CS_BIG
+#define CS_BIG 0
+#endif
+#ifndef CS_SMEM_MAX
+#define CS_SMEM_MAX 232448
+#endif
 
 #define CS_MAXLVL 32
 
@@ -754,6 +765,7 @@ __device__ void cs_condense_group(const CsBatch& bt, int slot, bool active, doub
   if (singular && tid == 0) atomicAdd(&bt.inst[b].singular, 1);
 }
 
+#if !CS_BIG
 // lanes per condensation group, from the size of the stage system
 #define CS_CGL ((CS_S1 > 48) ? 256 : ((CS_S1 > 16) ? 16 : 8))
 
@@ -793,6 +805,7 @@ __device__ __forceinline__ void cs_condense_entry(const CsBatch& bt) {
 }
 
 extern "C" __global__ void k_condense(CsBatch bt) { cs_condense_entry(bt); }
+#endif  // !CS_BIG
 
 // ------------------------------------------------------------------------
 // BABD solve, one CTA per instance: tree of pairwise QR eliminations over
@@ -986,6 +999,7 @@ __device__ void cs_backsub_warp(const double* rec, const double* yl, const doubl
   __syncwarp();
 }
 
+#if !CS_BIG
 // One tree level for every instance that needs a Newton direction: warp per
 // item; item mi < merges eliminates node (2 mi + 1) 2^l between rows 2 mi and
 // 2 mi + 1, the last item of an odd level carries its row up unchanged.
@@ -1147,6 +1161,7 @@ extern "C" __global__ void k_top(CsBatch bt) {
   const int njac = bt.nlist[1];
   for (int k = blockIdx.x * wpc + w; k < njac; k += gridDim.x * wpc) cs_top_warp(bt, bt.jac[k], top);
 }
+#endif  // !CS_BIG
 
 // Back substitution of one tree level (top-down), warp per merge.
 extern "C" __global__ void k_backsub_level(CsBatch bt, int l) {
@@ -1219,6 +1234,7 @@ extern "C" __global__ void k_recover(CsBatch bt) {
   }
 }
 
+#if !CS_BIG
 // The whole Newton direction of one instance in one CTA: tree levels up,
 // top system, back substitution down, stage recovery, then the line search
 // starts (alpha = 1).  One launch per super-step instead of 2 L + 3, which is
@@ -1310,6 +1326,561 @@ extern "C" __global__ void __launch_bounds__(256) k_babd_cta(CsBatch bt) {
     __syncthreads();
   }
 }
+
+#else
+// not used for large stage systems (the host never launches it)
+extern "C" __global__ void k_babd_cta(CsBatch bt) {}
+#endif  // !CS_BIG
+
+#if CS_BIG
+// ========================================================================
+// Large stage systems (pendulum chains of K >= 16: s = m (ny + nz) in the
+// hundreds, blocks of ny = 64 .. 128).  The matrices no longer fit in shared
+// memory, so each CTA owns a slab of global memory (bt.wsp; L2 resident) and
+// the kernels below replace k_condense, k_tree_level and k_top:
+//   k_condense    one CTA per interval, right-looking blocked LU of the
+//                 augmented system [W11 | R1] with panels of CS_NB columns in
+//                 shared memory.  Same operations in the same order as the
+//                 unblocked elimination of cs_condense_group (pivot rule,
+//                 multipliers, the fma chain of every entry), so both give
+//                 the same bits.
+//   k_tree_level  one CTA per merge, a warp per column of the Householder
+//                 updates (lanes over rows).
+//   k_top         one CTA per instance.
+#define CS_NB 16
+#define CS_LDG (((CS_NCOL1 + 3) / 4) * 4)   // row stride of the slab matrix
+#define CS_PLD (CS_NB + 1)                  // row stride of the panel (shared)
+// slab: W [S1][LDG] | stage Jacobians [M][RB][NFG] | X0 [RB][NRHS]
+#define CS_WS_COND ((long long)CS_S1 * CS_LDG + (long long)CS_M * CS_RB * CS_NFG + (long long)CS_RB * CS_NRHS)
+// shared: panel [S1][PLD] | U12 [NB][LDG] | fa [M RB] | hA [M M] | fb [NY] | inv [S1] | red [16] | piv [NB]
+#define CS_SM_COND (CS_S1 * CS_PLD + CS_NB * CS_LDG + CS_M * CS_RB + CS_M * CS_M + CS_NY + CS_S1 + 16 + CS_NB)
+// merge matrix and top system: in shared memory when they fit, else in the slab
+#define CS_QSZ (CS_QLD * CS_QC)
+#define CS_TSZ (CS_TLD * (CS_NT + 1))
+#define CS_DRSZ ((CS_NY + CS_NP) * (2 * CS_NY + CS_NP))
+#define CS_Q_SMEM (((long long)CS_QSZ + 32) * 8 <= CS_SMEM_MAX)
+#define CS_T_SMEM (((long long)CS_TSZ + 32) * 8 <= CS_SMEM_MAX)
+#define CS_WS_TREE (CS_Q_SMEM ? 0ll : (long long)CS_QSZ)
+#define CS_WS_TOP ((CS_T_SMEM ? 0ll : (long long)CS_TSZ) + (long long)CS_DRSZ)
+#define CS_SM_TREE ((CS_Q_SMEM ? CS_QSZ : 0) + 32)
+#define CS_SM_TOP ((CS_T_SMEM ? CS_TSZ : 0) + 32)
+
+__device__ __forceinline__ unsigned cs_dyn_smem_bytes() {
+  unsigned r;
+  asm volatile("mov.u32 %0, %%dynamic_smem_size;" : "=r"(r));
+  return r;
+}
+
+// the launch gives this CTA a slab of at least `slab` doubles and `sm`
+// doubles of shared memory; otherwise count a configuration error and do
+// nothing (the host reports it)
+__device__ __forceinline__ bool cs_big_ok(const CsBatch& bt, long long slab, long long sm) {
+  const bool ok = blockDim.x <= 256 && (blockDim.x & 31) == 0 && (long long)cs_dyn_smem_bytes() >= sm * 8 &&
+                  (slab == 0 || (bt.wsp != nullptr && (int)blockIdx.x < bt.wsp_ctas && bt.wsp_stride >= slab));
+  if (!ok && threadIdx.x == 0) atomicAdd(&bt.counters[7], 1ull);
+  return ok;
+}
+
+// largest key over the CTA, the smallest row on ties (red: 16 doubles)
+__device__ __forceinline__ void cs_cta_argmax(unsigned long long& best, int& brow, double* red) {
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long ob = __shfl_xor_sync(0xffffffffu, best, o);
+    const int orow = __shfl_xor_sync(0xffffffffu, brow, o);
+    if (ob > best || (ob == best && orow < brow)) { best = ob; brow = orow; }
+  }
+  const int nw = blockDim.x >> 5;
+  if ((threadIdx.x & 31) == 0) {
+    red[threadIdx.x >> 5] = __longlong_as_double((long long)best);
+    red[8 + (threadIdx.x >> 5)] = (double)brow;
+  }
+  __syncthreads();
+  best = (unsigned long long)__double_as_longlong(red[0]);
+  brow = (int)red[8];
+  for (int w = 1; w < nw; ++w) {
+    const unsigned long long ob = (unsigned long long)__double_as_longlong(red[w]);
+    const int orow = (int)red[8 + w];
+    if (ob > best || (ob == best && orow < brow)) { best = ob; brow = orow; }
+  }
+  __syncthreads();
+}
+
+// sum over the CTA; every thread gets the same value (red: 8 doubles)
+__device__ __forceinline__ double cs_cta_sum(double v, double* red) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  double s = 0.0;
+  for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += red[w];
+  __syncthreads();
+  return s;
+}
+
+// stage j: f, g at the stage point into fa, their Jacobians into the slab
+// (not inlined: the big problem functions keep their registers to
+// themselves, away from the elimination loops)
+__device__ __noinline__ void cs_stage_big(const CsBatch& bt, int slot, int b, int j, double h, double* JG, double* fa) {
+  constexpr int RB = CS_RB;
+  const double* th = bt.th + (size_t)b * (CS_NTH > 0 ? CS_NTH : 1);
+  const double* yi = bt.y + (size_t)slot * CS_NY;
+  const double* yd = bt.ydot + (size_t)slot * CS_M * CS_NY;
+  double pl[CS_NP > 0 ? CS_NP : 1];
+  for (int k = 0; k < CS_NP; ++k) pl[k] = bt.p[(size_t)b * CS_NP + k];
+  double yt[CS_NY], zl[CS_NZ > 0 ? CS_NZ : 1], f[CS_NY];
+  for (int k = 0; k < CS_NY; ++k) {
+    double s = 0.0;
+    for (int q = 0; q < CS_M; ++q) s += CS_A[j * CS_M + q] * yd[q * CS_NY + k];
+    yt[k] = yi[k] + h * s;
+  }
+  for (int k = 0; k < CS_NZ; ++k) zl[k] = bt.zt[((size_t)slot * CS_M + j) * CS_NZ + k];
+  double* Jj = JG + (size_t)j * RB * CS_NFG;
+  cs_f(yt, zl, pl, th, f);
+  cs_Df(yt, zl, pl, th, Jj);
+  for (int a = 0; a < CS_NY; ++a) fa[j * RB + a] = f[a] - yd[j * CS_NY + a];
+#if CS_NZ > 0
+  double g[CS_NZ];
+  cs_g(yt, zl, pl, th, bt.inst[b].alpha, g);
+  cs_Dg(yt, zl, pl, th, bt.inst[b].alpha, Jj + (size_t)CS_NY * CS_NFG);
+  for (int a = 0; a < CS_NZ; ++a) fa[j * RB + CS_NY + a] = g[a];
+#endif
+}
+
+__device__ void cs_condense_big(const CsBatch& bt, int slot, double* slab, double* sm) {
+  constexpr int RB = CS_RB;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  double* W = slab;                                   // [S1][LDG]
+  double* JG = slab + (size_t)CS_S1 * CS_LDG;         // [M][RB][NFG]: Df rows, then Dg rows
+  double* X0 = JG + (size_t)CS_M * RB * CS_NFG;       // [RB][NRHS]
+  double* P = sm;                                     // [S1][PLD]
+  double* U = P + CS_S1 * CS_PLD;                     // [NB][LDG], columns relative to the panel's end
+  double* fa = U + CS_NB * CS_LDG;
+  double* hA = fa + CS_M * RB;
+  double* fb = hA + CS_M * CS_M;
+  double* inv = fb + CS_NY;
+  double* red = inv + CS_S1;
+  int* piv = (int*)(red + 16);
+  const int b = bt.inst_of[slot];
+  const double h = bt.t[slot + 1] - bt.t[slot];
+  const double* yi = bt.y + (size_t)slot * CS_NY;
+  const double* yd = bt.ydot + (size_t)slot * CS_M * CS_NY;
+  // ---- stage functions and Jacobians, thread j for stage j
+  for (int j = tid; j < CS_M; j += nt) cs_stage_big(bt, slot, b, j, h, JG, fa);
+  for (int e = tid; e < CS_M * CS_M; e += nt) hA[e] = h * CS_A[e];
+  for (int k = tid; k < CS_NY; k += nt) {
+    double s = 0.0;
+    for (int j = 0; j < CS_M; ++j) s += CS_B[j] * yd[j * CS_NY + k];
+    fb[k] = yi[CS_NY + k] - yi[k] - h * s;
+  }
+  __syncthreads();
+  // ---- stage 0: [-I h_z0; 0 g_z0] X0 = R0, one thread per right-hand side
+  for (int c = tid; c < CS_NRHS; c += nt) {
+    const double* J0 = JG;
+#if CS_NZ > 0
+    double gz[CS_NZ][CS_NZ], xz[CS_NZ];
+    for (int a = 0; a < CS_NZ; ++a) {
+      for (int q = 0; q < CS_NZ; ++q) gz[a][q] = J0[(CS_NY + a) * CS_NFG + CS_NY + q];
+      xz[a] = cs_rhs(J0 + (CS_NY + a) * CS_NFG, fa, 0, CS_NY + a, c);
+    }
+    for (int kk = 0; kk < CS_NZ; ++kk) {
+      int pr = kk;
+      for (int r = kk + 1; r < CS_NZ; ++r)
+        if (cs_abskey(gz[r][kk]) > cs_abskey(gz[pr][kk])) pr = r;
+      if (pr != kk) {
+        for (int q = 0; q < CS_NZ; ++q) { const double t = gz[kk][q]; gz[kk][q] = gz[pr][q]; gz[pr][q] = t; }
+        const double t = xz[kk]; xz[kk] = xz[pr]; xz[pr] = t;
+      }
+      const double ip = 1.0 / gz[kk][kk];
+      for (int r = kk + 1; r < CS_NZ; ++r) {
+        const double l = gz[r][kk] * ip;
+        for (int q = kk + 1; q < CS_NZ; ++q) gz[r][q] = fma(-l, gz[kk][q], gz[r][q]);
+        xz[r] = fma(-l, xz[kk], xz[r]);
+      }
+    }
+    for (int r = CS_NZ - 1; r >= 0; --r) {
+      double v = xz[r];
+      for (int q = r + 1; q < CS_NZ; ++q) v = fma(-gz[r][q], xz[q], v);
+      xz[r] = v / gz[r][r];
+    }
+    for (int a = 0; a < CS_NZ; ++a) X0[(CS_NY + a) * CS_NRHS + c] = xz[a];
+#endif
+    for (int a = 0; a < CS_NY; ++a) {
+      double v = -cs_rhs(J0 + a * CS_NFG, fa, 0, a, c);
+#if CS_NZ > 0
+      for (int q = 0; q < CS_NZ; ++q) v = fma(J0[a * CS_NFG + CS_NY + q], xz[q], v);
+#endif
+      X0[a * CS_NRHS + c] = v;
+    }
+  }
+  __syncthreads();
+  // ---- the reduced system [W11 | R1 - W10 X0] (stages 1..M-1) into the slab
+  for (int e = tid; e < CS_S1 * CS_NCOL1; e += nt) {
+    const int row = e / CS_NCOL1, col = e - row * CS_NCOL1;
+    const int j = 1 + row / RB, a = row - (j - 1) * RB;
+    const double* J = JG + (size_t)(j * RB + a) * CS_NFG;
+    double v;
+    if (col < CS_S1) {
+      const int k = 1 + col / RB, q = col - (k - 1) * RB;
+      if (q < CS_NY) {
+        v = hA[j * CS_M + k] * J[q];
+        if (k == j && q == a) v -= 1.0;
+      } else {
+        v = (k == j) ? J[q] : 0.0;
+      }
+    } else {
+      const int c = col - CS_S1;
+      double w = 0.0;
+      for (int q = 0; q < CS_NY; ++q) w = fma(J[q], X0[q * CS_NRHS + c], w);
+      v = fma(-hA[j * CS_M], w, cs_rhs(J, fa, j, a, c));
+    }
+    W[(size_t)row * CS_LDG + col] = v;
+  }
+  __syncthreads();
+  // ---- blocked LU with partial pivoting
+  int singular = 0;
+#pragma unroll 1
+  for (int k0 = 0; k0 < CS_S1; k0 += CS_NB) {
+    const int kb = min(CS_NB, CS_S1 - k0);
+    const int pr = CS_S1 - k0;        // panel rows
+    for (int e = tid; e < pr * kb; e += nt) {
+      const int r = e / kb, c = e - r * kb;
+      P[r * CS_PLD + c] = W[(size_t)(k0 + r) * CS_LDG + k0 + c];
+    }
+    __syncthreads();
+#pragma unroll 1
+    for (int kk = 0; kk < kb; ++kk) {
+      unsigned long long best = 0ull;
+      int brow = CS_S1;  // larger than any row: loses every tie
+      for (int r = kk + tid; r < pr; r += nt) {
+        const unsigned long long v = cs_abskey(P[r * CS_PLD + kk]);
+        if (v > best || brow == CS_S1) { best = v; brow = r; }
+      }
+      cs_cta_argmax(best, brow, red);
+      if (tid == 0) piv[kk] = brow;
+      if (brow != kk)
+        for (int c = tid; c < kb; c += nt) {
+          const double tmp = P[kk * CS_PLD + c];
+          P[kk * CS_PLD + c] = P[brow * CS_PLD + c];
+          P[brow * CS_PLD + c] = tmp;
+        }
+      __syncthreads();
+      const double pv = P[kk * CS_PLD + kk];
+      const bool tiny = cs_abskey(pv) < 0x3ce4000000000000ull;  // |pv| < 10 * 2^-52
+      singular |= tiny;
+      const double ip = 1.0 / pv;
+      if (tid == 0) inv[k0 + kk] = ip;
+      const double mul = tiny ? 0.0 : ip;
+      for (int r = kk + 1 + tid; r < pr; r += nt) P[r * CS_PLD + kk] *= mul;
+      __syncthreads();
+      const int nc = kb - kk - 1;
+      if (nc > 0) {
+        const int ne = (pr - kk - 1) * nc;
+        for (int e = tid; e < ne; e += nt) {
+          const int rr = e / nc;
+          const int r = kk + 1 + rr, c = kk + 1 + (e - rr * nc);
+          P[r * CS_PLD + c] = fma(-P[r * CS_PLD + kk], P[kk * CS_PLD + c], P[r * CS_PLD + c]);
+        }
+      }
+      __syncthreads();
+    }
+    // panel rows 0..kb-1 (U11, multipliers below its diagonal) back to the slab
+    for (int e = tid; e < kb * kb; e += nt) {
+      const int r = e / kb, c = e - r * kb;
+      W[(size_t)(k0 + r) * CS_LDG + k0 + c] = P[r * CS_PLD + c];
+    }
+    // columns right of the panel: the row swaps in order, then U12 = L11^-1 A12
+    const int c0 = k0 + kb, ncol = CS_NCOL1 - c0;
+    for (int c = tid; c < ncol; c += nt) {
+      double* colp = W + c0 + c;
+      for (int kk = 0; kk < kb; ++kk) {
+        const int pr2 = piv[kk];
+        if (pr2 != kk) {
+          const double t0 = colp[(size_t)(k0 + kk) * CS_LDG];
+          colp[(size_t)(k0 + kk) * CS_LDG] = colp[(size_t)(k0 + pr2) * CS_LDG];
+          colp[(size_t)(k0 + pr2) * CS_LDG] = t0;
+        }
+      }
+      // column c of U12 in shared memory (this thread's own column)
+#pragma unroll 1
+      for (int i = 0; i < kb; ++i) {
+        double v = colp[(size_t)(k0 + i) * CS_LDG];
+        for (int l = 0; l < i; ++l) v = fma(-P[i * CS_PLD + l], U[l * CS_LDG + c], v);
+        colp[(size_t)(k0 + i) * CS_LDG] = v;
+        U[i * CS_LDG + c] = v;
+      }
+    }
+    __syncthreads();
+    // trailing update A22 -= L21 U12: warp items of 4 rows x 128 columns,
+    // lane owns columns lane + 32 q
+    const int r0 = k0 + kb, nr = CS_S1 - r0;
+    if (nr > 0 && ncol > 0) {
+      const int rt = (nr + 3) >> 2, ct = (ncol + 127) >> 7;
+      const int lane = tid & 31, w = tid >> 5, nw = nt >> 5;
+      for (int item = w; item < rt * ct; item += nw) {
+        const int ri = item / ct, ci = item - ri * ct;
+        const int ra = ri * 4, cb = ci * 128 + lane;
+        double acc[4][4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            const int r = ra + i, c = cb + 32 * q;
+            acc[i][q] = (r < nr && c < ncol) ? W[(size_t)(r0 + r) * CS_LDG + c0 + c] : 0.0;
+          }
+#pragma unroll 2
+        for (int l = 0; l < kb; ++l) {
+          double lv[4], uv[4];
+#pragma unroll
+          for (int i = 0; i < 4; ++i) lv[i] = (ra + i < nr) ? P[(kb + ra + i) * CS_PLD + l] : 0.0;
+#pragma unroll
+          for (int q = 0; q < 4; ++q) uv[q] = (cb + 32 * q < ncol) ? U[l * CS_LDG + cb + 32 * q] : 0.0;
+#pragma unroll
+          for (int i = 0; i < 4; ++i)
+#pragma unroll
+            for (int q = 0; q < 4; ++q) acc[i][q] = fma(-lv[i], uv[q], acc[i][q]);
+        }
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            const int r = ra + i, c = cb + 32 * q;
+            if (r < nr && c < ncol) W[(size_t)(r0 + r) * CS_LDG + c0 + c] = acc[i][q];
+          }
+      }
+    }
+    __syncthreads();
+  }
+  // ---- back substitution, blocks of CS_NB rows from the bottom; the
+  //      right-hand sides are columns S1.. of the slab rows
+#pragma unroll 1
+  for (int k0 = ((CS_S1 - 1) / CS_NB) * CS_NB; k0 >= 0; k0 -= CS_NB) {
+    const int kb = min(CS_NB, CS_S1 - k0);
+    // U column block [0, k0+kb) x [k0, k0+kb) into the panel buffer
+    for (int e = tid; e < (k0 + kb) * kb; e += nt) {
+      const int r = e / kb, c = e - r * kb;
+      P[r * CS_PLD + c] = W[(size_t)r * CS_LDG + k0 + c];
+    }
+    __syncthreads();
+    // diagonal block, one thread per right-hand side, rows from the bottom
+    for (int c = tid; c < CS_NRHS; c += nt) {
+      double* colp = W + CS_S1 + c;
+      for (int i = 0; i < kb; ++i) U[i * CS_LDG + c] = colp[(size_t)(k0 + i) * CS_LDG];
+#pragma unroll 1
+      for (int i = kb - 1; i >= 0; --i) {
+        const double xi = U[i * CS_LDG + c] * inv[k0 + i];
+        U[i * CS_LDG + c] = xi;
+        for (int q = 0; q < i; ++q) U[q * CS_LDG + c] = fma(-P[(k0 + q) * CS_PLD + i], xi, U[q * CS_LDG + c]);
+      }
+      for (int i = 0; i < kb; ++i) colp[(size_t)(k0 + i) * CS_LDG] = U[i * CS_LDG + c];
+    }
+    __syncthreads();
+    // rows above the block: B[q] -= U[q][k0 + i] x[i], i from the last
+    for (int e = tid; e < k0 * CS_NRHS; e += nt) {
+      const int q = e / CS_NRHS, c = e - q * CS_NRHS;
+      double v = W[(size_t)q * CS_LDG + CS_S1 + c];
+      for (int i = kb - 1; i >= 0; --i) v = fma(-P[q * CS_PLD + i], U[i * CS_LDG + c], v);
+      W[(size_t)q * CS_LDG + CS_S1 + c] = v;
+    }
+    __syncthreads();
+  }
+  // ---- X (column-major [NRHS][S]: stage-0 rows from X0, the others from W)
+  double* X = bt.X + (size_t)slot * CS_NRHS * CS_S;
+  for (int e = tid; e < CS_NRHS * CS_S; e += nt) {
+    const int c = e / CS_S, r = e - c * CS_S;
+    X[e] = (r < RB) ? X0[r * CS_NRHS + c] : W[(size_t)(r - RB) * CS_LDG + CS_S1 + c];
+  }
+  // ---- condensed block row: D X = h sum_j b_j X[(j, a)]
+  double* row = bt.rows0 + (size_t)slot * CS_ROWSZ;
+  for (int e = tid; e < CS_NRHS * CS_NY; e += nt) {
+    const int c = e / CS_NY, a = e - c * CS_NY;
+    double s = CS_B[0] * X0[a * CS_NRHS + c];
+    for (int j = 1; j < CS_M; ++j) s += CS_B[j] * W[(size_t)((j - 1) * RB + a) * CS_LDG + CS_S1 + c];
+    const double dx = h * s;
+    if (c < CS_NY) {
+      row[c * CS_NY + a] = (a == c) ? dx - 1.0 : dx;
+      row[(CS_NY + c) * CS_NY + a] = (a == c ? 1.0 : 0.0);
+    } else if (c < CS_NY + CS_NPE) {
+      row[(2 * CS_NY + (c - CS_NY)) * CS_NY + a] = dx;
+    } else {
+      row[(2 * CS_NY + CS_NPE) * CS_NY + a] = -fb[a] - dx;
+    }
+  }
+  singular = __syncthreads_or(singular);
+  if (singular && tid == 0) atomicAdd(&bt.inst[b].singular, 1);
+  __syncthreads();
+}
+
+extern "C" __global__ void __launch_bounds__(256, 2) k_condense(CsBatch bt) {
+  extern __shared__ double smem[];
+  if (!cs_big_ok(bt, CS_WS_COND, CS_SM_COND)) return;
+  double* slab = bt.wsp + (size_t)blockIdx.x * bt.wsp_stride;
+  const int njac = bt.nlist[1];
+  const long long total = bt.jac_pre[njac];
+  for (long long it = blockIdx.x; it < total; it += gridDim.x) {
+    const int k = cs_find(bt.jac_pre, njac, it);
+    const int b = bt.jac[k];
+    const int slot = bt.off[b] + (int)(it - bt.jac_pre[k]);
+    cs_condense_big(bt, slot, slab, smem);
+  }
+}
+
+// Householder column k of a column-major matrix A (leading dimension ld,
+// rows k..n-1) applied to columns k+1..nc-1, CTA-wide: a warp per column,
+// lanes over rows.  Sign rule and early skip as matrix_factorization_cuda.py:37-54.
+__device__ __forceinline__ void cs_householder_cta(double* A, int ld, int n, int nc, int k, double* red) {
+  const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, w = tid >> 5, nw = nt >> 5;
+  const double* vk = A + (size_t)k * ld;
+  double ss = 0.0;
+  for (int r = k + tid; r < n; r += nt) ss += vk[r] * vk[r];
+  ss = cs_cta_sum(ss, red);
+  const double x0 = vk[k];
+  const double sgn = (x0 >= 0.0) ? 1.0 : -1.0;
+  const double g = -sgn * sqrt(ss);
+  const double v0 = x0 - g;
+  const double vs = ss - x0 * x0 + v0 * v0;
+  if (vs < CS_EPS) return;  // uniform: nothing to eliminate in this column
+  const double beta = -2.0 / vs;
+  for (int c = k + 1 + w; c < nc; c += nw) {
+    double* col = A + (size_t)c * ld;
+    double wv = (lane == 0) ? v0 * col[k] : 0.0;
+    for (int r = k + 1 + lane; r < n; r += 32) wv = fma(vk[r], col[r], wv);
+    for (int o = 16; o > 0; o >>= 1) wv += __shfl_xor_sync(0xffffffffu, wv, o);
+    const double bw = beta * wv;
+    if (lane == 0) col[k] = fma(bw, v0, col[k]);
+    for (int r = k + 1 + lane; r < n; r += 32) col[r] = fma(bw, vk[r], col[r]);
+  }
+  __syncthreads();
+  double* ck = A + (size_t)k * ld;
+  if (tid == 0) ck[k] = g;
+  for (int r = k + 1 + tid; r < n; r += nt) ck[r] = 0.0;
+  __syncthreads();
+}
+
+// merge of block rows a and b, one CTA (layout as cs_merge_warp)
+__device__ void cs_merge_cta(const double* ra, const double* rb, double* out_row, double* rec, double* Q, double* red) {
+  const int tid = threadIdx.x, nt = blockDim.x;
+  for (int e = tid; e < CS_QC * CS_NY; e += nt) {
+    const int c = e / CS_NY, r = e - c * CS_NY;
+    double top, bot;
+    if (c < CS_NY) { top = ra[(CS_NY + c) * CS_NY + r]; bot = rb[c * CS_NY + r]; }
+    else if (c < 2 * CS_NY) { top = ra[(c - CS_NY) * CS_NY + r]; bot = 0.0; }
+    else if (c < 3 * CS_NY) { top = 0.0; bot = rb[(CS_NY + c - 2 * CS_NY) * CS_NY + r]; }
+    else if (c < 3 * CS_NY + CS_NPE) { top = ra[(2 * CS_NY + c - 3 * CS_NY) * CS_NY + r]; bot = rb[(2 * CS_NY + c - 3 * CS_NY) * CS_NY + r]; }
+    else { top = ra[(2 * CS_NY + CS_NPE) * CS_NY + r]; bot = rb[(2 * CS_NY + CS_NPE) * CS_NY + r]; }
+    Q[(size_t)c * CS_QLD + r] = top;
+    Q[(size_t)c * CS_QLD + CS_NY + r] = bot;
+  }
+  __syncthreads();
+#pragma unroll 1
+  for (int k = 0; k < CS_NY; ++k) cs_householder_cta(Q, CS_QLD, 2 * CS_NY, CS_QC, k, red);
+  for (int e = tid; e < CS_QC * CS_NY; e += nt) {
+    const int c = e / CS_NY, r = e - c * CS_NY;
+    rec[e] = Q[(size_t)c * CS_QLD + r];
+    if (c >= CS_NY) out_row[(size_t)(c - CS_NY) * CS_NY + r] = Q[(size_t)c * CS_QLD + CS_NY + r];
+  }
+  __syncthreads();
+}
+
+extern "C" __global__ void __launch_bounds__(256) k_tree_level(CsBatch bt, int l) {
+  extern __shared__ double smem[];
+  if (!cs_big_ok(bt, CS_WS_TREE, CS_SM_TREE)) return;
+  double* Q = CS_Q_SMEM ? smem : bt.wsp + (size_t)blockIdx.x * bt.wsp_stride;
+  double* red = CS_Q_SMEM ? smem + CS_QSZ : smem;
+  const int njac = bt.nlist[1];
+  const long long* pre = bt.lvl_pre + (size_t)l * (bt.B + 1);
+  const long long total = pre[njac];
+  const double* srcb = (l & 1) ? bt.rows1 : bt.rows0;
+  double* dstb = (l & 1) ? bt.rows0 : bt.rows1;
+  for (long long it = blockIdx.x; it < total; it += gridDim.x) {
+    const int k = cs_find(pre, njac, it);
+    const int b = bt.jac[k];
+    const int mi = (int)(it - pre[k]);
+    const int off = bt.off[b];
+    const int nl = cs_rows_at(bt.N[b] - 1, l);
+    const int merges = nl >> 1;
+    const double* src = srcb + (size_t)off * CS_ROWSZ;
+    double* dst = dstb + (size_t)off * CS_ROWSZ;
+    if (mi < merges) {
+      cs_merge_cta(src + (size_t)(2 * mi) * CS_ROWSZ, src + (size_t)(2 * mi + 1) * CS_ROWSZ, dst + (size_t)mi * CS_ROWSZ,
+                   bt.tree + (size_t)(off + ((2 * mi + 1) << l)) * CS_TREESZ, Q, red);
+    } else {
+      const double* sr = src + (size_t)(nl - 1) * CS_ROWSZ;
+      double* dr = dst + (size_t)merges * CS_ROWSZ;
+      for (int q = threadIdx.x; q < CS_ROWSZ; q += blockDim.x) dr[q] = sr[q];
+      __syncthreads();
+    }
+  }
+}
+
+// Top of the tree, one CTA per instance (as cs_top_warp; Dr goes to the slab).
+extern "C" __global__ void __launch_bounds__(256) k_top(CsBatch bt) {
+  extern __shared__ double smem[];
+  if (!cs_big_ok(bt, CS_WS_TOP, CS_SM_TOP)) return;
+  double* slab = bt.wsp + (size_t)blockIdx.x * bt.wsp_stride;
+  double* top = CS_T_SMEM ? smem : slab;
+  double* Dr = CS_T_SMEM ? slab : slab + CS_TSZ;
+  double* red = CS_T_SMEM ? smem + CS_TSZ : smem;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const int njac = bt.nlist[1];
+  for (int k = blockIdx.x; k < njac; k += gridDim.x) {
+    const int b = bt.jac[k];
+    const int N = bt.N[b], off = bt.off[b];
+    const int L = cs_levels(N - 1);
+    const double* row = ((L & 1) ? bt.rows1 : bt.rows0) + (size_t)off * CS_ROWSZ;
+    const double* th = bt.th + (size_t)b * (CS_NTH > 0 ? CS_NTH : 1);
+    if (tid == 0) {
+      double ya[CS_NY], yb[CS_NY], pl[CS_NP > 0 ? CS_NP : 1];
+      for (int q = 0; q < CS_NY; ++q) { ya[q] = bt.y[(size_t)off * CS_NY + q]; yb[q] = bt.y[(size_t)(off + N - 1) * CS_NY + q]; }
+      for (int q = 0; q < CS_NP; ++q) pl[q] = bt.p[(size_t)b * CS_NP + q];
+      double r[CS_NY + CS_NP];
+      cs_r(ya, yb, pl, th, r);
+      cs_Dr(ya, yb, pl, th, Dr);
+      for (int q = 0; q < CS_NY + CS_NP; ++q) top[(size_t)CS_NT * CS_TLD + CS_NY + q] = -r[q];
+    }
+    __syncthreads();
+    for (int e = tid; e < CS_NT * CS_NT; e += nt) {
+      const int c = e / CS_NT, r = e - c * CS_NT;
+      double v;
+      if (r < CS_NY) v = (c < 2 * CS_NY + CS_NPE) ? row[c * CS_NY + r] : 0.0;
+      else v = Dr[(r - CS_NY) * (2 * CS_NY + CS_NP) + c];
+      top[(size_t)c * CS_TLD + r] = v;
+    }
+    for (int r = tid; r < CS_NY; r += nt) top[(size_t)CS_NT * CS_TLD + r] = row[(2 * CS_NY + CS_NPE) * CS_NY + r];
+    __syncthreads();
+#pragma unroll 1
+    for (int kk = 0; kk < CS_NT; ++kk) cs_householder_cta(top, CS_TLD, CS_NT, CS_NT + 1, kk, red);
+    // back substitution, column-oriented
+    double* rhs = top + (size_t)CS_NT * CS_TLD;
+    bool sing = false;
+#pragma unroll 1
+    for (int r = CS_NT - 1; r >= 0; --r) {
+      const double d = top[(size_t)r * CS_TLD + r];
+      sing |= (d == 0.0);
+      const double xr = (d != 0.0) ? rhs[r] / d : 0.0;
+      __syncthreads();
+      if (tid == 0) rhs[r] = xr;
+      for (int q = tid; q < r; q += nt) rhs[q] = fma(-top[(size_t)r * CS_TLD + q], xr, rhs[q]);
+      __syncthreads();
+    }
+    if (tid == 0) {
+      if (sing) {
+        for (int r = 0; r < CS_NT; ++r) rhs[r] = 0.0;
+        bt.inst[b].singular += 1;
+      }
+    }
+    __syncthreads();
+    for (int q = tid; q < CS_NY; q += nt) {
+      bt.dy[(size_t)off * CS_NY + q] = rhs[q];
+      bt.dy[(size_t)(off + N - 1) * CS_NY + q] = rhs[CS_NY + q];
+    }
+    for (int q = tid; q < CS_NP; q += nt) bt.dp[(size_t)b * CS_NP + q] = rhs[2 * CS_NY + q];
+    if (tid == 0) {
+      bt.inst[b].status = ST_LS;
+      bt.inst[b].alpha_ls = 1.0;
+      bt.inst[b].ls_it = 0;
+    }
+    __syncthreads();
+  }
+}
+#endif
 
 // ------------------------------------------------------------------------
 // Segment residual at the M+1 Gauss points (residual_type 1, with the running

@@ -132,6 +132,9 @@ struct CsBatchDev {
   long long* acc_pre;
   long long* lvl_pre;
   int* nlist;
+  double* wsp;
+  long long wsp_stride;
+  int wsp_ctas, wsp_pad;
 };
 
 static const int CS_MAXLVL = 32;
@@ -263,13 +266,18 @@ struct cs_module {
   size_t top_smem;
   int sms = 1;
   int condense_grid = 1;
+  // large stage systems: kernels with a global-memory slab per CTA
+  bool big = false;
+  long long slab = 0;  // doubles per CTA
+  int big_ctas = 0;
 };
 
-static std::string build_source(const cs_module_desc* d) {
+static std::string build_source(const cs_module_desc* d, bool big, int smem_max) {
   std::ostringstream o;
   o << "// generated prelude\n";
   o << "#define CS_NY " << d->ny << "\n#define CS_NZ " << d->nz << "\n#define CS_NP " << d->np << "\n";
   o << "#define CS_NPE " << d->np_eff << "\n#define CS_NTH " << d->n_theta << "\n#define CS_M " << d->m << "\n";
+  if (big) o << "#define CS_BIG 1\n#define CS_SMEM_MAX " << smem_max << "\n";
   const int m = d->m;
   o << "__constant__ double CS_A[" << m * m << "] = {" << fmt_array(d->lobatto_A, m * m) << "};\n";
   o << "__constant__ double CS_B[" << m << "] = {" << fmt_array(d->lobatto_b, m) << "};\n";
@@ -354,15 +362,47 @@ extern "C" int cs_module_load(const cs_module_desc* d, cs_module** out) {
                      (size_t)rb * M->nrhs + s1 + 16;
   const size_t grp = (((raw + 7) / 16) * 16 + 8) * sizeof(double);
   const int gl = (s1 > 48) ? 256 : ((s1 > 16) ? 16 : 8);
-  if (grp > (size_t)smem_optin) {
+  // BABD tree: a merge matrix per warp (4 warps per CTA); top: one system per warp
+  const int qld = (2 * M->ny) | 1, qc = 3 * M->ny + M->npe + 1;
+  const int nt = 2 * M->ny + M->np, tld = nt | 1;
+  const size_t tree_small = (size_t)4 * qld * qc * sizeof(double);
+  const size_t top_per = (size_t)tld * (nt + 1) * sizeof(double);
+  const bool fits = grp <= (size_t)smem_optin && tree_small <= (size_t)smem_optin && top_per <= (size_t)smem_optin;
+  if (d->layout == 1 && !fits) {
     delete M;
     return set_err(CS_ERR_INVALID, "cs_module_load: stage system of size " + std::to_string(M->s) +
-                                       " does not fit in shared memory");
+                                       " does not fit in shared memory (layout 1)");
   }
+  M->big = d->layout == 2 || (d->layout == 0 && !fits);
   M->cgw = gl;
   int smem_sm = 0;
   CS_CUDA(cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev));
-  if (gl <= 32) {
+  CS_CUDA(cudaDeviceGetAttribute(&M->sms, cudaDevAttrMultiProcessorCount, dev));
+  if (M->big) {
+    // sizes of the large-system kernels (CS_NB .. CS_SM_TOP in cs_kernels.cuh;
+    // the kernels check what they get and report a mismatch)
+    const long long nb = 16, ncol1 = s1 + M->nrhs, ldg = ((ncol1 + 3) / 4) * 4, nfg = d->ny + d->nz + d->np;
+    const long long ws_cond = (long long)s1 * ldg + (long long)d->m * rb * nfg + (long long)rb * M->nrhs;
+    const long long sm_cond = (long long)s1 * (nb + 1) + nb * ldg + (long long)d->m * rb + d->m * d->m + d->ny + s1 + 16 + nb;
+    const long long qsz = (long long)qld * qc, tsz = (long long)tld * (nt + 1);
+    const long long drsz = (long long)(d->ny + d->np) * (2 * d->ny + d->np);
+    const bool q_smem = (qsz + 32) * 8 <= smem_optin, t_smem = (tsz + 32) * 8 <= smem_optin;
+    M->slab = std::max(ws_cond, std::max(q_smem ? 0ll : qsz, (t_smem ? 0ll : tsz) + drsz));
+    M->condense_smem = (size_t)sm_cond * 8;
+    M->tree_smem = (size_t)((q_smem ? qsz : 0) + 32) * 8;
+    M->top_smem = (size_t)((t_smem ? tsz : 0) + 32) * 8;
+    if (M->condense_smem > (size_t)smem_optin) {
+      delete M;
+      return set_err(CS_ERR_INVALID, "cs_module_load: stage system of size " + std::to_string(M->s) + " too large");
+    }
+    const int per_sm = std::max(1, std::min(8, (int)((size_t)smem_sm / (M->condense_smem + 1024))));
+    M->big_ctas = M->sms * per_sm;
+    M->condense_block = 256;
+    M->condense_per_cta = 1;
+    M->condense_grid = M->big_ctas;
+    M->top_wpc = 8;
+    M->babd_cta_smem = 0;
+  } else if (gl <= 32) {
     // warps per CTA that maximise resident groups per SM (shared memory bound)
     const int gpw = 32 / gl;
     int best_w = 1;
@@ -383,21 +423,14 @@ extern "C" int cs_module_load(const cs_module_desc* d, cs_module** out) {
     M->condense_block = gl;
     M->condense_smem = grp;
   }
-  // BABD tree: a merge matrix per warp (4 warps per CTA); top: one system per warp
-  const int qld = (2 * M->ny) | 1, qc = 3 * M->ny + M->npe + 1;
-  const int nt = 2 * M->ny + M->np, tld = nt | 1;
-  M->tree_smem = (size_t)4 * qld * qc * sizeof(double);
-  const size_t top_per = (size_t)tld * (nt + 1) * sizeof(double);
-  if (M->tree_smem > (size_t)smem_optin || top_per > (size_t)smem_optin) {
-    delete M;
-    return set_err(CS_ERR_INVALID, "cs_module_load: BABD blocks do not fit in shared memory");
+  if (!M->big) {
+    M->tree_smem = tree_small;
+    M->top_wpc = (int)std::max<size_t>(1, std::min<size_t>(4, (size_t)smem_optin / top_per));
+    M->babd_cta_smem = top_per + (size_t)8 * qld * qc * sizeof(double);
+    M->top_smem = top_per * M->top_wpc;
   }
-  M->top_wpc = (int)std::max<size_t>(1, std::min<size_t>(4, (size_t)smem_optin / top_per));
-  M->babd_cta_smem = top_per + (size_t)8 * qld * qc * sizeof(double);
-  M->top_smem = top_per * M->top_wpc;
-  CS_CUDA(cudaDeviceGetAttribute(&M->sms, cudaDevAttrMultiProcessorCount, dev));
 
-  std::string src = build_source(d);
+  std::string src = build_source(d, M->big, smem_optin);
   std::string cache = d->cache_dir ? d->cache_dir : "";
   if (cache.empty()) {
     const char* env = getenv("CS_GB300_CACHE");
@@ -442,7 +475,7 @@ extern "C" int cs_module_load(const cs_module_desc* d, cs_module** out) {
   if (M->babd_cta_smem > (size_t)smem_optin) M->babd_cta_smem = 0;  // per-level kernels only
   else if (M->babd_cta_smem > 48 * 1024)
     CS_CU(g_drv.funcSetAttribute(M->f_babd_cta, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, (int)M->babd_cta_smem));
-  {
+  if (!M->big) {
     // resident CTAs of the condensation kernel per SM, for its persistent grid
     int smem_sm2 = 0;
     CS_CUDA(cudaDeviceGetAttribute(&smem_sm2, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev));
@@ -495,6 +528,7 @@ struct cs_batch {
   DBuf t[2], y[2], ydot[2], zt[2], znode[2];
   int cur = 0;
   DBuf inst_of, dy, dydot, dzt, X, rows0, rows1, tree, res;
+  DBuf wsp;  // large stage systems: slab per CTA
   std::vector<int> hN, hoff;
   cs_opts opts;
   // work lists
@@ -623,6 +657,11 @@ static CsBatchDev devview(cs_batch* bt) {
   v.acc_pre = (long long*)bt->l_accp.p;
   v.lvl_pre = (long long*)bt->l_lvlp.p;
   v.nlist = (int*)bt->l_n.p;
+  if (bt->M->big) {
+    v.wsp = (double*)bt->wsp.p;
+    v.wsp_stride = bt->M->slab;
+    v.wsp_ctas = bt->M->big_ctas;
+  }
   return v;
 }
 
@@ -682,6 +721,17 @@ static int run_condense(cs_batch* bt, CsBatchDev& v) {
   return launch_k(bt, M->f_condense, (unsigned)M->condense_grid, M->condense_block, M->condense_smem, args, 0);
 }
 
+// large-system kernels count a launch that gave them too little shared
+// memory or slab in counters[7] and skip their work
+static int check_config(cs_batch* bt) {
+  if (!bt->M->big) return CS_OK;
+  unsigned long long c7 = 0;
+  CS_CUDA(cudaMemcpyAsync(&c7, (unsigned long long*)bt->dcounters.p + 7, sizeof(c7), cudaMemcpyDeviceToHost, bt->stream));
+  CS_CUDA(cudaStreamSynchronize(bt->stream));
+  if (c7 != 0) return set_err(CS_ERR_STATE, "large-system kernel launched without its shared memory or slab");
+  return CS_OK;
+}
+
 static int tree_levels(const cs_batch* bt) {
   int mx = 1;
   for (int n : bt->hN) mx = std::max(mx, n - 1);
@@ -722,11 +772,13 @@ static int run_direction(cs_batch* bt, CsBatchDev& v, int nlvl) {
   const unsigned g = (unsigned)(M->sms * 8);
   for (int l = 0; l < nlvl; ++l) {
     void* a[] = {&v, &l};
-    CS_TRY(launch_k(bt, M->f_tree_level, g, 128, M->tree_smem, a, 1));
+    if (M->big) CS_TRY(launch_k(bt, M->f_tree_level, (unsigned)M->big_ctas, 256, M->tree_smem, a, 1));
+    else CS_TRY(launch_k(bt, M->f_tree_level, g, 128, M->tree_smem, a, 1));
   }
   {
     void* a[] = {&v};
-    CS_TRY(launch_k(bt, M->f_top, (unsigned)(M->sms * 4), 32 * M->top_wpc, M->top_smem, a, 1));
+    if (M->big) CS_TRY(launch_k(bt, M->f_top, (unsigned)std::min(M->big_ctas, bt->B), 256, M->top_smem, a, 1));
+    else CS_TRY(launch_k(bt, M->f_top, (unsigned)(M->sms * 4), 32 * M->top_wpc, M->top_smem, a, 1));
   }
   for (int l = nlvl - 1; l >= 0; --l) {
     void* a[] = {&v, &l};
@@ -787,9 +839,15 @@ extern "C" int cs_batch_create(cs_module* M, int batch, long long node_capacity,
       (rc = dalloc(bt->l_accp, (batch + 1) * sizeof(long long))) ||
       (rc = dalloc(bt->l_lvlp, (size_t)CS_MAXLVL * (batch + 1) * sizeof(long long))) ||
       (rc = dalloc(bt->l_n, 4 * sizeof(int))) ||
-      (rc = alloc_slots(bt, std::max<long long>(node_capacity, 2 * batch), false))) {
+      (rc = alloc_slots(bt, std::max<long long>(node_capacity, 2 * batch), false)) ||
+      (M->big && (rc = dalloc(bt->wsp, (size_t)M->big_ctas * M->slab * d)))) {
     cs_batch_free(bt);
     return rc;
+  }
+  if (cudaMemsetAsync(bt->dcounters.p, 0, 64, bt->stream) != cudaSuccess ||
+      cudaStreamSynchronize(bt->stream) != cudaSuccess) {
+    cs_batch_free(bt);
+    return set_err(CS_ERR_CUDA, "cs_batch_create: counter reset failed");
   }
   *out = bt;
   return CS_OK;
@@ -801,7 +859,7 @@ extern "C" void cs_batch_free(cs_batch* bt) {
   DBuf* all[] = {&bt->dN, &bt->doff, &bt->doff2, &bt->dp, &bt->dth, &bt->ddp, &bt->dinst, &bt->dcounters,
                  &bt->inst_of, &bt->dy, &bt->dydot, &bt->dzt, &bt->X, &bt->rows0, &bt->rows1, &bt->tree, &bt->res,
                  &bt->iN, &bt->ioff, &bt->it, &bt->iy, &bt->iz, &bt->ip, &bt->l_act, &bt->l_jac, &bt->l_acc,
-                 &bt->l_actp, &bt->l_jacp, &bt->l_accp, &bt->l_lvlp, &bt->l_n};
+                 &bt->l_actp, &bt->l_jacp, &bt->l_accp, &bt->l_lvlp, &bt->l_n, &bt->wsp};
   for (DBuf* b : all) dfree(*b);
   if (bt->graph) cudaGraphExecDestroy(bt->graph);
   if (bt->h_n) cudaFreeHost(bt->h_n);
@@ -1128,6 +1186,7 @@ extern "C" int cs_solve(cs_batch* bt, const cs_opts* opts) {
     }
     if (!any_newton) break;
   }
+  if (rc == CS_OK) rc = check_config(bt);
   if (rc == CS_OK) CS_CUDA(cudaStreamSynchronize(bt->stream));
   return rc;
 }
@@ -1270,6 +1329,7 @@ extern "C" int cs_stage_newton_direction(cs_batch* bt, double alpha, double* row
   if (dzt && M->nz > 0) CS_CUDA(cudaMemcpyAsync(dzt, bt->dzt.p, (size_t)bt->T * M->m * M->nz * d, cudaMemcpyDeviceToHost, st));
   if (dp && M->np > 0) CS_CUDA(cudaMemcpyAsync(dp, bt->ddp.p, (size_t)bt->B * M->np * d, cudaMemcpyDeviceToHost, st));
   CS_CUDA(cudaStreamSynchronize(st));
+  CS_TRY(check_config(bt));
   return set_all_status(bt, ST_FRESH, alpha, 0);
 }
 
@@ -1323,6 +1383,7 @@ extern "C" int cs_time_condense(cs_batch* bt, int reps, double* ms) {
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   *ms = (double)t / reps;
+  CS_TRY(check_config(bt));
   return set_all_status(bt, ST_FRESH, bt->opts.alpha0, 0);
 }
 

@@ -30,9 +30,10 @@ def _tables(m):
                 L0=arr(st["L0"]), L1=arr(st["L1"]))
 
 
-def kernel_program_text(problem, m):
+def kernel_program_text(problem, m, big=False, smem_max=232448):
     """The NVRTC program for (problem, m) as one CUDA source (used for nvcc
-    compile checks; the library builds the same text at run time)."""
+    compile checks; the library builds the same text at run time).  big:
+    the large-system kernels."""
     pc = ProblemCode(problem.sym)
     t = _tables(m)
 
@@ -41,6 +42,8 @@ def kernel_program_text(problem, m):
 
     out = "#define CS_NY %d\n#define CS_NZ %d\n#define CS_NP %d\n#define CS_NPE %d\n#define CS_NTH %d\n#define CS_M %d\n" % (
         pc.ny, pc.nz, pc.np, pc.np_eff, pc.nth, m)
+    if big:
+        out += "#define CS_BIG 1\n#define CS_SMEM_MAX %d\n" % smem_max
     out += arr("CS_A", t["A"]) + arr("CS_B", t["b"]) + arr("CS_C", t["c"]) + arr("CS_GW", t["gw"])
     out += arr("CS_GL", t["gL"]) + arr("CS_GI", t["gI"]) + arr("CS_L0", t["L0"]) + arr("CS_L1", t["L1"])
     out += cuda_problem_source(pc)
@@ -49,9 +52,13 @@ def kernel_program_text(problem, m):
 
 
 class CompiledProblem:
-    """A problem compiled for the GPU with m collocation points."""
+    """A problem compiled for the GPU with m collocation points.
 
-    def __init__(self, problem, m, cache_dir=DEFAULT_CACHE):
+    layout: 0 automatic, 1 shared-memory kernels only, 2 the large-system
+    kernels (global-memory slab per CTA; chosen automatically when a stage
+    system or a BABD block does not fit in shared memory)."""
+
+    def __init__(self, problem, m, cache_dir=DEFAULT_CACHE, layout=0):
         lib = _lib.load()
         self.problem = problem
         self.m = m
@@ -70,6 +77,8 @@ class CompiledProblem:
         d.gauss_w, d.gauss_L, d.gauss_I = (_lib.dptr(self._t[k]) for k in ("gw", "gL", "gI"))
         d.L0, d.L1 = _lib.dptr(self._t["L0"]), _lib.dptr(self._t["L1"])
         d.cache_dir = self._cache if cache_dir else None
+        d.layout = int(layout)
+        self.layout = int(layout)
         h = ctypes.c_void_p()
         _lib.check(lib.cs_module_load(ctypes.byref(d), ctypes.byref(h)), "cs_module_load")
         self.handle = h

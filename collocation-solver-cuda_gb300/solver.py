@@ -29,10 +29,11 @@ def compiled(problem, m):
     return cp
 
 
-def solve_single(problem, m=4, T0=None, Y0=None, Z0=None, P0=None, theta=None, opts=None):
+def solve_single(problem, m=4, T0=None, Y0=None, Z0=None, P0=None, theta=None, opts=None, layout=0):
     """Solve one instance from its initial guess (defaults: the problem's
-    BvpDae T0/Y0/Z0/P0).  Returns the solution dict of Batch.solution()."""
-    cp = compiled(problem, m)
+    BvpDae T0/Y0/Z0/P0).  Returns the solution dict of Batch.solution().
+    layout: kernel layout of CompiledProblem (0 automatic)."""
+    cp = compiled(problem, m) if layout == 0 else CompiledProblem(problem, m, layout=layout)
     bt = Batch(cp, 1)
     t = np.asarray(problem.T0 if T0 is None else T0, dtype=np.float64)
     y = np.asarray(problem.Y0 if Y0 is None else Y0, dtype=np.float64)

@@ -63,6 +63,11 @@ typedef struct cs_module_desc {
   const double* L0;         /* m: L_k(0) */
   const double* L1;         /* m: L_k(1) */
   const char* cache_dir;    /* compiled-code cache directory, or NULL */
+  int layout;               /* 0: automatic; 1: stage systems and BABD blocks in
+                               shared memory (fails if they do not fit);
+                               2: large-system kernels (global-memory slab per
+                               CTA, blocked LU), chosen automatically when the
+                               blocks do not fit in shared memory */
 } cs_module_desc;
 
 /* Compile (or load from the cache) and load the module on the current device. */

@@ -1,0 +1,177 @@
+"""Large stage systems: the kernels with a global-memory slab per CTA
+(blocked LU condensation, CTA-per-merge tree, CTA top solve), through the
+C ABI.
+
+* On the golden stage cases, the large-system layout gives the condensed
+  blocks of the shared-memory layout to 1e-14 relative: the blocked LU
+  performs the unblocked elimination's operations in the same order, and
+  only the problem functions, compiled into other kernels, may round a
+  product-sum differently (most cases agree bit for bit).  The Newton
+  directions agree to 1e-12 (the Householder updates of the tree sum in
+  another order).
+* End-to-end with the large-system layout: the reference's golden solves
+  (same Newton, residual and remesh counts, solutions within 1e-8).
+* Pendulum chains of K = 16 (ny 64, nz 4, np 32, m 5: s = 340) and K = 32
+  (ny 128, nz 8, np 64, m 4: s = 544), which only the large-system layout
+  can hold, against the oracle: stage residual 1e-12, condensed blocks 1e-9,
+  Newton directions 1e-8 (relative to the largest entry), segment residual
+  1e-11, and whole solves (same counts, solutions within 1e-8).
+"""
+import numpy as np
+import pytest
+
+from conftest import OracleProblem, golden, load_problem, pkg
+from oracle import collocation_oracle as O
+
+pytestmark = pytest.mark.gpu
+
+STAGES = [("vdp_n21_m4", "vdp"), ("vdp_n33_m5", "vdp"), ("dint_n33_m3", "dint_param"),
+          ("pend2_n21_m5", "pend2"), ("econ_n17_m3", "eqcon")]
+E2E = [("vdp_cfg1", "vdp"), ("pend2", "pend2"), ("vdp_ineq", "vdp_ineq")]
+
+
+@pytest.fixture(scope="module")
+def cs():
+    c = pkg()
+    c._lib.load()
+    return c
+
+
+_CP = {}
+
+
+def compiled(cs, key, make_problem, m, layout):
+    k = (key, m, layout)
+    if k not in _CP:
+        _CP[k] = cs.CompiledProblem(make_problem(), m, layout=layout)
+    return _CP[k]
+
+
+def _direction(cs, cp, t, y, yd, zt, p, alpha, theta=None):
+    bt = cs.Batch(cp, 1)
+    bt.set_state([(t, y, yd, zt)], np.asarray(p, float).reshape(1, -1),
+                 None if theta is None else np.asarray(theta, float).reshape(1, -1))
+    return bt, bt.stage_newton_direction(alpha)
+
+
+@pytest.mark.parametrize("case,prob", STAGES)
+def test_large_layout_matches_shared_memory_layout(cs, case, prob):
+    g = golden("stage_" + case)
+    m, N = int(g["m"]), int(g["N"])
+    outs = []
+    for layout in (1, 2):
+        cp = compiled(cs, prob, lambda: load_problem(prob), m, layout)
+        _, out = _direction(cs, cp, g["t"], g["y"], g["y_dot"], g["z_tilde"], g["p"], float(g["alpha"]))
+        outs.append(out)
+    small, big = outs
+    rs, rb = small["rows"][:N - 1], big["rows"][:N - 1]
+    np.testing.assert_allclose(rb, rs, rtol=1e-14, atol=1e-14 * max(1.0, np.abs(rs).max()))
+    for k in ("dy", "dydot", "dzt", "dp"):
+        a, b = np.asarray(big[k]), np.asarray(small[k])
+        if a.size == 0:
+            continue
+        scale = max(1.0, np.abs(b).max())
+        np.testing.assert_allclose(a, b, rtol=0, atol=1e-12 * scale, err_msg=k)
+
+
+@pytest.mark.parametrize("case,prob", E2E)
+def test_large_layout_end_to_end_matches_reference(cs, case, prob):
+    g = golden("e2e_" + case)
+    m = int(g["m"])
+    pr = load_problem(prob)
+    sol = cs.solver.solve_single(pr, m, layout=2)
+    assert sol["success"] == bool(g["success"])
+    assert sol["N"] == g["t"].shape[0]
+    assert sol["newton_steps"] == int(g["jacobian_counts"])
+    assert sol["residual_evals"] == int(g["residual_counts"])
+    np.testing.assert_array_equal(sol["t"], g["t"])
+    np.testing.assert_allclose(sol["y"], g["y"], atol=1e-8, rtol=0)
+    np.testing.assert_allclose(sol["z"], g["z"], atol=1e-8, rtol=0)
+    np.testing.assert_allclose(sol["p"], g["p"], atol=1e-8, rtol=0)
+
+
+# ------------------------------------------------------- pendulum chains ---
+PEND = {16: 5, 32: 4}   # K -> m (the sizes of the large single-instance workloads)
+
+
+def _pendulum(cs, K, nodes):
+    theta0 = np.random.default_rng(0).uniform(-0.5, 0.5, K)
+    return cs.ocp.Problem(cs.workloads.pendulum_ocp(K, theta0, nodes=nodes), name="pend%d" % K)
+
+
+def _pend_state(cs, K, m, nodes, seed=3):
+    """A generic state: the problem's initial input plus noise."""
+    pr = _pendulum(cs, K, nodes)
+    P = OracleProblem(pr)
+    rk = cs.tables.lobatto(m)
+    y, yd, zt = O.form_initial_input(P, m, nodes, np.asarray(pr.Y0, float), np.asarray(pr.Z0, float),
+                                     np.asarray(pr.P0, float), rk)
+    rng = np.random.default_rng(seed)
+    y = y + 0.05 * rng.standard_normal(y.shape)
+    yd = yd + 0.05 * rng.standard_normal(yd.shape)
+    zt = zt + 0.05 * rng.standard_normal(zt.shape)
+    p = np.asarray(pr.P0, float) + 0.05 * rng.standard_normal(pr.size_p)
+    return pr, P, rk, np.asarray(pr.T0, float), y, yd, zt, p
+
+
+@pytest.mark.parametrize("K", [16, 32])
+def test_pendulum_stages_match_oracle(cs, K):
+    m = PEND[K]
+    nodes = 9
+    pr, P, rk, t, y, yd, zt, p = _pend_state(cs, K, m, nodes)
+    cp = compiled(cs, "pend%d" % K, lambda: pr, m, 0)
+    alpha = 0.1
+    # residual pieces
+    bt = cs.Batch(cp, 1)
+    bt.set_state([(t, y, yd, zt)], p.reshape(1, -1))
+    norms, fa, fb = bt.stage_residual(alpha, pieces=True)
+    f_q, y_tilde, f_a, f_b, r_bc = O.compute_f_q(P, m, nodes, rk, t, y, yd, zt, p, alpha)
+    sc = max(1.0, np.abs(f_q).max())
+    np.testing.assert_allclose(fa[:nodes - 1], f_a, rtol=0, atol=1e-12 * sc)
+    np.testing.assert_allclose(fb[:nodes - 1], f_b, rtol=0, atol=1e-12 * sc)
+    assert abs(norms[0] - np.abs(f_q).max()) <= 1e-12 * sc
+    # condensed blocks and the Newton direction
+    out = bt.stage_newton_direction(alpha)
+    ny, npe = cp.ny, cp.np_eff
+    J, V, D, W, B_0, B_n, V_n = O.construct_jacobian(P, m, nodes, rk, t, y, y_tilde, zt, p, alpha)
+    A, C, H, b = O.reduce_jacobian(ny, cp.nz, cp.np, m, nodes, W, D, J, V, f_a, f_b)
+    rows = out["rows"][:nodes - 1].reshape(nodes - 1, 2 * ny + npe + 1, ny)
+    gA = np.transpose(rows[:, :ny, :], (0, 2, 1))
+    gb = rows[:, 2 * ny + npe, :]
+    np.testing.assert_allclose(gA, A.reshape(nodes - 1, ny, ny), rtol=0, atol=1e-9 * max(1.0, np.abs(A).max()))
+    np.testing.assert_allclose(gb, b, rtol=0, atol=1e-9 * max(1.0, np.abs(b).max()))
+    dy, dyd, dzt, dp = O.newton_step(P, m, nodes, rk, t, y, yd, zt, p, alpha, f_a, f_b, r_bc, y_tilde)
+    scale = max(1.0, np.abs(dy).max())
+    np.testing.assert_allclose(out["dy"][:nodes], dy, rtol=0, atol=1e-8 * scale)
+    np.testing.assert_allclose(out["dp"][0], dp, rtol=0, atol=1e-8 * scale)
+    np.testing.assert_allclose(out["dydot"][:nodes - 1].reshape(-1, ny), dyd, rtol=0,
+                               atol=1e-8 * max(1.0, np.abs(dyd).max()))
+    np.testing.assert_allclose(out["dzt"][:nodes - 1].reshape(-1, cp.nz), dzt, rtol=0,
+                               atol=1e-8 * max(1.0, np.abs(dzt).max()))
+    # segment residual
+    res, mx = bt.stage_segment_residual(alpha, pr.tolerance)
+    ref, ref_max = O.segment_residual(P, m, nodes, t, y, yd, zt, p, alpha, pr.tolerance, cs.tables.segment_tables(m))
+    np.testing.assert_allclose(res[:nodes], ref, rtol=1e-11, atol=1e-12)
+    assert abs(mx[0] - ref_max) <= 1e-11 * abs(ref_max)
+
+
+@pytest.mark.parametrize("K", [16, 32])
+def test_pendulum_solve_matches_oracle(cs, K):
+    """Whole solves from a coarse 9-node guess: remeshes, the continuation
+    and the Newton counts as the oracle's."""
+    m = PEND[K]
+    pr = _pendulum(cs, K, 9)
+    cp = compiled(cs, "pend%d" % K, lambda: pr, m, 0)
+    bt = cs.Batch(cp, 1)
+    bt.set_guess([(np.asarray(pr.T0, float), np.asarray(pr.Y0, float), np.asarray(pr.Z0, float))],
+                 np.asarray(pr.P0, float).reshape(1, -1))
+    bt.solve(cs.default_opts(pr))
+    s = bt.solution()[0]
+    P = OracleProblem(pr)
+    ref = O.solve(P, m, cs.tables.lobatto(m), cs.tables.segment_tables(m))
+    assert s["success"] == ref.success
+    assert (s["N"], s["newton_steps"], s["residual_evals"]) == (ref.N, ref.jacobian_count, ref.residual_count)
+    assert s["remeshes"] == len(ref.nodes_after_remesh)
+    np.testing.assert_allclose(s["y"], ref.y, rtol=0, atol=1e-8)
+    np.testing.assert_allclose(s["z"], ref.z, rtol=0, atol=1e-8)
+    np.testing.assert_allclose(s["p"], ref.p, rtol=0, atol=1e-8)
