@@ -528,13 +528,210 @@ def run_plain(args, cs, rank, world, local_rank, cpu, cfg, instances):
         dist.destroy_process_group()
 
 
+# ------------------------------------------------ large single instances ---
+PENDULUM = {16: dict(m=5, nodes=8193, tol=1e-6, seed=0), 32: dict(m=4, nodes=16385, tol=1e-8, seed=2)}
+
+
+def pendulum_problem(cs, K):
+    c = PENDULUM[K]
+    theta0 = np.random.default_rng(c["seed"]).uniform(-0.5, 0.5, K)
+    return cs.ocp.Problem(cs.workloads.pendulum_ocp(K, theta0, nodes=c["nodes"], tol=c["tol"]), name="pend%d" % K)
+
+
+def executed_flops_per_interval(m, ny, nz, npe):
+    """FP64 flops the structured condensation executes per interval: LU of
+    the stage system without its stage-0 block (s1 = (m-1)(ny+nz) rows) with
+    r right-hand sides, their back substitution, and the stage-0 coupling of
+    the right-hand sides (2 s1 r ny)."""
+    s1 = (m - 1) * (ny + nz)
+    r = ny + npe + 1
+    return 2.0 / 3.0 * s1 ** 3 + 2.0 * s1 * s1 * r + 2.0 * s1 * r * ny
+
+
+def _cpu_pendulum(cs, pr, m, slice_intervals=256):
+    """The oracle (numpy, BLAS threads on all host cores) on one residual and
+    one Newton step of the first `slice_intervals` intervals of the mesh;
+    seconds per interval of each."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from oracle import collocation_oracle as O
+
+    class P:
+        pass
+
+    op = P()
+    op.__dict__.update(pr.__dict__)
+    op.ny, op.nz, op.np = pr.size_y, pr.size_z, pr.size_p
+    nf = cs.codegen.NumpyProblem(cs.codegen.ProblemCode(pr.sym))
+    for k in ("f", "g", "Df", "Dg", "r", "Dr"):
+        setattr(op, k, getattr(nf, k))
+    n = slice_intervals + 1
+    t = np.asarray(pr.T0, float)[:n]
+    rk = cs.tables.lobatto(m)
+    y, yd, zt = O.form_initial_input(op, m, n, np.asarray(pr.Y0, float)[:n], np.asarray(pr.Z0, float)[:n],
+                                     np.asarray(pr.P0, float), rk)
+    p = np.asarray(pr.P0, float)
+    t0 = time.time()
+    f_q, y_tilde, f_a, f_b, r_bc = O.compute_f_q(op, m, n, rk, t, y, yd, zt, p, 0.1)
+    t_res = time.time() - t0
+    t0 = time.time()
+    O.newton_step(op, m, n, rk, t, y, yd, zt, p, 0.1, f_a, f_b, r_bc, y_tilde)
+    t_newton = time.time() - t0
+    return t_res / slice_intervals, t_newton / slice_intervals
+
+
+def run_pendulum_reference(args, cs, cores):
+    """The reference's algorithm (the oracle port, numpy with BLAS on all
+    cores) on the pendulum workload: a whole solve is minutes, so each step
+    is one residual and one Newton step on 256 intervals, scaled to the
+    full mesh and the solve's counts (3 Newton steps, 7 residuals, as the
+    GPU solve of this configuration takes)."""
+    c = PENDULUM[args.pendulum]
+    pr = pendulum_problem(cs, args.pendulum)
+    n_int = c["nodes"] - 1
+    for _ in range(args.warmup):
+        _cpu_pendulum(cs, pr, c["m"])
+    t0 = time.time()
+    ts = [_cpu_pendulum(cs, pr, c["m"]) for _ in range(args.steps)]
+    wall = time.time() - t0
+    t_res = float(np.mean([a for a, _ in ts]))
+    t_nw = float(np.mean([b for _, b in ts]))
+    t_solve = 3 * t_nw * n_int + 7 * t_res * n_int
+    v = 1.0 / t_solve
+    line = {"impl": "reference", "metric": "solves/sec to %g residual: one large instance (pendulum chain K=%d), "
+                                            "plain GPU solver" % (c["tol"], args.pendulum),
+            "value": v, "unit": "solves/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1000 * wall / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "pendulum chain K=%d, Nodes=%d, m=%d" % (args.pendulum, c["nodes"], c["m"])},
+            "cpu_baseline": {"value": v, "unit": "solves/s", "cores": cores, "kind": "port",
+                             "sample": "one residual + one Newton step on 256 intervals per step, scaled"},
+            "e2e": {"value": v, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def run_pendulum(args, cs, rank, world, local_rank):
+    """One large instance per step (pendulum chain, FP64): solves/s, e2e from
+    host buffers, roofline of the condensation, the oracle extrapolated."""
+    K = args.pendulum
+    c = PENDULUM[K]
+    m, nodes = c["m"], c["nodes"]
+    cores = os.cpu_count() or 1
+    pr = pendulum_problem(cs, K)
+    cpu_t = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cpu_t = _cpu_pendulum(cs, pr, m)
+    dist = _dist_setup(world, local_rank)
+    cs.build.build_library()
+    cs._lib.load()
+    fp64_peak = cs.module.measure_fp64_peak()
+    cp = cs.CompiledProblem(pr, m)
+    bt = cs.Batch(cp, 1, node_capacity=4 * nodes)
+    T0 = cs.module.PinnedArray((nodes,), np.float64)
+    T0.array[...] = np.asarray(pr.T0, float)
+    Y0 = cs.module.PinnedArray((nodes, cp.ny), np.float64)
+    Y0.array[...] = np.asarray(pr.Y0, float)
+    Z0 = cs.module.PinnedArray((nodes, cp.nz), np.float64)
+    Z0.array[...] = np.asarray(pr.Z0, float)
+    P0 = cs.module.PinnedArray((1, cp.np), np.float64)
+    P0.array[...] = np.asarray(pr.P0, float)
+    Nh = cs.module.PinnedArray((1,), np.int32)
+    Nh.array[...] = nodes
+    bt.set_guess_packed(Nh.array, T0.array, Y0.array, Z0.array, P0.array, None)
+    opts = cs.default_opts(pr)
+    for _ in range(args.warmup):
+        bt.reset()
+        bt.solve(opts)
+    bt.profile_reset(timing=False)
+    _barrier(dist)
+    with ClockSampler(local_rank) as clk:
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            bt.reset()
+            bt.solve(opts)
+        dt = _max_over_ranks(dist, time.perf_counter() - t0)
+    sol = bt.solution()[0]
+    launches = bt.profile()["launches"]
+    ok = int(sol["success"])
+    value = _sum_over_ranks(dist, args.steps * ok) / dt
+    # phases (one extra solve with per-launch event timing)
+    bt.reset()
+    bt.profile_reset(timing=True)
+    bt.solve(opts)
+    prof = bt.profile()
+    bt.profile_reset(timing=False)
+    # end to end: guess from pinned host memory, solution back to pinned memory
+    cap = 4 * nodes
+    out = {k: cs.module.PinnedArray(sh) for k, sh in (("t", (cap,)), ("y", (cap, cp.ny)), ("z", (cap, cp.nz)),
+                                                       ("p", (1, cp.np)))}
+    _barrier(dist)
+    t0 = time.perf_counter()
+    d2h = 0
+    for _ in range(args.steps):
+        bt.set_guess_packed(Nh.array, T0.array, Y0.array, Z0.array, P0.array, None)
+        bt.solve(opts)
+        Nn, T = bt.sizes()
+        st = (cs._lib.Stats * 1)()
+        cs._lib.check(bt._lib.cs_get_solution(bt.handle, cs._lib.dptr(out["t"].array), cs._lib.dptr(out["y"].array),
+                                              cs._lib.dptr(out["z"].array), cs._lib.dptr(out["p"].array), st),
+                      "cs_get_solution")
+        d2h = 8 * T * (1 + cp.ny + cp.nz) + 8 * cp.np + 64
+    dte = _max_over_ranks(dist, time.perf_counter() - t0)
+    h2d = T0.array.nbytes + Y0.array.nbytes + Z0.array.nbytes + P0.array.nbytes + Nh.array.nbytes
+    e2e = {"value": _sum_over_ranks(dist, args.steps * ok) / dte, "unit": "solves/s", "h2d_bytes_per_step": h2d,
+           "d2h_bytes_per_step": d2h}
+    # roofline: one condensation of every interval of the final mesh
+    bt.reset()
+    ms = bt.time_condense(reps=3)
+    n_int = nodes - 1
+    fc = flops_per_interval(m, cp.ny, cp.nz, cp.np_eff)
+    fe = executed_flops_per_interval(m, cp.ny, cp.nz, cp.np_eff)
+    roof = {"bound": "fp64", "kernel": "k_condense", "achieved": fc * n_int / (ms * 1e-3) / 1e12, "peak": fp64_peak,
+            "unit": "TFLOP/s", "frac": fc * n_int / (ms * 1e-3) / 1e12 / fp64_peak, "traffic": None,
+            "ms_per_launch": ms, "flops_per_launch": fc * n_int,
+            "executed_tflops": fe * n_int / (ms * 1e-3) / 1e12,
+            "executed_frac": fe * n_int / (ms * 1e-3) / 1e12 / fp64_peak,
+            "flops_note": "achieved: contract flops (2/3)s^3 + 2 s^2 r per interval, s = m(ny+nz) = %d, r = %d; "
+                          "executed: (2/3)s1^3 + 2 s1^2 r + 2 s1 r ny with s1 = (m-1)(ny+nz) = %d (the stage-0 "
+                          "block is eliminated directly); peak of measured FP64 (DFMA microbenchmark, this run)"
+                          % (m * (cp.ny + cp.nz), cp.ny + cp.np_eff + 1, (m - 1) * (cp.ny + cp.nz))}
+    cpu = None
+    if cpu_t is not None:
+        t_solve = sol["newton_steps"] * cpu_t[1] * n_int + sol["residual_evals"] * cpu_t[0] * n_int
+        cpu = {"value": 1.0 / t_solve, "unit": "solves/s", "cores": cores, "kind": "port",
+               "sample": "oracle (numpy, BLAS on all cores) timed on one residual (%.2f ms/interval) and one Newton "
+                         "step (%.2f ms/interval) of 256 intervals, scaled to the %d intervals and the %d Newton steps "
+                         "and %d residuals of this solve" % (1e3 * cpu_t[0], 1e3 * cpu_t[1], n_int,
+                                                              sol["newton_steps"], sol["residual_evals"])}
+    if rank == 0:
+        line = {"metric": "solves/sec to %g residual: one large instance (pendulum chain K=%d), plain GPU solver"
+                          % (c["tol"], K),
+                "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+                "ms_per_step": 1000 * dt / args.steps, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "config": {"workload": "pendulum chain K=%d (ny %d, nz %d, np %d), Nodes=%d, m=%d, tol %g, "
+                                       "theta(0)~U[-0.5,0.5] seed %d, guess theta_i(0)(1-t/T)"
+                                       % (K, cp.ny, cp.nz, cp.np, nodes, m, c["tol"], c["seed"]),
+                           "l2": "working set %.1f GB, larger than L2 (129 MB)"
+                                 % (nodes * 8 * ((cp.ny + cp.np_eff + 1) * cp.s + 2 * cp.rowsz) / 1e9)},
+                "e2e": e2e, "roofline": roof, "cpu_baseline": cpu, "clocks": clk.summary(),
+                "gpu_launches": int(launches),
+                "solve_stats": {"success": bool(sol["success"]), "N": sol["N"], "newton_steps": sol["newton_steps"],
+                                "residual_evals": sol["residual_evals"], "max_residual": sol["max_residual"]},
+                "phase_ms": {"condense": prof["condense_ms"], "babd": prof["babd_ms"],
+                             "residual": prof["residual_ms"]}}
+        print(json.dumps(line))
+    if dist is not None:
+        dist.destroy_process_group()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="warm", choices=["warm", "plain"])
+    ap.add_argument("--workload", default="warm", choices=["warm", "plain", "pendulum"])
+    ap.add_argument("--pendulum", type=int, default=16, choices=[16, 32], help="chain length K (pendulum)")
     ap.add_argument("--batch", type=int, default=None, help="instances per step (warm: 8192, plain: 4096)")
     ap.add_argument("--train", type=int, default=65536, help="training solutions (warm)")
     ap.add_argument("--epochs", type=int, default=150)
@@ -562,6 +759,13 @@ def main():
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
     cs = _pkg()
     cores = os.cpu_count() or 1
+    if args.workload == "pendulum":
+        if args.impl == "reference":
+            if rank == 0:
+                run_pendulum_reference(args, cs, cores)
+            return
+        run_pendulum(args, cs, rank, world, local_rank)
+        return
     if args.batch is None:
         args.batch = 8192 if args.workload == "warm" else BATCH
     if args.workload == "warm":

@@ -1358,11 +1358,14 @@ extern "C" __global__ void k_babd_cta(CsBatch bt) {}
 #define CS_QSZ (CS_QLD * CS_QC)
 #define CS_TSZ (CS_TLD * (CS_NT + 1))
 #define CS_DRSZ ((CS_NY + CS_NP) * (2 * CS_NY + CS_NP))
-#define CS_Q_SMEM (((long long)CS_QSZ + 32) * 8 <= CS_SMEM_MAX)
+// merges: Householder panels of CS_HB reflectors; shared: V [HB][QLD] | T [HB][HB] | G [HB][HB] | tau [HB] | red [32]
+#define CS_HB 16
+#define CS_SM_HB (CS_HB * CS_QLD + 2 * CS_HB * CS_HB + CS_HB + 32)
+#define CS_Q_SMEM (((long long)CS_QSZ + CS_SM_HB) * 8 <= CS_SMEM_MAX)
 #define CS_T_SMEM (((long long)CS_TSZ + 32) * 8 <= CS_SMEM_MAX)
 #define CS_WS_TREE (CS_Q_SMEM ? 0ll : (long long)CS_QSZ)
 #define CS_WS_TOP ((CS_T_SMEM ? 0ll : (long long)CS_TSZ) + (long long)CS_DRSZ)
-#define CS_SM_TREE ((CS_Q_SMEM ? CS_QSZ : 0) + 32)
+#define CS_SM_TREE ((CS_Q_SMEM ? CS_QSZ : 0) + CS_SM_HB)
 #define CS_SM_TOP ((CS_T_SMEM ? CS_TSZ : 0) + 32)
 
 __device__ __forceinline__ unsigned cs_dyn_smem_bytes() {
@@ -1754,9 +1757,21 @@ __device__ __forceinline__ void cs_householder_cta(double* A, int ld, int n, int
   __syncthreads();
 }
 
-// merge of block rows a and b, one CTA (layout as cs_merge_warp)
-__device__ void cs_merge_cta(const double* ra, const double* rb, double* out_row, double* rec, double* Q, double* red) {
-  const int tid = threadIdx.x, nt = blockDim.x;
+// Merge of block rows a and b, one CTA (layout as cs_merge_warp), blocked
+// Householder (compact WY, as LAPACK's geqrt): each panel of CS_HB columns is
+// factorised column by column (cs_householder_cta restricted to the panel),
+// its reflectors H_i = I - tau_i v_i v_i^T (tau = 2/|v|^2, the sign rule of
+// matrix_factorization_cuda.py:37-54) are accumulated as
+// H_1 ... H_kb = I - V T V^T, and the columns right of the panel are updated
+// at once, C <- C - V (T^T (V^T C)), one thread per column.
+__device__ void cs_merge_cta(const double* ra, const double* rb, double* out_row, double* rec, double* Q, double* sh) {
+  const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, w = tid >> 5, nw = nt >> 5;
+  constexpr int n = 2 * CS_NY;
+  double* V = sh;                          // [HB][QLD] column-major, zero above row k0 + i
+  double* Tm = V + CS_HB * CS_QLD;         // [HB][HB], T[j][i] at Tm[i * HB + j]
+  double* G = Tm + CS_HB * CS_HB;          // [HB][HB], V_j . V_i at G[i * HB + j]
+  double* tau = G + CS_HB * CS_HB;         // [HB]
+  double* red = tau + CS_HB;               // [32]
   for (int e = tid; e < CS_QC * CS_NY; e += nt) {
     const int c = e / CS_NY, r = e - c * CS_NY;
     double top, bot;
@@ -1770,7 +1785,100 @@ __device__ void cs_merge_cta(const double* ra, const double* rb, double* out_row
   }
   __syncthreads();
 #pragma unroll 1
-  for (int k = 0; k < CS_NY; ++k) cs_householder_cta(Q, CS_QLD, 2 * CS_NY, CS_QC, k, red);
+  for (int k0 = 0; k0 < CS_NY; k0 += CS_HB) {
+    const int kb = min(CS_HB, CS_NY - k0);
+    const int pe = k0 + kb;  // panel end (exclusive)
+    // ---- panel: reflectors of columns k0 .. pe-1, applied inside the panel
+#pragma unroll 1
+    for (int kk = 0; kk < kb; ++kk) {
+      const int k = k0 + kk;
+      double* vk = Q + (size_t)k * CS_QLD;
+      double ss = 0.0;
+      for (int r = k + tid; r < n; r += nt) ss += vk[r] * vk[r];
+      ss = cs_cta_sum(ss, red);
+      const double x0 = vk[k];
+      const double g = (x0 >= 0.0) ? -sqrt(ss) : sqrt(ss);
+      const double v0 = x0 - g;
+      const double vs = ss - x0 * x0 + v0 * v0;
+      double* Vi = V + kk * CS_QLD;
+      if (vs < CS_EPS) {  // uniform: nothing to eliminate, H = I
+        for (int r = tid; r < n; r += nt) Vi[r] = 0.0;
+        if (tid == 0) tau[kk] = 0.0;
+        __syncthreads();
+        continue;
+      }
+      const double beta = -2.0 / vs;
+      for (int r = tid; r < n; r += nt) Vi[r] = (r < k) ? 0.0 : ((r == k) ? v0 : vk[r]);
+      if (tid == 0) tau[kk] = 2.0 / vs;
+      for (int c = k + 1 + w; c < pe; c += nw) {
+        double* col = Q + (size_t)c * CS_QLD;
+        double wv = (lane == 0) ? v0 * col[k] : 0.0;
+        for (int r = k + 1 + lane; r < n; r += 32) wv = fma(vk[r], col[r], wv);
+        for (int o = 16; o > 0; o >>= 1) wv += __shfl_xor_sync(0xffffffffu, wv, o);
+        const double bw = beta * wv;
+        if (lane == 0) col[k] = fma(bw, v0, col[k]);
+        for (int r = k + 1 + lane; r < n; r += 32) col[r] = fma(bw, vk[r], col[r]);
+      }
+      __syncthreads();
+      if (tid == 0) vk[k] = g;
+      for (int r = k + 1 + tid; r < n; r += nt) vk[r] = 0.0;
+      __syncthreads();
+    }
+    // a last panel narrower than CS_HB: its unused reflectors are the identity
+    for (int e = tid; e < (CS_HB - kb) * CS_QLD; e += nt) V[kb * CS_QLD + e] = 0.0;
+    for (int e = tid; e < (CS_HB - kb) * CS_HB; e += nt) Tm[kb * CS_HB + e] = 0.0;
+    // ---- T: G = V^T V (upper part), then T column by column
+    for (int e = tid; e < kb * kb; e += nt) {
+      const int i = e / kb, j = e - i * kb;
+      if (j < i) {
+        const double* vi = V + i * CS_QLD;
+        const double* vj = V + j * CS_QLD;
+        double d = 0.0;
+        for (int r = k0 + i; r < n; ++r) d = fma(vj[r], vi[r], d);
+        G[i * CS_HB + j] = d;
+      }
+    }
+    __syncthreads();
+    if (tid == 0) {
+      for (int i = 0; i < kb; ++i) {
+        const double ti = tau[i];
+        for (int j = 0; j < i; ++j) {
+          double sj = 0.0;
+          for (int q = j; q < i; ++q) sj = fma(Tm[q * CS_HB + j], G[i * CS_HB + q], sj);
+          Tm[i * CS_HB + j] = -ti * sj;
+        }
+        Tm[i * CS_HB + i] = ti;
+      }
+    }
+    __syncthreads();
+    // ---- trailing columns: C <- C - V (T^T (V^T C)), thread per column
+    for (int c = pe + tid; c < CS_QC; c += nt) {
+      double* col = Q + (size_t)c * CS_QLD;
+      double wv[CS_HB];
+#pragma unroll
+      for (int i = 0; i < CS_HB; ++i) wv[i] = 0.0;
+      for (int r = k0; r < n; ++r) {
+        const double x = col[r];
+#pragma unroll
+        for (int i = 0; i < CS_HB; ++i) wv[i] = fma(V[i * CS_QLD + r], x, wv[i]);
+      }
+      double tw[CS_HB];
+#pragma unroll
+      for (int i = 0; i < CS_HB; ++i) {
+        double sacc = 0.0;
+#pragma unroll
+        for (int j = 0; j <= i; ++j) sacc = fma(Tm[i * CS_HB + j], wv[j], sacc);
+        tw[i] = sacc;
+      }
+      for (int r = k0; r < n; ++r) {
+        double x = col[r];
+#pragma unroll
+        for (int i = 0; i < CS_HB; ++i) x = fma(-V[i * CS_QLD + r], tw[i], x);
+        col[r] = x;
+      }
+    }
+    __syncthreads();
+  }
   for (int e = tid; e < CS_QC * CS_NY; e += nt) {
     const int c = e / CS_NY, r = e - c * CS_NY;
     rec[e] = Q[(size_t)c * CS_QLD + r];
@@ -1783,7 +1891,7 @@ extern "C" __global__ void __launch_bounds__(256) k_tree_level(CsBatch bt, int l
   extern __shared__ double smem[];
   if (!cs_big_ok(bt, CS_WS_TREE, CS_SM_TREE)) return;
   double* Q = CS_Q_SMEM ? smem : bt.wsp + (size_t)blockIdx.x * bt.wsp_stride;
-  double* red = CS_Q_SMEM ? smem + CS_QSZ : smem;
+  double* sh = CS_Q_SMEM ? smem + CS_QSZ : smem;
   const int njac = bt.nlist[1];
   const long long* pre = bt.lvl_pre + (size_t)l * (bt.B + 1);
   const long long total = pre[njac];
@@ -1800,7 +1908,7 @@ extern "C" __global__ void __launch_bounds__(256) k_tree_level(CsBatch bt, int l
     double* dst = dstb + (size_t)off * CS_ROWSZ;
     if (mi < merges) {
       cs_merge_cta(src + (size_t)(2 * mi) * CS_ROWSZ, src + (size_t)(2 * mi + 1) * CS_ROWSZ, dst + (size_t)mi * CS_ROWSZ,
-                   bt.tree + (size_t)(off + ((2 * mi + 1) << l)) * CS_TREESZ, Q, red);
+                   bt.tree + (size_t)(off + ((2 * mi + 1) << l)) * CS_TREESZ, Q, sh);
     } else {
       const double* sr = src + (size_t)(nl - 1) * CS_ROWSZ;
       double* dr = dst + (size_t)merges * CS_ROWSZ;

@@ -386,10 +386,11 @@ extern "C" int cs_module_load(const cs_module_desc* d, cs_module** out) {
     const long long sm_cond = (long long)s1 * (nb + 1) + nb * ldg + (long long)d->m * rb + d->m * d->m + d->ny + s1 + 16 + nb;
     const long long qsz = (long long)qld * qc, tsz = (long long)tld * (nt + 1);
     const long long drsz = (long long)(d->ny + d->np) * (2 * d->ny + d->np);
-    const bool q_smem = (qsz + 32) * 8 <= smem_optin, t_smem = (tsz + 32) * 8 <= smem_optin;
+    const long long hb = 16, sm_hb = hb * qld + 2 * hb * hb + hb + 32;
+    const bool q_smem = (qsz + sm_hb) * 8 <= smem_optin, t_smem = (tsz + 32) * 8 <= smem_optin;
     M->slab = std::max(ws_cond, std::max(q_smem ? 0ll : qsz, (t_smem ? 0ll : tsz) + drsz));
     M->condense_smem = (size_t)sm_cond * 8;
-    M->tree_smem = (size_t)((q_smem ? qsz : 0) + 32) * 8;
+    M->tree_smem = (size_t)((q_smem ? qsz : 0) + sm_hb) * 8;
     M->top_smem = (size_t)((t_smem ? tsz : 0) + 32) * 8;
     if (M->condense_smem > (size_t)smem_optin) {
       delete M;
