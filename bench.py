@@ -739,9 +739,22 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--babd-path", type=int, default=0, help="0 automatic, 1 one CTA per instance, 2 per level")
     ap.add_argument("--profile-case", action="store_true",
-                    help="small case for ncu: 512 instances, one full-batch condensation per m group, one solve")
+                    help="small case for ncu: 512 instances, one full-batch condensation per m group, one solve; "
+                         "with --workload pendulum: one Newton direction of the large instance")
     args = ap.parse_args()
     BABD_PATH[0] = args.babd_path
+    if args.profile_case and args.workload == "pendulum":
+        # one Newton direction of the large instance (for ncu)
+        cs = _pkg()
+        cs.build.build_library()
+        pr = pendulum_problem(cs, args.pendulum)
+        cp = cs.CompiledProblem(pr, PENDULUM[args.pendulum]["m"])
+        bt = cs.Batch(cp, 1)
+        bt.set_guess([(np.asarray(pr.T0, float), np.asarray(pr.Y0, float), np.asarray(pr.Z0, float))],
+                     np.asarray(pr.P0, float).reshape(1, -1))
+        out = bt.stage_newton_direction(0.1)
+        print("profile case ok", float(np.abs(out["dy"]).max()))
+        return
     if args.profile_case:
         cs = _pkg()
         cs.build.build_library()

@@ -1851,16 +1851,27 @@ __device__ void cs_merge_cta(const double* ra, const double* rb, double* out_row
       }
     }
     __syncthreads();
-    // ---- trailing columns: C <- C - V (T^T (V^T C)), thread per column
-    for (int c = pe + tid; c < CS_QC; c += nt) {
-      double* col = Q + (size_t)c * CS_QLD;
+    // ---- trailing columns: C <- C - V (T^T (V^T C)); four consecutive lanes
+    //      per column, each over every fourth row, V^T C summed across them
+    const int nc = CS_QC - pe;
+    for (int base = 0; base < 4 * nc; base += nt) {
+      const int u = base + tid;
+      const int c = pe + (u >> 2), part = u & 3;
+      const bool act = c < CS_QC;
+      double* col = Q + (size_t)(act ? c : pe) * CS_QLD;
       double wv[CS_HB];
 #pragma unroll
       for (int i = 0; i < CS_HB; ++i) wv[i] = 0.0;
-      for (int r = k0; r < n; ++r) {
+#pragma unroll 2
+      for (int r = k0 + part; r < n; r += 4) {
         const double x = col[r];
 #pragma unroll
         for (int i = 0; i < CS_HB; ++i) wv[i] = fma(V[i * CS_QLD + r], x, wv[i]);
+      }
+#pragma unroll
+      for (int i = 0; i < CS_HB; ++i) {
+        wv[i] += __shfl_xor_sync(0xffffffffu, wv[i], 1);
+        wv[i] += __shfl_xor_sync(0xffffffffu, wv[i], 2);
       }
       double tw[CS_HB];
 #pragma unroll
@@ -1870,11 +1881,14 @@ __device__ void cs_merge_cta(const double* ra, const double* rb, double* out_row
         for (int j = 0; j <= i; ++j) sacc = fma(Tm[i * CS_HB + j], wv[j], sacc);
         tw[i] = sacc;
       }
-      for (int r = k0; r < n; ++r) {
-        double x = col[r];
+      if (act) {
+#pragma unroll 2
+        for (int r = k0 + part; r < n; r += 4) {
+          double x = col[r];
 #pragma unroll
-        for (int i = 0; i < CS_HB; ++i) x = fma(-V[i * CS_QLD + r], tw[i], x);
-        col[r] = x;
+          for (int i = 0; i < CS_HB; ++i) x = fma(-V[i * CS_QLD + r], tw[i], x);
+          col[r] = x;
+        }
       }
     }
     __syncthreads();

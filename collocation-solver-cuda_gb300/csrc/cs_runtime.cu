@@ -56,6 +56,7 @@ struct DriverApi {
   decltype(&cuLaunchKernel) launchKernel = nullptr;
   decltype(&cuFuncSetAttribute) funcSetAttribute = nullptr;
   decltype(&cuGetErrorString) getErrorString = nullptr;
+  decltype(&cuOccupancyMaxActiveBlocksPerMultiprocessor) occupancy = nullptr;
   bool ok = false;
 };
 DriverApi g_drv;
@@ -192,6 +193,7 @@ int ensure_context() {
     CS_TRY(resolve("cuLaunchKernel", (void**)&g_drv.launchKernel));
     CS_TRY(resolve("cuFuncSetAttribute", (void**)&g_drv.funcSetAttribute));
     CS_TRY(resolve("cuGetErrorString", (void**)&g_drv.getErrorString));
+    CS_TRY(resolve("cuOccupancyMaxActiveBlocksPerMultiprocessor", (void**)&g_drv.occupancy));
     g_drv.ok = true;
   }
   return CS_OK;
@@ -269,7 +271,8 @@ struct cs_module {
   // large stage systems: kernels with a global-memory slab per CTA
   bool big = false;
   long long slab = 0;  // doubles per CTA
-  int big_ctas = 0;
+  int big_ctas = 0;    // CTAs with a slab (the largest grid of the slab kernels)
+  int tree_grid = 0;   // k_tree_level grid (large systems)
 };
 
 static std::string build_source(const cs_module_desc* d, bool big, int smem_max) {
@@ -473,6 +476,15 @@ extern "C" int cs_module_load(const cs_module_desc* d, cs_module** out) {
     CS_CU(g_drv.funcSetAttribute(M->f_tree_level, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, (int)M->tree_smem));
   if (M->top_smem > 48 * 1024)
     CS_CU(g_drv.funcSetAttribute(M->f_top, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, (int)M->top_smem));
+  if (M->big) {
+    // persistent grids from the kernels' occupancy (registers and shared memory)
+    int pc = 0, pt = 0;
+    CS_CU(g_drv.occupancy(&pc, M->f_condense, 256, M->condense_smem));
+    CS_CU(g_drv.occupancy(&pt, M->f_tree_level, 256, M->tree_smem));
+    M->condense_grid = M->sms * std::max(1, pc);
+    M->tree_grid = M->sms * std::max(1, pt);
+    M->big_ctas = std::max(M->condense_grid, M->tree_grid);
+  }
   if (M->babd_cta_smem > (size_t)smem_optin) M->babd_cta_smem = 0;  // per-level kernels only
   else if (M->babd_cta_smem > 48 * 1024)
     CS_CU(g_drv.funcSetAttribute(M->f_babd_cta, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, (int)M->babd_cta_smem));
@@ -773,7 +785,7 @@ static int run_direction(cs_batch* bt, CsBatchDev& v, int nlvl) {
   const unsigned g = (unsigned)(M->sms * 8);
   for (int l = 0; l < nlvl; ++l) {
     void* a[] = {&v, &l};
-    if (M->big) CS_TRY(launch_k(bt, M->f_tree_level, (unsigned)M->big_ctas, 256, M->tree_smem, a, 1));
+    if (M->big) CS_TRY(launch_k(bt, M->f_tree_level, (unsigned)M->tree_grid, 256, M->tree_smem, a, 1));
     else CS_TRY(launch_k(bt, M->f_tree_level, g, 128, M->tree_smem, a, 1));
   }
   {
