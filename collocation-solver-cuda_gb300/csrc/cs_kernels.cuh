@@ -63,13 +63,19 @@
 #define FAIL_MESH 3
 #define FAIL_NAN 4
 
+// Line-search trials evaluated in one super-step once the first trial of a
+// direction was rejected (alpha, alpha/2, ...; the decision walks them in
+// order, so the accepted trial and every count are the sequential ones).
+#define CS_LSW 8
+
 struct CsInst {
   int status, it, ls_it, alphacal;
   int need_jac, accepted, fail_reason, N_new;
   int residual_count, jac_count, seg_count, remesh_count;
-  int iter_time, singular, pad0, pad1;
+  int iter_time, singular, ntrial, ls_prev;   // trials of the next residual evaluation; rejected trials of the last line search
   double alpha_ls, norm_x, alpha, max_res;
   unsigned long long norm_bits, res_bits;
+  unsigned long long trial_bits[CS_LSW - 1];  // norms of trials 1 .. ntrial-1
 };
 
 struct CsConsts {
@@ -226,9 +232,18 @@ extern "C" __global__ void k_residual(CsBatch bt) {
       active = (st == ST_FRESH || st == ST_LS);
     }
     unsigned long long nb = 0;
+    int trial = 0;
     if (active) {
       const bool ls = (st == ST_LS);
-      const double a = ls ? bt.inst[b].alpha_ls : 0.0;
+      if (ls) {
+        // item i of instance b covers trial i / (N-1), interval i % (N-1)
+        const int nm1 = bt.N[b] - 1;
+        trial = i / nm1;
+        i -= trial * nm1;
+        slot = bt.off[b] + i;
+      }
+      double a = ls ? bt.inst[b].alpha_ls : 0.0;
+      for (int q = 0; q < trial; ++q) a *= 0.5;
       const double* th = bt.th + (size_t)b * (CS_NTH > 0 ? CS_NTH : 1);
       double pl[CS_NP > 0 ? CS_NP : 1];
       for (int k = 0; k < CS_NP; ++k) {
@@ -267,7 +282,7 @@ extern "C" __global__ void k_residual(CsBatch bt) {
           double r = f[k] - yd[j][k];
           nan |= (r != r);
           mx = fmax(mx, fabs(r));
-          if (bt.fa_out) bt.fa_out[(size_t)slot * CS_S + j * (CS_NY + CS_NZ) + k] = r;
+          if (bt.fa_out && trial == 0) bt.fa_out[(size_t)slot * CS_S + j * (CS_NY + CS_NZ) + k] = r;
         }
   #if CS_NZ > 0
         double g[CS_NZ];
@@ -275,7 +290,7 @@ extern "C" __global__ void k_residual(CsBatch bt) {
         for (int k = 0; k < CS_NZ; ++k) {
           nan |= (g[k] != g[k]);
           mx = fmax(mx, fabs(g[k]));
-          if (bt.fa_out) bt.fa_out[(size_t)slot * CS_S + j * (CS_NY + CS_NZ) + CS_NY + k] = g[k];
+          if (bt.fa_out && trial == 0) bt.fa_out[(size_t)slot * CS_S + j * (CS_NY + CS_NZ) + CS_NY + k] = g[k];
         }
   #endif
       }
@@ -285,7 +300,7 @@ extern "C" __global__ void k_residual(CsBatch bt) {
         double r = yi1[k] - yi[k] - h * s;
         nan |= (r != r);
         mx = fmax(mx, fabs(r));
-        if (bt.fb_out) bt.fb_out[(size_t)slot * CS_NY + k] = r;
+        if (bt.fb_out && trial == 0) bt.fb_out[(size_t)slot * CS_NY + k] = r;
       }
       if (i == 0) {
         int last = bt.off[b] + bt.N[b] - 1;
@@ -304,7 +319,9 @@ extern "C" __global__ void k_residual(CsBatch bt) {
       nb = nan ? 0x7ff8000000000000ull : cs_abs_bits(mx);
     }
 
-    cs_warp_max_atomic(active ? &bt.inst[b].norm_bits : nullptr, b, nb, active);
+    unsigned long long* dst = nullptr;
+    if (active) dst = trial == 0 ? &bt.inst[b].norm_bits : &bt.inst[b].trial_bits[trial - 1];
+    cs_warp_max_atomic(dst, b * CS_LSW + trial, nb, active);
   }
 }
 
@@ -336,36 +353,55 @@ extern "C" __global__ void k_decide(CsBatch bt, CsConsts c) {
   s.accepted = 0;
   s.need_jac = 0;
   if (s.status == ST_FRESH || s.status == ST_LS) {
-    atomicAdd(&bt.counters[3], (unsigned long long)(bt.N[b] - 1));
+    const int ntr = (s.status == ST_LS) ? max(1, s.ntrial) : 1;
+    atomicAdd(&bt.counters[3], (unsigned long long)(bt.N[b] - 1) * ntr);
     double nt = cs_from_bits(s.norm_bits);
     s.norm_bits = 0ull;
     s.residual_count += 1;
+    s.ntrial = 1;
     if (s.status == ST_FRESH) {
       s.norm_x = nt;
       cs_iteration_start(s, bt.N[b], c, false);
-    } else if (nt < s.norm_x) {
-      s.accepted = 1;
-      s.norm_x = nt;
-      cs_iteration_start(s, bt.N[b], c, true);
     } else {
-      s.ls_it += 1;
-      s.alpha_ls *= 0.5;
-      if (s.ls_it >= c.max_ls) {
-        // No trial accepted: the iterate is unchanged, so every remaining
-        // Newton iteration recomputes the same residual, Jacobian, direction
-        // and rejected trials (the reference loops exactly so until
-        // max_iter, collocation_solver_parallel_2d_shared.py:109-174).  Take
-        // that outcome directly: same state, same counts, then the
-        // iteration-limit failure.
-        const int rem = c.max_iter - s.it;
-        if (rem > 0) {
-          s.residual_count += rem * (1 + c.max_ls);
-          s.jac_count += rem;
-          s.it = c.max_iter;
+      // trials in the reference's order: alpha_ls, alpha_ls/2, ...
+      bool done = false;
+      for (int j = 0; j < ntr && !done; ++j) {
+        const double ntj = (j == 0) ? nt : cs_from_bits(s.trial_bits[j - 1]);
+        if (j > 0) s.residual_count += 1;
+        if (ntj < s.norm_x) {
+          s.accepted = 1;
+          s.norm_x = ntj;
+          s.ls_prev = s.ls_it;
+          cs_iteration_start(s, bt.N[b], c, true);
+          done = true;
+          break;
         }
-        cs_iteration_start(s, bt.N[b], c, false);
+        s.ls_it += 1;
+        s.alpha_ls *= 0.5;
+        if (s.ls_it >= c.max_ls) {
+          // No trial accepted: the iterate is unchanged, so every remaining
+          // Newton iteration recomputes the same residual, Jacobian,
+          // direction and rejected trials (the reference loops exactly so
+          // until max_iter, collocation_solver_parallel_2d_shared.py:109-174).
+          // Take that outcome directly: same state, same counts, then the
+          // iteration-limit failure.
+          const int rem = c.max_iter - s.it;
+          if (rem > 0) {
+            s.residual_count += rem * (1 + c.max_ls);
+            s.jac_count += rem;
+            s.it = c.max_iter;
+          }
+          cs_iteration_start(s, bt.N[b], c, false);
+          done = true;
+        }
       }
+      for (int j = 0; j < CS_LSW - 1; ++j) s.trial_bits[j] = 0ull;
+      // still searching: the next super-step evaluates several trials
+      if (!done) s.ntrial = min(CS_LSW, c.max_ls - s.ls_it);
     }
+    // a new direction follows: an instance whose last line search rejected
+    // trials evaluates several at once from the start
+    if (s.need_jac) s.ntrial = (s.ls_prev > 0) ? min(CS_LSW, c.max_ls) : 1;
     if (s.status == ST_FRESH || s.status == ST_LS || s.need_jac) atomicAdd(&bt.counters[0], 1ull);
     if (s.need_jac) {
       atomicAdd(&bt.counters[1], (unsigned long long)(bt.N[b] - 1));
@@ -453,6 +489,13 @@ __device__ int cs_build_list(int n, F flag, Wt weight, int* list, long long* pre
   return (int)cpos;
 }
 
+// residual work items of an instance: its intervals times the line-search
+// trials of its next residual evaluation
+__device__ __forceinline__ long long cs_res_items(const CsInst& s, int N) {
+  const int t = (s.status == ST_LS || s.need_jac) ? max(1, s.ntrial) : 1;
+  return (long long)(N - 1) * t;
+}
+
 extern "C" __global__ void k_lists(CsBatch bt, int mode, int nlvl) {
   __shared__ long long sh[32];
   const int B = bt.B;
@@ -461,11 +504,11 @@ extern "C" __global__ void k_lists(CsBatch bt, int mode, int nlvl) {
   int nact, njac = 0, nacc = 0;
   if (mode == 0) {
     nact = cs_build_list(B, [&](int b) { int st = I[b].status; return st == ST_FRESH || st == ST_LS; },
-                         [&](int b) { return (long long)(N[b] - 1); }, bt.act, bt.act_pre, sh);
+                         [&](int b) { return cs_res_items(I[b], N[b]); }, bt.act, bt.act_pre, sh);
     if (threadIdx.x == 0) { bt.jac_pre[0] = 0; bt.acc_pre[0] = 0; }
   } else {
     nact = cs_build_list(B, [&](int b) { int st = I[b].status; return st == ST_FRESH || st == ST_LS || I[b].need_jac; },
-                         [&](int b) { return (long long)(N[b] - 1); }, bt.act, bt.act_pre, sh);
+                         [&](int b) { return cs_res_items(I[b], N[b]); }, bt.act, bt.act_pre, sh);
     njac = cs_build_list(B, [&](int b) { return I[b].need_jac != 0; }, [&](int b) { return (long long)(N[b] - 1); },
                          bt.jac, bt.jac_pre, sh);
     nacc = cs_build_list(B, [&](int b) { return I[b].accepted != 0; }, [&](int b) { return (long long)N[b]; },

@@ -84,15 +84,17 @@ const char* drv_err(CUresult r) {
   } while (0)
 
 // Must match struct CsInst in cs_kernels.cuh.
+static const int CS_LSW = 8;  // line-search trials per super-step (cs_kernels.cuh)
 struct CsInst {
   int status, it, ls_it, alphacal;
   int need_jac, accepted, fail_reason, N_new;
   int residual_count, jac_count, seg_count, remesh_count;
-  int iter_time, singular, pad0, pad1;
+  int iter_time, singular, ntrial, ls_prev;
   double alpha_ls, norm_x, alpha, max_res;
   unsigned long long norm_bits, res_bits;
+  unsigned long long trial_bits[CS_LSW - 1];
 };
-static_assert(sizeof(CsInst) == 112, "CsInst layout");
+static_assert(sizeof(CsInst) == 168, "CsInst layout");
 
 struct CsConsts {
   double tol, alpha_m, beta;
@@ -1283,6 +1285,8 @@ static int set_all_status(cs_batch* bt, int status, double alpha, int need_jac) 
     s.accepted = 0;
     s.norm_bits = 0;
     s.res_bits = 0;
+    s.ntrial = 1;
+    memset(s.trial_bits, 0, sizeof(s.trial_bits));
   }
   return write_inst(bt, hi);
 }
