@@ -52,49 +52,140 @@ def _pkg():
     return importlib.import_module(PKG)
 
 
+_T_START = time.time()
+
+
+def _log(msg):
+    """Progress on stderr (the JSON line goes to stdout)."""
+    print("[bench %7.1f s] %s" % (time.time() - _T_START, msg), file=sys.stderr, flush=True)
+
+
 # ------------------------------------------------------------ CPU oracle ---
+_WORKER_PROBLEMS = {}
+
+
+def _family(cs, name):
+    ws = cs.warmstart
+    return ws.vdp_family() if name == "vdp" else ws.pendulum_family(8)
+
+
+def _family_batch(cs, name, n, seed, train=False):
+    """Seeded instances of a warm-start family (training draws use shorter meshes)."""
+    if name == "vdp":
+        return cs.workloads.vdp_batch(n, seed=seed, n_range=(32, 256) if train else (32, 2048))
+    return cs.workloads.pendulum_batch(n, K=8, seed=seed, n_range=(32, 128))
+
+
+def _inst_args(family, inst):
+    if family == "vdp":
+        return (family, tuple(inst.x0), inst.T, inst.r, inst.intervals, inst.m)
+    return (family, tuple(inst.theta0), inst.T, inst.k, inst.intervals, inst.m)
+
+
 def _oracle_worker(args):
-    """Solve one instance with the CPU oracle (runs in a spawned process)."""
-    x0, T, r, intervals, m = args
-    os.environ.setdefault("OMP_NUM_THREADS", "1")
+    """Solve one instance with the CPU oracle (runs in a spawned process;
+    a = None only prepares the problem)."""
+    family, a, T, c, intervals, m = args
     cs = _pkg()
     from oracle import collocation_oracle as O
-    pr = cs.workloads.vdp_family_problem()
+    if family not in _WORKER_PROBLEMS:
+        fam = _family(cs, family)
+        pr = fam.problem
 
-    class P:
-        pass
+        class P:
+            pass
 
-    op = P()
-    op.__dict__.update(pr.__dict__)
-    op.ny, op.nz, op.np = pr.size_y, pr.size_z, pr.size_p
-    nf = cs.codegen.NumpyProblem(cs.codegen.ProblemCode(pr.sym))
-    for k in ("f", "g", "Df", "Dg", "r", "Dr"):
-        setattr(op, k, getattr(nf, k))
-    op.theta = np.array([x0[0], x0[1], r])
-    inst = cs.workloads.VdpInstance(np.array(x0), T, r, intervals, m)
-    t, y, z, p = inst.guess()
+        op = P()
+        op.__dict__.update(pr.__dict__)
+        op.ny, op.nz, op.np = pr.size_y, pr.size_z, pr.size_p
+        nf = cs.codegen.NumpyProblem(cs.codegen.ProblemCode(pr.sym))
+        for k in ("f", "g", "Df", "Dg", "r", "Dr"):
+            setattr(op, k, getattr(nf, k))
+        _WORKER_PROBLEMS[family] = (fam, op)
+    fam, op = _WORKER_PROBLEMS[family]
+    if a is None:
+        return None
+    if family == "vdp":
+        inst = cs.workloads.VdpInstance(np.array(a), T, c, intervals, m)
+    else:
+        inst = cs.workloads.PendulumInstance(np.array(a), T, c, intervals, m)
+    op.theta = fam.theta(inst)
+    t, y, z, p = fam.plain_guess(inst)
     res = O.solve(op, m, cs.tables.lobatto(m), cs.tables.segment_tables(m), T0=t, Y0=y, Z0=z, P0=p)
     return res.success, res.N
 
 
-def cpu_oracle_rate(instances, procs, target_s=20.0, min_n=None):
-    """Solves/s of the oracle on a bounded sample, with `procs` processes."""
-    ctx = mp.get_context("spawn")
-    args = [(tuple(i.x0), i.T, i.r, i.intervals, i.m) for i in instances]
-    n = min_n or procs
-    with ctx.Pool(procs) as pool:
-        pool.map(_oracle_worker, args[:procs])  # import / codegen warm-up
+def _oracle_prepare(family):
+    """Import, derivation and numpy code generation in a worker (no solve)."""
+    return _oracle_worker((family, None, 0.0, 0.0, 0, 0))
+
+
+class OracleSampler:
+    """A pool of single-threaded oracle processes (spawned, BLAS pinned to
+    one thread each before numpy loads in the children) that solves
+    instances for a bounded wall-clock window."""
+
+    ENV = ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS")
+
+    def __init__(self, family, procs):
+        self.family, self.procs = family, procs
+        saved = {k: os.environ.get(k) for k in self.ENV}
+        for k in self.ENV:
+            os.environ[k] = "1"
+        try:
+            self.pool = mp.get_context("spawn").Pool(procs)
+        finally:
+            for k, v in saved.items():
+                if v is None:
+                    os.environ.pop(k, None)
+                else:
+                    os.environ[k] = v
+        self.pool.map(_oracle_prepare, [family] * procs)
+
+    def run(self, instances, window_s, grace_s=30.0):
+        """Solve instances in order, `procs` at a time, starting new ones
+        until `window_s` has passed; returns (completed, seconds from the
+        start to the last completion).  Solves still running `grace_s` after
+        the window are abandoned (the sample then favours the CPU)."""
+        it = iter([_inst_args(self.family, i) for i in instances])
+        pending = []
         t0 = time.time()
+        t_last = t0
         done = 0
-        while True:
-            chunk = args[done:done + n]
-            if not chunk:
+
+        def submit():
+            a = next(it, None)
+            if a is not None:
+                pending.append(self.pool.apply_async(_oracle_worker, (a,)))
+
+        for _ in range(self.procs):
+            submit()
+        while pending:
+            for r in [r for r in pending if r.ready()]:
+                pending.remove(r)
+                r.get()
+                done += 1
+                t_last = time.time()
+                if t_last - t0 < window_s:
+                    submit()
+            if time.time() - t0 > window_s + grace_s:
                 break
-            pool.map(_oracle_worker, chunk)
-            done += len(chunk)
-            if time.time() - t0 > target_s:
-                break
-        dt = time.time() - t0
+            time.sleep(0.005)
+        self.abandoned = len(pending)
+        return done, max(t_last - t0, 1e-9)
+
+    def close(self):
+        self.pool.terminate()
+        self.pool.join()
+
+
+def cpu_oracle_rate(instances, procs, target_s=20.0, family="vdp"):
+    """Solves/s of the oracle on a bounded sample, with `procs` processes."""
+    smp = OracleSampler(family, procs)
+    try:
+        done, dt = smp.run(instances, target_s)
+    finally:
+        smp.close()
     return done / dt, done, dt
 
 
@@ -297,8 +388,9 @@ def _roofline(groups, fp64_peak):
         bt.reset()
         ms = bt.time_condense(reps=5)
         n_int = bt.sizes()[1] - bt.B
-        flops += n_int * flops_per_interval(m)
-        cbytes += n_int * bytes_per_interval(m)
+        cp = bt.cp
+        flops += n_int * flops_per_interval(m, cp.ny, cp.nz, cp.np_eff)
+        cbytes += n_int * bytes_per_interval(m, cp.ny, cp.nz, cp.np_eff)
         cms += ms
         n_all += n_int
     achieved = flops / (cms * 1e-3) / 1e12
@@ -316,46 +408,51 @@ def _roofline(groups, fp64_peak):
             "hbm_gbs": cbytes / (cms * 1e-3) / 1e9}
 
 
-def _cpu_baseline(instances, cores, seed=3):
+def _cpu_baseline(instances, cores, seed=3, family="vdp"):
     rng = np.random.default_rng(seed)
     idx = rng.permutation(len(instances))
     sample = [instances[i] for i in idx]
-    rate, n, dt = cpu_oracle_rate(sample, cores, target_s=20.0)
+    rate, n, dt = cpu_oracle_rate(sample, cores, target_s=20.0, family=family)
     return {"value": rate, "unit": "solves/s", "cores": cores, "kind": "port",
             "sample": "%d random instances of the batch solved by the oracle from the plain guess in %.1f s, one "
-                      "process per core" % (n, dt)}
+                      "process per core (single-threaded BLAS)" % (n, dt)}
 
 
 def run_reference(args, instances, cfg, cores):
     """The reference's CPU implementation of the path (its Python restated as
-    the oracle), all host cores, bounded sample per step."""
-    procs = cores
+    the oracle), all host cores, one process per core; each step is a
+    bounded sample: the instances that finish in a 10 s window."""
     sample = instances[:]
     rng = np.random.default_rng(7)
     rng.shuffle(sample)
-    per_step = 2 * procs
-    ctx = mp.get_context("spawn")
-    a = [(tuple(i.x0), i.T, i.r, i.intervals, i.m) for i in sample]
-    with ctx.Pool(procs) as pool:
-        pool.map(_oracle_worker, a[:procs])
-        pos = 0
+    smp = OracleSampler(args.family, cores)
+    window = 10.0
+    pos = 0
+    try:
         for _ in range(args.warmup):
-            pool.map(_oracle_worker, a[pos:pos + per_step])
-            pos += per_step
-        t0 = time.time()
+            d, _ = smp.run(sample[pos:], window)
+            pos += d + smp.abandoned
+        done = 0
+        t_all = 0.0
+        wall0 = time.time()
         for _ in range(args.steps):
-            pool.map(_oracle_worker, a[pos:pos + per_step])
-            pos += per_step
-        dt = time.time() - t0
-    v = args.steps * per_step / dt
+            d, dt = smp.run(sample[pos:], window)
+            pos += d + smp.abandoned
+            done += d
+            t_all += dt
+        wall = time.time() - wall0
+    finally:
+        smp.close()
+    v = done / t_all
     cfg = dict(cfg, l2="n/a (CPU)")
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "solves/s", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * dt / args.steps,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * wall / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic", "config": cfg,
-            "cpu_baseline": {"value": v, "unit": "solves/s", "cores": procs, "kind": "port",
-                             "sample": "%d random instances of the batch per step from the plain guess (the "
-                                       "reference has no warm start), one per process" % per_step},
+            "cpu_baseline": {"value": v, "unit": "solves/s", "cores": cores, "kind": "port",
+                             "sample": "%d random instances of the batch from the plain guess (the reference has no "
+                                       "warm start), one process per core, those finishing in a %.0f s window per "
+                                       "step" % (done, window)},
             "e2e": {"value": v, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
@@ -366,20 +463,24 @@ def run_warm(args, cs, rank, world, local_rank, cpu, cfg):
     cs._lib.load()
     ws = cs.warmstart
     fp64_peak = cs.module.measure_fp64_peak()
-    fam = ws.vdp_family()
-    solver = ws.BatchSolver(fam, cs.default_opts(fam.problem, max_nodes=20000, babd_path=args.babd_path))
+    fam = _family(cs, args.family)
+    solver = ws.BatchSolver(fam, cs.default_opts(fam.problem, max_nodes=20000, babd_path=args.babd_path),
+                            layout=args.layout)
     # ---- set-up: training data from the batched solver, then training
     t0 = time.perf_counter()
-    train = cs.workloads.vdp_batch(args.train, seed=1000 + 100 * rank, n_range=(32, 256))
+    train = _family_batch(cs, args.family, args.train, 1000 + 100 * rank, train=True)
+    _log("training set: solving %d instances" % len(train))
     X, Y, _ = ws.training_set(fam, solver, train)
     t_data = time.perf_counter() - t0
+    _log("training set: %d solutions in %.1f s; training" % (len(X), t_data))
     t0 = time.perf_counter()
     net = ws.Mlp(X.shape[1], Y.shape[1], width=256, depth=4, seed=0)
     net.fit_normalization(X, Y)
     loss = net.train(X, Y, epochs=args.epochs, batch=1024, lr=1e-3, seed=0)
     t_train = time.perf_counter() - t0
     # ---- evaluation batch, resident in HBM
-    held = cs.workloads.vdp_batch(args.batch, seed=7 + 100 * rank)
+    _log("trained in %.1f s (loss %.3g)" % (t_train, loss))
+    held = _family_batch(cs, args.family, args.batch, 7 + 100 * rank)
     runner = ws.WarmRunner(fam, solver, net, held)
     ws_gb = sum(g["bt"].sizes()[1] for g in runner.groups) * 8 * 300 / 1e9
     cfg["l2"] = cfg["l2"] % ("%.1f" % ws_gb)
@@ -387,6 +488,7 @@ def run_warm(args, cs, rank, world, local_rank, cpu, cfg):
         runner.run(warm=True)
     for g in runner.groups:
         g["bt"].profile_reset(timing=False)
+    _log("warm-up done; timed warm-started steps")
     _barrier(dist)
     with ClockSampler(local_rank) as clk:
         t0 = time.perf_counter()
@@ -399,6 +501,7 @@ def run_warm(args, cs, rank, world, local_rank, cpu, cfg):
     value = _sum_over_ranks(dist, args.steps * solved) / dt
     newton_warm = np.mean([s["newton_steps"] for s in sols])
     # ---- plain batched solve of the same instances
+    _log("warm: %.1f solves/s; plain batched" % value)
     runner.run(warm=False)
     t0 = time.perf_counter()
     for _ in range(args.steps):
@@ -407,6 +510,7 @@ def run_warm(args, cs, rank, world, local_rank, cpu, cfg):
     plain_batched = _sum_over_ranks(dist, args.steps * solved_p) / dtp
     newton_plain = np.mean([s["newton_steps"] for s in sols_p])
     # ---- plain one-instance GPU solver on a random sample of the same batch
+    _log("plain batched: %.1f solves/s; plain one-instance sample" % plain_batched)
     rng = np.random.default_rng(11)
     sample = [held[k] for k in rng.choice(len(held), size=args.single_sample, replace=False)]
     solver.solve(sample[:2])
@@ -417,12 +521,13 @@ def run_warm(args, cs, rank, world, local_rank, cpu, cfg):
     dts = time.perf_counter() - t0
     plain_single = n_ok / dts
     # ---- end to end through the C ABI from pinned host buffers
+    _log("plain one-instance: %.1f solves/s; end to end" % plain_single)
     Xh = cs.module.PinnedArray((len(runner.instances), X.shape[1]), np.float32)
     Xh.array[...] = np.array([fam.features(i) for i in runner.instances], np.float32)
     hosts = []
     for g in runner.groups:
         insts = runner.instances[g["first"]:g["first"] + g["n"]]
-        N, t, y, z, p, th = cs.workloads.pack_vdp(insts)
+        N, t, y, z, p, th = ws.pack_family(fam, insts)
         hh = {}
         for k, a in (("N", N), ("t", t), ("y", y), ("z", z), ("p", p), ("th", th)):
             pa = cs.module.PinnedArray(a.shape, a.dtype)
@@ -731,6 +836,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="warm", choices=["warm", "plain", "pendulum"])
+    ap.add_argument("--family", default="vdp", choices=["vdp", "pendulum8"],
+                    help="warm-start family (warm workload and its reference arm)")
     ap.add_argument("--pendulum", type=int, default=16, choices=[16, 32], help="chain length K (pendulum)")
     ap.add_argument("--batch", type=int, default=None, help="instances per step (warm: 8192, plain: 4096)")
     ap.add_argument("--train", type=int, default=65536, help="training solutions (warm)")
@@ -738,6 +845,8 @@ def main():
     ap.add_argument("--single-sample", type=int, default=64)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--babd-path", type=int, default=0, help="0 automatic, 1 one CTA per instance, 2 per level")
+    ap.add_argument("--layout", type=int, default=0,
+                    help="kernel layout: 0 automatic, 1 shared-memory kernels, 2 large-system kernels")
     ap.add_argument("--profile-case", action="store_true",
                     help="small case for ncu: 512 instances, one full-batch condensation per m group, one solve; "
                          "with --workload pendulum: one Newton direction of the large instance")
@@ -781,7 +890,16 @@ def main():
         return
     if args.batch is None:
         args.batch = 8192 if args.workload == "warm" else BATCH
-    if args.workload == "warm":
+    if args.workload == "warm" and args.family == "pendulum8":
+        instances = _family_batch(cs, "pendulum8", args.batch, 7 + 100 * rank)
+        cfg = {"workload": "NN-warm-started batched solve: pendulum chain K=8 family (ny 32, nz 2, np 16), %d "
+                           "held-out instances per GPU (theta(0)~U[-0.5,0.5]^8, T~U[5,15], k~U[0.2,1.0], "
+                           "N~U{32..128} intervals, m=4, seed 7 + 100 rank), MLP trained on %d batched-solver "
+                           "solutions (seed 1000)" % (args.batch, args.train),
+               "batch_per_gpu": args.batch, "tol": 1e-6, "precision": "fp64 solver, bf16/fp32 network",
+               "warm_start": "MLP 4x256 GELU, 64 normalised-time nodes, fallback to the plain guess",
+               "l2": "working set %s GB per step, larger than L2 (129 MB)"}
+    elif args.workload == "warm":
         instances = cs.workloads.vdp_batch(args.batch, seed=7 + 100 * rank)
         cfg = {"workload": "NN-warm-started batched solve: Van der Pol family, %d held-out instances per GPU "
                            "(x0~U[-2,2]^2, T~U[2,8], r~logU[0.1,10], N~U{32..2048} intervals, m~U{3,4,5}, seed 7 + "
@@ -804,7 +922,9 @@ def main():
     # CPU baseline first: its spawned pool starts before any GPU call
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
-        cpu = _cpu_baseline(instances, cores)
+        _log("CPU baseline (oracle on %d cores)" % cores)
+        cpu = _cpu_baseline(instances, cores, family=args.family if args.workload == "warm" else "vdp")
+        _log("CPU baseline: %.3g solves/s" % cpu["value"])
     if args.workload == "warm":
         run_warm(args, cs, rank, world, local_rank, cpu, cfg)
     else:

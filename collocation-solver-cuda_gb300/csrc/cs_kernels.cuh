@@ -125,9 +125,17 @@ struct CsBatch {
   int wsp_ctas, wsp_pad;
 };
 
-#ifndef CS_BIG
-#define CS_BIG 0
+// Large-system kernels (global-memory slab per CTA): CS_BIG_COND selects
+// the blocked-LU condensation, CS_BIG_TREE the CTA-per-merge tree and the
+// CTA top solve; each is chosen when its blocks outgrow the shared-memory
+// kernels (the condensation also when a whole CTA would serve an interval).
+#ifndef CS_BIG_COND
+#define CS_BIG_COND 0
 #endif
+#ifndef CS_BIG_TREE
+#define CS_BIG_TREE 0
+#endif
+#define CS_BIG (CS_BIG_COND || CS_BIG_TREE)
 #ifndef CS_SMEM_MAX
 #define CS_SMEM_MAX 232448
 #endif
@@ -808,7 +816,7 @@ __device__ void cs_condense_group(const CsBatch& bt, int slot, bool active, doub
   if (singular && tid == 0) atomicAdd(&bt.inst[b].singular, 1);
 }
 
-#if !CS_BIG
+#if !CS_BIG_COND
 // lanes per condensation group, from the size of the stage system
 #define CS_CGL ((CS_S1 > 48) ? 256 : ((CS_S1 > 16) ? 16 : 8))
 
@@ -848,7 +856,7 @@ __device__ __forceinline__ void cs_condense_entry(const CsBatch& bt) {
 }
 
 extern "C" __global__ void k_condense(CsBatch bt) { cs_condense_entry(bt); }
-#endif  // !CS_BIG
+#endif  // !CS_BIG_COND
 
 // ------------------------------------------------------------------------
 // BABD solve, one CTA per instance: tree of pairwise QR eliminations over
@@ -1042,7 +1050,7 @@ __device__ void cs_backsub_warp(const double* rec, const double* yl, const doubl
   __syncwarp();
 }
 
-#if !CS_BIG
+#if !CS_BIG_TREE
 // One tree level for every instance that needs a Newton direction: warp per
 // item; item mi < merges eliminates node (2 mi + 1) 2^l between rows 2 mi and
 // 2 mi + 1, the last item of an odd level carries its row up unchanged.
@@ -1204,7 +1212,7 @@ extern "C" __global__ void k_top(CsBatch bt) {
   const int njac = bt.nlist[1];
   for (int k = blockIdx.x * wpc + w; k < njac; k += gridDim.x * wpc) cs_top_warp(bt, bt.jac[k], top);
 }
-#endif  // !CS_BIG
+#endif  // !CS_BIG_TREE
 
 // Back substitution of one tree level (top-down), warp per merge.
 extern "C" __global__ void k_backsub_level(CsBatch bt, int l) {
@@ -1277,7 +1285,7 @@ extern "C" __global__ void k_recover(CsBatch bt) {
   }
 }
 
-#if !CS_BIG
+#if !CS_BIG_TREE
 // The whole Newton direction of one instance in one CTA: tree levels up,
 // top system, back substitution down, stage recovery, then the line search
 // starts (alpha = 1).  One launch per super-step instead of 2 L + 3, which is
@@ -1373,7 +1381,7 @@ extern "C" __global__ void __launch_bounds__(256) k_babd_cta(CsBatch bt) {
 #else
 // not used for large stage systems (the host never launches it)
 extern "C" __global__ void k_babd_cta(CsBatch bt) {}
-#endif  // !CS_BIG
+#endif  // !CS_BIG_TREE
 
 #if CS_BIG
 // ========================================================================
@@ -1461,6 +1469,7 @@ __device__ __forceinline__ double cs_cta_sum(double v, double* red) {
   return s;
 }
 
+#if CS_BIG_COND
 // stage j: f, g at the stage point into fa, their Jacobians into the slab
 // (not inlined: the big problem functions keep their registers to
 // themselves, away from the elimination loops)
@@ -1768,6 +1777,9 @@ extern "C" __global__ void __launch_bounds__(256, 2) k_condense(CsBatch bt) {
   }
 }
 
+#endif  // CS_BIG_COND
+
+#if CS_BIG_TREE
 // Householder column k of a column-major matrix A (leading dimension ld,
 // rows k..n-1) applied to columns k+1..nc-1, CTA-wide: a warp per column,
 // lanes over rows.  Sign rule and early skip as matrix_factorization_cuda.py:37-54.
@@ -2045,7 +2057,8 @@ extern "C" __global__ void __launch_bounds__(256) k_top(CsBatch bt) {
     __syncthreads();
   }
 }
-#endif
+#endif  // CS_BIG_TREE
+#endif  // CS_BIG
 
 // ------------------------------------------------------------------------
 // Segment residual at the M+1 Gauss points (residual_type 1, with the running

@@ -271,18 +271,20 @@ struct cs_module {
   int sms = 1;
   int condense_grid = 1;
   // large stage systems: kernels with a global-memory slab per CTA
-  bool big = false;
+  bool big = false, big_cond = false, big_tree = false;
   long long slab = 0;  // doubles per CTA
   int big_ctas = 0;    // CTAs with a slab (the largest grid of the slab kernels)
   int tree_grid = 0;   // k_tree_level grid (large systems)
 };
 
-static std::string build_source(const cs_module_desc* d, bool big, int smem_max) {
+static std::string build_source(const cs_module_desc* d, bool big_cond, bool big_tree, int smem_max) {
   std::ostringstream o;
   o << "// generated prelude\n";
   o << "#define CS_NY " << d->ny << "\n#define CS_NZ " << d->nz << "\n#define CS_NP " << d->np << "\n";
   o << "#define CS_NPE " << d->np_eff << "\n#define CS_NTH " << d->n_theta << "\n#define CS_M " << d->m << "\n";
-  if (big) o << "#define CS_BIG 1\n#define CS_SMEM_MAX " << smem_max << "\n";
+  if (big_cond) o << "#define CS_BIG_COND 1\n";
+  if (big_tree) o << "#define CS_BIG_TREE 1\n";
+  if (big_cond || big_tree) o << "#define CS_SMEM_MAX " << smem_max << "\n";
   const int m = d->m;
   o << "__constant__ double CS_A[" << m * m << "] = {" << fmt_array(d->lobatto_A, m * m) << "};\n";
   o << "__constant__ double CS_B[" << m << "] = {" << fmt_array(d->lobatto_b, m) << "};\n";
@@ -372,20 +374,26 @@ extern "C" int cs_module_load(const cs_module_desc* d, cs_module** out) {
   const int nt = 2 * M->ny + M->np, tld = nt | 1;
   const size_t tree_small = (size_t)4 * qld * qc * sizeof(double);
   const size_t top_per = (size_t)tld * (nt + 1) * sizeof(double);
-  const bool fits = grp <= (size_t)smem_optin && tree_small <= (size_t)smem_optin && top_per <= (size_t)smem_optin;
-  if (d->layout == 1 && !fits) {
+  const bool fits_cond = grp <= (size_t)smem_optin;
+  const bool fits_tree = tree_small <= (size_t)smem_optin && top_per <= (size_t)smem_optin;
+  if (d->layout == 1 && !(fits_cond && fits_tree)) {
     delete M;
     return set_err(CS_ERR_INVALID, "cs_module_load: stage system of size " + std::to_string(M->s) +
                                        " does not fit in shared memory (layout 1)");
   }
-  M->big = d->layout == 2 || (d->layout == 0 && !fits);
+  // layout 0: the blocked-LU condensation whenever a whole CTA would serve
+  // one interval (measured faster from s1 = 102 on) or the system does not
+  // fit; the CTA tree kernels only when the merge or top blocks do not fit
+  M->big_cond = d->layout == 2 || (d->layout == 0 && (!fits_cond || gl > 32));
+  M->big_tree = d->layout == 2 || (d->layout == 0 && !fits_tree);
+  M->big = M->big_cond || M->big_tree;
   M->cgw = gl;
   int smem_sm = 0;
   CS_CUDA(cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev));
   CS_CUDA(cudaDeviceGetAttribute(&M->sms, cudaDevAttrMultiProcessorCount, dev));
-  if (M->big) {
-    // sizes of the large-system kernels (CS_NB .. CS_SM_TOP in cs_kernels.cuh;
-    // the kernels check what they get and report a mismatch)
+  // sizes of the large-system kernels (CS_NB .. CS_SM_TOP in cs_kernels.cuh;
+  // the kernels check what they get and report a mismatch)
+  {
     const long long nb = 16, ncol1 = s1 + M->nrhs, ldg = ((ncol1 + 3) / 4) * 4, nfg = d->ny + d->nz + d->np;
     const long long ws_cond = (long long)s1 * ldg + (long long)d->m * rb * nfg + (long long)rb * M->nrhs;
     const long long sm_cond = (long long)s1 * (nb + 1) + nb * ldg + (long long)d->m * rb + d->m * d->m + d->ny + s1 + 16 + nb;
@@ -393,50 +401,56 @@ extern "C" int cs_module_load(const cs_module_desc* d, cs_module** out) {
     const long long drsz = (long long)(d->ny + d->np) * (2 * d->ny + d->np);
     const long long hb = 16, sm_hb = hb * qld + 2 * hb * hb + hb + 32;
     const bool q_smem = (qsz + sm_hb) * 8 <= smem_optin, t_smem = (tsz + 32) * 8 <= smem_optin;
-    M->slab = std::max(ws_cond, std::max(q_smem ? 0ll : qsz, (t_smem ? 0ll : tsz) + drsz));
-    M->condense_smem = (size_t)sm_cond * 8;
-    M->tree_smem = (size_t)((q_smem ? qsz : 0) + sm_hb) * 8;
-    M->top_smem = (size_t)((t_smem ? tsz : 0) + 32) * 8;
-    if (M->condense_smem > (size_t)smem_optin) {
-      delete M;
-      return set_err(CS_ERR_INVALID, "cs_module_load: stage system of size " + std::to_string(M->s) + " too large");
+    M->slab = 0;
+    if (M->big_cond) M->slab = std::max(M->slab, ws_cond);
+    if (M->big_tree) M->slab = std::max(M->slab, std::max(q_smem ? 0ll : qsz, (t_smem ? 0ll : tsz) + drsz));
+    if (M->big_cond) {
+      M->condense_smem = (size_t)sm_cond * 8;
+      if (M->condense_smem > (size_t)smem_optin) {
+        delete M;
+        return set_err(CS_ERR_INVALID, "cs_module_load: stage system of size " + std::to_string(M->s) + " too large");
+      }
+      M->condense_block = 256;
+      M->condense_per_cta = 1;
     }
-    const int per_sm = std::max(1, std::min(8, (int)((size_t)smem_sm / (M->condense_smem + 1024))));
-    M->big_ctas = M->sms * per_sm;
-    M->condense_block = 256;
-    M->condense_per_cta = 1;
-    M->condense_grid = M->big_ctas;
-    M->top_wpc = 8;
-    M->babd_cta_smem = 0;
-  } else if (gl <= 32) {
-    // warps per CTA that maximise resident groups per SM (shared memory bound)
-    const int gpw = 32 / gl;
-    int best_w = 1;
-    long long best_groups = 0;
-    for (int w = 1; w <= 8; ++w) {
-      const size_t cta = grp * gpw * w;
-      if (cta > (size_t)smem_optin) break;
-      long long ctas = (long long)(smem_sm / (cta + 1024));
-      ctas = std::min<long long>(ctas, 64 / w);  // 64 warps per SM
-      const long long groups = ctas * w * gpw;
-      if (groups > best_groups) { best_groups = groups; best_w = w; }
+    if (M->big_tree) {
+      M->tree_smem = (size_t)((q_smem ? qsz : 0) + sm_hb) * 8;
+      M->top_smem = (size_t)((t_smem ? tsz : 0) + 32) * 8;
+      M->top_wpc = 8;
+      M->babd_cta_smem = 0;
     }
-    M->condense_per_cta = best_w * gpw;
-    M->condense_block = 32 * best_w;
-    M->condense_smem = grp * gpw * best_w;
-  } else {
-    M->condense_per_cta = 1;
-    M->condense_block = gl;
-    M->condense_smem = grp;
   }
-  if (!M->big) {
+  if (!M->big_cond) {
+    if (gl <= 32) {
+      // warps per CTA that maximise resident groups per SM (shared memory bound)
+      const int gpw = 32 / gl;
+      int best_w = 1;
+      long long best_groups = 0;
+      for (int w = 1; w <= 8; ++w) {
+        const size_t cta = grp * gpw * w;
+        if (cta > (size_t)smem_optin) break;
+        long long ctas = (long long)(smem_sm / (cta + 1024));
+        ctas = std::min<long long>(ctas, 64 / w);  // 64 warps per SM
+        const long long groups = ctas * w * gpw;
+        if (groups > best_groups) { best_groups = groups; best_w = w; }
+      }
+      M->condense_per_cta = best_w * gpw;
+      M->condense_block = 32 * best_w;
+      M->condense_smem = grp * gpw * best_w;
+    } else {
+      M->condense_per_cta = 1;
+      M->condense_block = gl;
+      M->condense_smem = grp;
+    }
+  }
+  if (!M->big_tree) {
     M->tree_smem = tree_small;
     M->top_wpc = (int)std::max<size_t>(1, std::min<size_t>(4, (size_t)smem_optin / top_per));
     M->babd_cta_smem = top_per + (size_t)8 * qld * qc * sizeof(double);
     M->top_smem = top_per * M->top_wpc;
   }
 
-  std::string src = build_source(d, M->big, smem_optin);
+  std::string src = build_source(d, M->big_cond, M->big_tree, smem_optin);
   std::string cache = d->cache_dir ? d->cache_dir : "";
   if (cache.empty()) {
     const char* env = getenv("CS_GB300_CACHE");
@@ -480,17 +494,24 @@ extern "C" int cs_module_load(const cs_module_desc* d, cs_module** out) {
     CS_CU(g_drv.funcSetAttribute(M->f_top, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, (int)M->top_smem));
   if (M->big) {
     // persistent grids from the kernels' occupancy (registers and shared memory)
-    int pc = 0, pt = 0;
-    CS_CU(g_drv.occupancy(&pc, M->f_condense, 256, M->condense_smem));
-    CS_CU(g_drv.occupancy(&pt, M->f_tree_level, 256, M->tree_smem));
-    M->condense_grid = M->sms * std::max(1, pc);
-    M->tree_grid = M->sms * std::max(1, pt);
-    M->big_ctas = std::max(M->condense_grid, M->tree_grid);
+    M->big_ctas = 0;
+    if (M->big_cond) {
+      int pc = 0;
+      CS_CU(g_drv.occupancy(&pc, M->f_condense, 256, M->condense_smem));
+      M->condense_grid = M->sms * std::max(1, pc);
+      M->big_ctas = std::max(M->big_ctas, M->condense_grid);
+    }
+    if (M->big_tree) {
+      int pt = 0;
+      CS_CU(g_drv.occupancy(&pt, M->f_tree_level, 256, M->tree_smem));
+      M->tree_grid = M->sms * std::max(1, pt);
+      M->big_ctas = std::max(M->big_ctas, M->tree_grid);
+    }
   }
   if (M->babd_cta_smem > (size_t)smem_optin) M->babd_cta_smem = 0;  // per-level kernels only
   else if (M->babd_cta_smem > 48 * 1024)
     CS_CU(g_drv.funcSetAttribute(M->f_babd_cta, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, (int)M->babd_cta_smem));
-  if (!M->big) {
+  if (!M->big_cond) {
     // resident CTAs of the condensation kernel per SM, for its persistent grid
     int smem_sm2 = 0;
     CS_CUDA(cudaDeviceGetAttribute(&smem_sm2, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev));
@@ -787,12 +808,12 @@ static int run_direction(cs_batch* bt, CsBatchDev& v, int nlvl) {
   const unsigned g = (unsigned)(M->sms * 8);
   for (int l = 0; l < nlvl; ++l) {
     void* a[] = {&v, &l};
-    if (M->big) CS_TRY(launch_k(bt, M->f_tree_level, (unsigned)M->tree_grid, 256, M->tree_smem, a, 1));
+    if (M->big_tree) CS_TRY(launch_k(bt, M->f_tree_level, (unsigned)M->tree_grid, 256, M->tree_smem, a, 1));
     else CS_TRY(launch_k(bt, M->f_tree_level, g, 128, M->tree_smem, a, 1));
   }
   {
     void* a[] = {&v};
-    if (M->big) CS_TRY(launch_k(bt, M->f_top, (unsigned)std::min(M->big_ctas, bt->B), 256, M->top_smem, a, 1));
+    if (M->big_tree) CS_TRY(launch_k(bt, M->f_top, (unsigned)std::min(M->big_ctas, bt->B), 256, M->top_smem, a, 1));
     else CS_TRY(launch_k(bt, M->f_top, (unsigned)(M->sms * 4), 32 * M->top_wpc, M->top_smem, a, 1));
   }
   for (int l = nlvl - 1; l >= 0; --l) {

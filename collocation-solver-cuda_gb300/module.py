@@ -33,7 +33,7 @@ def _tables(m):
 def kernel_program_text(problem, m, big=False, smem_max=232448):
     """The NVRTC program for (problem, m) as one CUDA source (used for nvcc
     compile checks; the library builds the same text at run time).  big:
-    the large-system kernels."""
+    the large-system kernels (condensation and tree)."""
     pc = ProblemCode(problem.sym)
     t = _tables(m)
 
@@ -43,7 +43,7 @@ def kernel_program_text(problem, m, big=False, smem_max=232448):
     out = "#define CS_NY %d\n#define CS_NZ %d\n#define CS_NP %d\n#define CS_NPE %d\n#define CS_NTH %d\n#define CS_M %d\n" % (
         pc.ny, pc.nz, pc.np, pc.np_eff, pc.nth, m)
     if big:
-        out += "#define CS_BIG 1\n#define CS_SMEM_MAX %d\n" % smem_max
+        out += "#define CS_BIG_COND 1\n#define CS_BIG_TREE 1\n#define CS_SMEM_MAX %d\n" % smem_max
     out += arr("CS_A", t["A"]) + arr("CS_B", t["b"]) + arr("CS_C", t["c"]) + arr("CS_GW", t["gw"])
     out += arr("CS_GL", t["gL"]) + arr("CS_GI", t["gI"]) + arr("CS_L0", t["L0"]) + arr("CS_L1", t["L1"])
     out += cuda_problem_source(pc)

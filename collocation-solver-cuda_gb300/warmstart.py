@@ -144,18 +144,40 @@ def vdp_family():
                   theta=lambda i: i.theta, final_time=lambda i: i.T, plain_guess=lambda i: i.guess(), name="vdp")
 
 
+def pendulum_family(K=8):
+    """Pendulum chain of K: features theta(0), T, k."""
+    from .workloads import pendulum_family_problem
+    pr = pendulum_family_problem(K)
+    ny, nz, npar = pr.size_y, pr.size_z, pr.size_p
+    return Family(pr, features=lambda i: np.concatenate([i.theta0, [i.T, i.k]]), theta=lambda i: i.theta,
+                  final_time=lambda i: i.T, plain_guess=lambda i: i.guess(ny, nz, npar), name="pendulum%d" % K)
+
+
+def pack_family(family, instances):
+    """Packed host arrays (N, t, y, z, p, theta) of the plain guesses."""
+    parts = [family.plain_guess(i) for i in instances]
+    N = np.array([len(p[0]) for p in parts], dtype=np.int32)
+    t = np.concatenate([p[0] for p in parts])
+    y = np.concatenate([p[1] for p in parts])
+    z = np.concatenate([p[2] for p in parts]) if family.nz else np.zeros((int(N.sum()), 0))
+    p = np.array([pp[3] for pp in parts]).reshape(len(instances), -1)
+    th = np.array([family.theta(i) for i in instances]).reshape(len(instances), -1)
+    return N, t, y, z, p, th
+
+
 class BatchSolver:
     """Solves lists of instances of a family in one batch per m; compiled
     problems are kept per m."""
 
-    def __init__(self, family, opts=None):
+    def __init__(self, family, opts=None, layout=0):
         self.family = family
         self.compiled = {}
+        self.layout = layout
         self.opts = opts if opts is not None else default_opts(family.problem, max_nodes=20000)
 
     def cp(self, m):
         if m not in self.compiled:
-            self.compiled[m] = CompiledProblem(self.family.problem, m)
+            self.compiled[m] = CompiledProblem(self.family.problem, m, layout=self.layout)
         return self.compiled[m]
 
     def solve(self, instances, guesses=None):
@@ -269,6 +291,7 @@ class WarmRunner:
             if warm:
                 bt.warm_start(self.dY.ptr + 4 * g["first"] * self.mlp.n_out, N_NODES, self.mlp.n_out)
             bt.solve(self.solver.opts)
+            g["t_solve"] = time.perf_counter() - t1
             g["sols"] = bt.solution()
             g["fallback"] = []
             if warm and fallback:
@@ -280,6 +303,7 @@ class WarmRunner:
                     for k, s in zip(failed, plain):
                         g["sols"][k] = dict(s, fallback=True)
                     g["fallback"] = failed
+            g["t_done"] = time.perf_counter() - t1
 
         if threads:
             ths = [threading.Thread(target=one, args=(g,)) for g in self.groups]
@@ -296,6 +320,7 @@ class WarmRunner:
         for g in self.groups:
             sols += g["sols"]
             n_fb += len(g["fallback"])
-        self.times = {"predict_s": t1 - t0, "solve_and_fallback_s": t2 - t1}
+        self.times = {"predict_s": t1 - t0, "solve_and_fallback_s": t2 - t1,
+                      "groups": [(g["m"], round(g["t_solve"], 4), round(g["t_done"], 4)) for g in self.groups]}
         solved = sum(int(s["success"]) for s in sols)
         return solved, n_fb, sols

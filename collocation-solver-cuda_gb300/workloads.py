@@ -70,6 +70,50 @@ def pack_vdp(instances, ny=4, nz=1, np_=2):
     return Ns, t, y, z, p, th
 
 
+class PendulumInstance:
+    """One instance of the pendulum-chain family: initial angles theta0 (K),
+    final time T, coupling k, mesh intervals and m."""
+    __slots__ = ("theta0", "T", "k", "intervals", "m")
+
+    def __init__(self, theta0, T, k, intervals, m):
+        self.theta0, self.T, self.k, self.intervals, self.m = theta0, T, k, intervals, m
+
+    @property
+    def theta(self):
+        """Instance constants in the OCP's order: kc, a1 .. aK."""
+        return np.concatenate([[self.k], self.theta0])
+
+    def guess(self, ny, nz, np_):
+        """theta_i(t) = theta_i(0) (1 - t/T), every other value 0, p = 1."""
+        N = self.intervals + 1
+        t = np.linspace(0.0, self.T, N)
+        y = np.zeros((N, ny))
+        K = len(self.theta0)
+        y[:, :K] = self.theta0[None, :] * (1.0 - t / self.T)[:, None]
+        return t, y, np.zeros((N, nz)), np.ones(np_)
+
+
+def pendulum_family_problem(K=8, max_nodes=20000):
+    """The pendulum chain with kc and the initial angles as instance
+    constants (the final time comes from each instance's mesh)."""
+    pr = Problem(pendulum_ocp(K, np.zeros(K), max_nodes=max_nodes), name="pendulum%d_family" % K)
+    pr.maximum_nodes = max_nodes
+    return pr
+
+
+def pendulum_batch(n, K=8, seed=1, n_range=(32, 128), m_choices=(4,), theta_range=0.5, T_range=(5.0, 15.0),
+                   k_range=(0.2, 1.0)):
+    """n seeded instances of the pendulum-chain family: theta(0) ~ U[-0.5,0.5]^K,
+    T ~ U[5,15], coupling k ~ U[0.2,1.0]."""
+    rng = np.random.default_rng(seed)
+    th = rng.uniform(-theta_range, theta_range, (n, K))
+    T = rng.uniform(T_range[0], T_range[1], n)
+    k = rng.uniform(k_range[0], k_range[1], n)
+    N = rng.integers(n_range[0], n_range[1] + 1, n)
+    m = rng.choice(np.array(m_choices), n)
+    return [PendulumInstance(th[i], float(T[i]), float(k[i]), int(N[i]), int(m[i])) for i in range(n)]
+
+
 def pendulum_ocp(K, theta0, T=10.0, k=0.5, nodes=101, actuated_every=4, ctrl_weight=0.1, tol=1e-6,
                  max_nodes=40000):
     """OCP text for a chain of K pendulums with free ends."""

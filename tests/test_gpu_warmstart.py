@@ -34,3 +34,78 @@ def test_warm_start_gains_over_plain_guess():
     for s in final:
         if s["success"]:
             assert s["last_norm"] < 1e-6 and s["max_residual"] <= 1.0
+
+
+def _family(cs, name):
+    ws = cs.warmstart
+    return ws.vdp_family() if name == "vdp" else ws.pendulum_family(8)
+
+
+def _instances(cs, name, n, seed, n_range):
+    if name == "vdp":
+        return cs.workloads.vdp_batch(n, seed=seed, n_range=n_range, m_choices=(4,))
+    return cs.workloads.pendulum_batch(n, K=8, seed=seed, n_range=n_range)
+
+
+@pytest.mark.parametrize("name", ["vdp", "pendulum8"])
+def test_device_warm_fill_matches_host_interpolation(name):
+    """The device fill (trajectory vectors -> y, z at the mesh nodes, p,
+    then the stage values) equals the host interpolation followed by the
+    oracle's initial input, for both families."""
+    from conftest import OracleProblem
+    from oracle import collocation_oracle as O
+    cs = pkg()
+    ws = cs.warmstart
+    fam = _family(cs, name)
+    insts = _instances(cs, name, 5, 3, (20, 60))
+    m = 4
+    cp = cs.CompiledProblem(fam.problem, m)
+    bt = cs.Batch(cp, len(insts))
+    N, t, y, z, p, th = ws.pack_family(fam, insts)
+    bt.set_guess_packed(N, t, y, z, p, th)
+    V = np.random.default_rng(1).standard_normal((len(insts), fam.n_out)).astype(np.float32)
+    d = cs.module.DeviceArray(V.shape, np.float32)
+    d.upload(V)
+    bt.warm_start(d.ptr, ws.N_NODES, fam.n_out)
+    st = bt.state()
+    P = OracleProblem(fam.problem)
+    rk = cs.tables.lobatto(m)
+    off = 0
+    for b, inst in enumerate(insts):
+        n = int(N[b])
+        tb = t[off:off + n]
+        yh, zh, ph = ws.guess_from_vector(V[b].astype(np.float64), tb, fam.final_time(inst), fam.ny, fam.nz, fam.np)
+        np.testing.assert_allclose(st["y"][off:off + n], yh, rtol=0, atol=1e-12 * max(1.0, np.abs(yh).max()))
+        np.testing.assert_allclose(st["z"][off:off + n], zh, rtol=0, atol=1e-12 * max(1.0, np.abs(zh).max()))
+        np.testing.assert_array_equal(st["p"][b], ph)
+        P.theta = fam.theta(inst)
+        _, yd, zt = O.form_initial_input(P, m, n, st["y"][off:off + n], st["z"][off:off + n], st["p"][b], rk)
+        np.testing.assert_allclose(st["ydot"][off:off + n - 1].reshape(-1, fam.ny), yd, rtol=1e-12,
+                                   atol=1e-12 * max(1.0, np.abs(yd).max()))
+        off += n
+
+
+def test_pendulum_family_warm_start_gains_over_plain_guess():
+    """The second warm-start family (pendulum chain K = 8, theta(0), T and the
+    coupling as parameters): fewer Newton steps than the plain guess, no
+    instance lost."""
+    cs = pkg()
+    ws = cs.warmstart
+    fam = ws.pendulum_family(8)
+    solver = ws.BatchSolver(fam)
+    train = cs.workloads.pendulum_batch(1024, K=8, seed=1000, n_range=(32, 64))
+    held = cs.workloads.pendulum_batch(128, K=8, seed=7, n_range=(32, 64))
+    X, Y, _ = ws.training_set(fam, solver, train)
+    assert len(X) > 900
+    net = ws.Mlp(X.shape[1], Y.shape[1], width=256, depth=4, seed=0)
+    net.fit_normalization(X, Y)
+    net.train(X, Y, epochs=200, batch=256, lr=1e-3, seed=0)
+    plain = solver.solve(held)
+    final, fb, warm = ws.solve_warm(fam, solver, net, held)
+    assert all(f["success"] or not p["success"] for p, f in zip(plain, final))
+    newton_plain = np.mean([s["newton_steps"] for s in plain])
+    newton_warm = np.mean([s["newton_steps"] for s in warm])
+    assert newton_warm < newton_plain, (newton_warm, newton_plain)
+    for s in final:
+        if s["success"]:
+            assert s["last_norm"] < 1e-6 and s["max_residual"] <= 1.0
