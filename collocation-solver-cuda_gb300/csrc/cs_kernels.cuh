@@ -1663,42 +1663,32 @@ __device__ void cs_condense_big(const CsBatch& bt, int slot, double* slab, doubl
       }
     }
     __syncthreads();
-    // trailing update A22 -= L21 U12: warp items of 4 rows x 128 columns,
-    // lane owns columns lane + 32 q
+    // trailing update A22 -= L21 U12: warp items of 16 rows x 32 columns,
+    // lane owns one column (fills the lanes for any trailing width)
     const int r0 = k0 + kb, nr = CS_S1 - r0;
     if (nr > 0 && ncol > 0) {
-      const int rt = (nr + 3) >> 2, ct = (ncol + 127) >> 7;
+      const int rt = (nr + 15) >> 4, ct = (ncol + 31) >> 5;
       const int lane = tid & 31, w = tid >> 5, nw = nt >> 5;
       for (int item = w; item < rt * ct; item += nw) {
         const int ri = item / ct, ci = item - ri * ct;
-        const int ra = ri * 4, cb = ci * 128 + lane;
-        double acc[4][4];
+        const int ra = ri * 16, c = ci * 32 + lane;
+        const bool cok = c < ncol;
+        double acc[16];
 #pragma unroll
-        for (int i = 0; i < 4; ++i)
-#pragma unroll
-          for (int q = 0; q < 4; ++q) {
-            const int r = ra + i, c = cb + 32 * q;
-            acc[i][q] = (r < nr && c < ncol) ? W[(size_t)(r0 + r) * CS_LDG + c0 + c] : 0.0;
-          }
+        for (int i = 0; i < 16; ++i)
+          acc[i] = (cok && ra + i < nr) ? W[(size_t)(r0 + ra + i) * CS_LDG + c0 + c] : 0.0;
 #pragma unroll 2
         for (int l = 0; l < kb; ++l) {
-          double lv[4], uv[4];
+          const double uv = cok ? U[l * CS_LDG + c] : 0.0;
 #pragma unroll
-          for (int i = 0; i < 4; ++i) lv[i] = (ra + i < nr) ? P[(kb + ra + i) * CS_PLD + l] : 0.0;
-#pragma unroll
-          for (int q = 0; q < 4; ++q) uv[q] = (cb + 32 * q < ncol) ? U[l * CS_LDG + cb + 32 * q] : 0.0;
-#pragma unroll
-          for (int i = 0; i < 4; ++i)
-#pragma unroll
-            for (int q = 0; q < 4; ++q) acc[i][q] = fma(-lv[i], uv[q], acc[i][q]);
+          for (int i = 0; i < 16; ++i) {
+            const double lv = (ra + i < nr) ? P[(kb + ra + i) * CS_PLD + l] : 0.0;
+            acc[i] = fma(-lv, uv, acc[i]);
+          }
         }
 #pragma unroll
-        for (int i = 0; i < 4; ++i)
-#pragma unroll
-          for (int q = 0; q < 4; ++q) {
-            const int r = ra + i, c = cb + 32 * q;
-            if (r < nr && c < ncol) W[(size_t)(r0 + r) * CS_LDG + c0 + c] = acc[i][q];
-          }
+        for (int i = 0; i < 16; ++i)
+          if (cok && ra + i < nr) W[(size_t)(r0 + ra + i) * CS_LDG + c0 + c] = acc[i];
       }
     }
     __syncthreads();

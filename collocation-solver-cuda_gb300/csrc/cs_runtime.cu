@@ -410,7 +410,9 @@ extern "C" int cs_module_load(const cs_module_desc* d, cs_module** out) {
         delete M;
         return set_err(CS_ERR_INVALID, "cs_module_load: stage system of size " + std::to_string(M->s) + " too large");
       }
-      M->condense_block = 256;
+      // small stage systems: CTAs of 128 (four per SM overlap the serial
+      // panel phases of one another)
+      M->condense_block = (s1 <= 128) ? 128 : 256;
       M->condense_per_cta = 1;
     }
     if (M->big_tree) {
@@ -497,7 +499,7 @@ extern "C" int cs_module_load(const cs_module_desc* d, cs_module** out) {
     M->big_ctas = 0;
     if (M->big_cond) {
       int pc = 0;
-      CS_CU(g_drv.occupancy(&pc, M->f_condense, 256, M->condense_smem));
+      CS_CU(g_drv.occupancy(&pc, M->f_condense, M->condense_block, M->condense_smem));
       M->condense_grid = M->sms * std::max(1, pc);
       M->big_ctas = std::max(M->big_ctas, M->condense_grid);
     }
