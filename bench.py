@@ -856,13 +856,38 @@ def main():
         # one Newton direction of the large instance (for ncu)
         cs = _pkg()
         cs.build.build_library()
+        lib = cs._lib.load()
         pr = pendulum_problem(cs, args.pendulum)
         cp = cs.CompiledProblem(pr, PENDULUM[args.pendulum]["m"])
         bt = cs.Batch(cp, 1)
         bt.set_guess([(np.asarray(pr.T0, float), np.asarray(pr.Y0, float), np.asarray(pr.Z0, float))],
                      np.asarray(pr.P0, float).reshape(1, -1))
+        cs._lib.check(lib.cs_profiler_start(), "cs_profiler_start")
         out = bt.stage_newton_direction(0.1)
+        cs._lib.check(lib.cs_profiler_stop(), "cs_profiler_stop")
         print("profile case ok", float(np.abs(out["dy"]).max()))
+        return
+    if args.profile_case and args.workload == "warm":
+        # one warm-started batch solve (2048 held-out instances, MLP trained on
+        # 2048 solutions) inside the profiler range (cs_profiler_start/stop)
+        cs = _pkg()
+        cs.build.build_library()
+        lib = cs._lib.load()
+        ws = cs.warmstart
+        fam = _family(cs, args.family)
+        solver = ws.BatchSolver(fam, cs.default_opts(fam.problem, max_nodes=20000), layout=args.layout)
+        X, Y, _ = ws.training_set(fam, solver, _family_batch(cs, args.family, 2048, 1000, train=True))
+        net = ws.Mlp(X.shape[1], Y.shape[1], width=256, depth=4, seed=0)
+        net.fit_normalization(X, Y)
+        net.train(X, Y, epochs=60, batch=1024, lr=1e-3, seed=0)
+        runner = ws.WarmRunner(fam, solver, net, _family_batch(cs, args.family, 2048, 7))
+        # the m-groups one after another on this thread (profilers serialise
+        # kernels anyway, and a single host thread keeps the capture simple)
+        runner.run(warm=True, threads=False)
+        cs._lib.check(lib.cs_profiler_start(), "cs_profiler_start")
+        solved, n_fb, _ = runner.run(warm=True, threads=False)
+        cs._lib.check(lib.cs_profiler_stop(), "cs_profiler_stop")
+        print("profile case ok: solved %d of 2048, %d fallbacks" % (solved, n_fb))
         return
     if args.profile_case:
         cs = _pkg()

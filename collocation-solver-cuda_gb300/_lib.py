@@ -69,6 +69,8 @@ SIGNATURES = {
     "cs_last_error": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_size_t]),
     "cs_time_condense": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _dp]),
     "cs_measure_fp64_peak": (ctypes.c_int, [_dp]),
+    "cs_profiler_start": (ctypes.c_int, []),
+    "cs_profiler_stop": (ctypes.c_int, []),
     "cs_batch_reset": (ctypes.c_int, [ctypes.c_void_p]),
     "cs_profile_reset": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "cs_profile_get": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Profile)]),

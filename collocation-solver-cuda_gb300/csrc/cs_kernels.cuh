@@ -66,7 +66,8 @@
 // Line-search trials evaluated in one super-step once the first trial of a
 // direction was rejected (alpha, alpha/2, ...; the decision walks them in
 // order, so the accepted trial and every count are the sequential ones).
-#define CS_LSW 8
+// Their norms live in CsBatch::trials ([B][CS_LSW]).
+#define CS_LSW 20
 
 struct CsInst {
   int status, it, ls_it, alphacal;
@@ -75,7 +76,6 @@ struct CsInst {
   int iter_time, singular, ntrial, ls_prev;   // trials of the next residual evaluation; rejected trials of the last line search
   double alpha_ls, norm_x, alpha, max_res;
   unsigned long long norm_bits, res_bits;
-  unsigned long long trial_bits[CS_LSW - 1];  // norms of trials 1 .. ntrial-1
 };
 
 struct CsConsts {
@@ -119,6 +119,7 @@ struct CsBatch {
   long long* acc_pre;       // [B+1] prefix of node counts
   long long* lvl_pre;       // [CS_MAXLVL][B+1] prefix of tree items per level over jac
   int* nlist;               // [4] nact, njac, nacc, -
+  unsigned long long* trials;  // [B][CS_LSW] residual norms of line-search trials 1.. (bits)
   // large stage systems (CS_BIG): a slab of global memory per CTA
   double* wsp;              // [wsp_ctas][wsp_stride]
   long long wsp_stride;     // doubles per CTA
@@ -328,7 +329,7 @@ extern "C" __global__ void k_residual(CsBatch bt) {
     }
 
     unsigned long long* dst = nullptr;
-    if (active) dst = trial == 0 ? &bt.inst[b].norm_bits : &bt.inst[b].trial_bits[trial - 1];
+    if (active) dst = trial == 0 ? &bt.inst[b].norm_bits : &bt.trials[(size_t)b * CS_LSW + trial];
     cs_warp_max_atomic(dst, b * CS_LSW + trial, nb, active);
   }
 }
@@ -374,7 +375,7 @@ extern "C" __global__ void k_decide(CsBatch bt, CsConsts c) {
       // trials in the reference's order: alpha_ls, alpha_ls/2, ...
       bool done = false;
       for (int j = 0; j < ntr && !done; ++j) {
-        const double ntj = (j == 0) ? nt : cs_from_bits(s.trial_bits[j - 1]);
+        const double ntj = (j == 0) ? nt : cs_from_bits(bt.trials[(size_t)b * CS_LSW + j]);
         if (j > 0) s.residual_count += 1;
         if (ntj < s.norm_x) {
           s.accepted = 1;
@@ -403,7 +404,7 @@ extern "C" __global__ void k_decide(CsBatch bt, CsConsts c) {
           done = true;
         }
       }
-      for (int j = 0; j < CS_LSW - 1; ++j) s.trial_bits[j] = 0ull;
+      for (int j = 1; j < ntr; ++j) bt.trials[(size_t)b * CS_LSW + j] = 0ull;
       // still searching: the next super-step evaluates several trials
       if (!done) s.ntrial = min(CS_LSW, c.max_ls - s.ls_it);
     }
@@ -1291,7 +1292,7 @@ extern "C" __global__ void k_recover(CsBatch bt) {
 // starts (alpha = 1).  One launch per super-step instead of 2 L + 3, which is
 // what matters when few instances are left; used for batches of small and
 // medium instances (the per-level kernels above serve large single ones).
-extern "C" __global__ void __launch_bounds__(256) k_babd_cta(CsBatch bt) {
+extern "C" __global__ void __launch_bounds__(256) k_babd_cta(CsBatch bt, int recover) {
   extern __shared__ double smem[];
   const int nw = blockDim.x >> 5, w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   double* top = smem;                                  // CS_TLD x (CS_NT + 1)
@@ -1360,8 +1361,9 @@ extern "C" __global__ void __launch_bounds__(256) k_babd_cta(CsBatch bt) {
 #endif
       __syncthreads();
     }
-    // ---- stage recovery, warp per interval, lanes over stage rows
-    for (int iv = w; iv < n0; iv += nw) {
+    // ---- stage recovery, warp per interval, lanes over stage rows (or by
+    //      k_recover across the GPU when recover == 0)
+    for (int iv = w; recover && iv < n0; iv += nw) {
       const int slot = off + iv;
       const double* X = bt.X + (size_t)slot * CS_NRHS * CS_S;
       const double* dyi = bt.dy + (size_t)slot * CS_NY;
@@ -1380,7 +1382,7 @@ extern "C" __global__ void __launch_bounds__(256) k_babd_cta(CsBatch bt) {
 
 #else
 // not used for large stage systems (the host never launches it)
-extern "C" __global__ void k_babd_cta(CsBatch bt) {}
+extern "C" __global__ void k_babd_cta(CsBatch bt, int recover) {}
 #endif  // !CS_BIG_TREE
 
 #if CS_BIG

@@ -11,6 +11,7 @@
 // runs the mesh phase (segment residual, remesh with repacking) between
 // Newton phases.
 #include <cuda.h>
+#include <cuda_profiler_api.h>
 #include <cuda_runtime.h>
 #include <nvrtc.h>
 
@@ -84,7 +85,7 @@ const char* drv_err(CUresult r) {
   } while (0)
 
 // Must match struct CsInst in cs_kernels.cuh.
-static const int CS_LSW = 8;  // line-search trials per super-step (cs_kernels.cuh)
+static const int CS_LSW = 20;  // line-search trials per super-step (cs_kernels.cuh)
 struct CsInst {
   int status, it, ls_it, alphacal;
   int need_jac, accepted, fail_reason, N_new;
@@ -92,9 +93,8 @@ struct CsInst {
   int iter_time, singular, ntrial, ls_prev;
   double alpha_ls, norm_x, alpha, max_res;
   unsigned long long norm_bits, res_bits;
-  unsigned long long trial_bits[CS_LSW - 1];
 };
-static_assert(sizeof(CsInst) == 168, "CsInst layout");
+static_assert(sizeof(CsInst) == 112, "CsInst layout");
 
 struct CsConsts {
   double tol, alpha_m, beta;
@@ -135,6 +135,7 @@ struct CsBatchDev {
   long long* acc_pre;
   long long* lvl_pre;
   int* nlist;
+  unsigned long long* trials;
   double* wsp;
   long long wsp_stride;
   int wsp_ctas, wsp_pad;
@@ -561,7 +562,7 @@ struct cs_batch {
   bool own_stream = false;
   bool have_guess = false;
   // per instance
-  DBuf dN, doff, doff2, dp, dth, ddp, dinst, dcounters;
+  DBuf dN, doff, doff2, dp, dth, ddp, dinst, dcounters, dtrials;
   // per slot (set 0 / set 1 for the arrays a remesh rewrites)
   DBuf t[2], y[2], ydot[2], zt[2], znode[2];
   int cur = 0;
@@ -572,11 +573,13 @@ struct cs_batch {
   // work lists
   DBuf l_act, l_jac, l_acc, l_actp, l_jacp, l_accp, l_lvlp, l_n;
   int* h_n = nullptr;  // pinned copy of nlist
-  // captured super-step
-  cudaGraphExec_t graph = nullptr;
-  int graph_nlvl = -1;
-  CsBatchDev graph_view;
-  CsConsts graph_consts;
+  // captured super-step, one graph per Newton-direction path (0 per level,
+  // 1 one CTA per instance)
+  cudaGraphExec_t graph[2] = {nullptr, nullptr};
+  int graph_nlvl[2] = {-1, -1};
+  CsBatchDev graph_view[2];
+  CsConsts graph_consts[2];
+  int cta_now = -1;  // automatic path choice of the running solve (-1: none)
   // device copy of the last initial guess (cs_batch_reset)
   DBuf iN, ioff, it, iy, iz, ip;
   std::vector<int> ihN, ihoff;
@@ -695,6 +698,7 @@ static CsBatchDev devview(cs_batch* bt) {
   v.acc_pre = (long long*)bt->l_accp.p;
   v.lvl_pre = (long long*)bt->l_lvlp.p;
   v.nlist = (int*)bt->l_n.p;
+  v.trials = (unsigned long long*)bt->dtrials.p;
   if (bt->M->big) {
     v.wsp = (double*)bt->wsp.p;
     v.wsp_stride = bt->M->slab;
@@ -789,6 +793,7 @@ static bool use_cta_path(const cs_batch* bt) {
   if (bt->M->babd_cta_smem == 0) return false;
   if (bt->opts.babd_path == 1) return true;
   if (bt->opts.babd_path == 2) return false;
+  if (bt->cta_now >= 0) return bt->cta_now != 0;
   int mx = 0;
   for (int n : bt->hN) mx = std::max(mx, n);
   return bt->B <= 8 && mx <= 1024;
@@ -804,8 +809,11 @@ static int run_lists(cs_batch* bt, CsBatchDev& v, int mode, int nlvl) {
 static int run_direction(cs_batch* bt, CsBatchDev& v, int nlvl) {
   cs_module* M = bt->M;
   if (use_cta_path(bt)) {
-    void* a[] = {&v};
-    return launch_k(bt, M->f_babd_cta, (unsigned)(M->sms * 2), 256, M->babd_cta_smem, a, 1);
+    int recover = 0;
+    void* a[] = {&v, &recover};
+    CS_TRY(launch_k(bt, M->f_babd_cta, (unsigned)(M->sms * 2), 256, M->babd_cta_smem, a, 1));
+    void* ar[] = {&v};
+    return launch_k(bt, M->f_recover, (unsigned)(M->sms * 8), 128, 0, ar, 1);
   }
   const unsigned g = (unsigned)(M->sms * 8);
   for (int l = 0; l < nlvl; ++l) {
@@ -871,6 +879,7 @@ extern "C" int cs_batch_create(cs_module* M, int batch, long long node_capacity,
       (rc = dalloc(bt->ddp, batch * std::max(M->np, 1) * d)) ||
       (rc = dalloc(bt->dth, batch * std::max(M->nth, 1) * d)) || (rc = dalloc(bt->dinst, batch * sizeof(CsInst))) ||
       (rc = dalloc(bt->dcounters, 64)) || (rc = dalloc(bt->l_act, batch * sizeof(int))) ||
+      (rc = dalloc(bt->dtrials, (size_t)batch * CS_LSW * sizeof(unsigned long long))) ||
       (rc = dalloc(bt->l_jac, batch * sizeof(int))) || (rc = dalloc(bt->l_acc, batch * sizeof(int))) ||
       (rc = dalloc(bt->l_actp, (batch + 1) * sizeof(long long))) ||
       (rc = dalloc(bt->l_jacp, (batch + 1) * sizeof(long long))) ||
@@ -883,6 +892,7 @@ extern "C" int cs_batch_create(cs_module* M, int batch, long long node_capacity,
     return rc;
   }
   if (cudaMemsetAsync(bt->dcounters.p, 0, 64, bt->stream) != cudaSuccess ||
+      cudaMemsetAsync(bt->dtrials.p, 0, (size_t)batch * CS_LSW * sizeof(unsigned long long), bt->stream) != cudaSuccess ||
       cudaStreamSynchronize(bt->stream) != cudaSuccess) {
     cs_batch_free(bt);
     return set_err(CS_ERR_CUDA, "cs_batch_create: counter reset failed");
@@ -894,12 +904,13 @@ extern "C" int cs_batch_create(cs_module* M, int batch, long long node_capacity,
 extern "C" void cs_batch_free(cs_batch* bt) {
   if (!bt) return;
   if (bt->stream) cudaStreamSynchronize(bt->stream);
-  DBuf* all[] = {&bt->dN, &bt->doff, &bt->doff2, &bt->dp, &bt->dth, &bt->ddp, &bt->dinst, &bt->dcounters,
+  DBuf* all[] = {&bt->dN, &bt->doff, &bt->doff2, &bt->dp, &bt->dth, &bt->ddp, &bt->dinst, &bt->dcounters, &bt->dtrials,
                  &bt->inst_of, &bt->dy, &bt->dydot, &bt->dzt, &bt->X, &bt->rows0, &bt->rows1, &bt->tree, &bt->res,
                  &bt->iN, &bt->ioff, &bt->it, &bt->iy, &bt->iz, &bt->ip, &bt->l_act, &bt->l_jac, &bt->l_acc,
                  &bt->l_actp, &bt->l_jacp, &bt->l_accp, &bt->l_lvlp, &bt->l_n, &bt->wsp};
   for (DBuf* b : all) dfree(*b);
-  if (bt->graph) cudaGraphExecDestroy(bt->graph);
+  for (int k = 0; k < 2; ++k)
+    if (bt->graph[k]) cudaGraphExecDestroy(bt->graph[k]);
   if (bt->h_n) cudaFreeHost(bt->h_n);
   for (auto& e : bt->ev_pool) {
     cudaEventDestroy(e.a);
@@ -1062,12 +1073,13 @@ static int super_step(cs_batch* bt, const CsConsts& c, int nlvl) {
 // a remesh changes the buffers).
 static int get_graph(cs_batch* bt, const CsConsts& c, int nlvl, int reps) {
   const CsBatchDev v = devview(bt);
-  if (bt->graph && bt->graph_nlvl == nlvl && memcmp(&bt->graph_view, &v, sizeof(v)) == 0 &&
-      memcmp(&bt->graph_consts, &c, sizeof(c)) == 0)
+  const int k = use_cta_path(bt) ? 1 : 0;
+  if (bt->graph[k] && bt->graph_nlvl[k] == nlvl && memcmp(&bt->graph_view[k], &v, sizeof(v)) == 0 &&
+      memcmp(&bt->graph_consts[k], &c, sizeof(c)) == 0)
     return CS_OK;
-  if (bt->graph) {
-    cudaGraphExecDestroy(bt->graph);
-    bt->graph = nullptr;
+  if (bt->graph[k]) {
+    cudaGraphExecDestroy(bt->graph[k]);
+    bt->graph[k] = nullptr;
   }
   cudaGraph_t g = nullptr;
   CS_CUDA(cudaStreamBeginCapture(bt->stream, cudaStreamCaptureModeThreadLocal));
@@ -1082,12 +1094,12 @@ static int get_graph(cs_batch* bt, const CsConsts& c, int nlvl, int reps) {
     return rc;
   }
   if (e != cudaSuccess) return set_err(CS_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
-  e = cudaGraphInstantiate(&bt->graph, g, 0);
+  e = cudaGraphInstantiate(&bt->graph[k], g, 0);
   cudaGraphDestroy(g);
   if (e != cudaSuccess) return set_err(CS_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
-  bt->graph_view = v;
-  bt->graph_consts = c;
-  bt->graph_nlvl = nlvl;
+  bt->graph_view[k] = v;
+  bt->graph_consts[k] = c;
+  bt->graph_nlvl[k] = nlvl;
   return CS_OK;
 }
 
@@ -1157,19 +1169,26 @@ extern "C" int cs_solve(cs_batch* bt, const cs_opts* opts) {
   const long long max_super = 10000000;
   long long steps = 0;
   const int per_launch_steps = 1;
+  // automatic Newton-direction path: per-level kernels while many instances
+  // iterate, one CTA per instance once at most one SM's worth of them is left
+  // (the per-level path then costs ~2 nlvl dependent launches per super-step)
+  const bool auto_path = o.babd_path == 0 && bt->M->babd_cta_smem > 0;
+  const int cta_max = bt->M->sms;
+  if (auto_path) bt->cta_now = bt->B <= cta_max ? 1 : 0;
   for (int outer = 0; outer < 1000000 && rc == CS_OK; ++outer) {
     // ---- Newton phase: device state machine, work lists, graph replays
     const int nlvl = tree_levels(bt);
     CsBatchDev v0 = devview(bt);
     if ((rc = run_lists(bt, v0, 0, nlvl)) != CS_OK) break;
     const bool use_graph = !bt->timing;
-    if (use_graph && (rc = get_graph(bt, c, nlvl, per_launch_steps)) != CS_OK) break;
     for (;;) {
+      if (use_graph && (rc = get_graph(bt, c, nlvl, per_launch_steps)) != CS_OK) break;
+      const bool cta = use_cta_path(bt);
       for (int k = 0; k < o.check_every && rc == CS_OK; ++k) {
         if (use_graph) {
-          cudaError_t e = cudaGraphLaunch(bt->graph, bt->stream);
+          cudaError_t e = cudaGraphLaunch(bt->graph[cta ? 1 : 0], bt->stream);
           if (e != cudaSuccess) rc = set_err(CS_ERR_CUDA, std::string("graph launch: ") + cudaGetErrorString(e));
-          bt->launches += use_cta_path(bt) ? 6 : 9 + 2 * nlvl;
+          bt->launches += cta ? 7 : 9 + 2 * nlvl;
           bt->super_steps += 1;
         } else {
           rc = super_step(bt, c, nlvl);
@@ -1183,6 +1202,7 @@ extern "C" int cs_solve(cs_batch* bt, const cs_opts* opts) {
         break;
       }
       if (bt->h_n[0] == 0) break;
+      if (auto_path) bt->cta_now = bt->h_n[0] <= cta_max ? 1 : 0;
       if (steps > max_super) {
         rc = set_err(CS_ERR_STATE, "Newton phase did not terminate");
         break;
@@ -1224,6 +1244,7 @@ extern "C" int cs_solve(cs_batch* bt, const cs_opts* opts) {
     }
     if (!any_newton) break;
   }
+  bt->cta_now = -1;
   if (rc == CS_OK) rc = check_config(bt);
   if (rc == CS_OK) CS_CUDA(cudaStreamSynchronize(bt->stream));
   return rc;
@@ -1309,7 +1330,6 @@ static int set_all_status(cs_batch* bt, int status, double alpha, int need_jac) 
     s.norm_bits = 0;
     s.res_bits = 0;
     s.ntrial = 1;
-    memset(s.trial_bits, 0, sizeof(s.trial_bits));
   }
   return write_inst(bt, hi);
 }
@@ -1579,4 +1599,17 @@ extern "C" int cs_last_error(char* buf, size_t len) {
   memcpy(buf, g_err.data(), n);
   buf[n] = '\0';
   return (int)g_err.size();
+}
+
+extern "C" int cs_profiler_start(void) {
+  CS_TRY(ensure_context());
+  CS_CUDA(cudaDeviceSynchronize());
+  CS_CUDA(cudaProfilerStart());
+  return CS_OK;
+}
+
+extern "C" int cs_profiler_stop(void) {
+  CS_CUDA(cudaDeviceSynchronize());
+  CS_CUDA(cudaProfilerStop());
+  return CS_OK;
 }

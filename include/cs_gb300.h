@@ -294,6 +294,12 @@ int cs_time_condense(cs_batch* bt, int reps, double* ms);
  * fractions. */
 int cs_measure_fp64_peak(double* tflops);
 
+/* Start / stop the profiler's collection range (cudaProfilerStart/Stop), so
+ * a profiler launched with collection off from the start captures exactly
+ * the region between them.  No reference counterpart. */
+int cs_profiler_start(void);
+int cs_profiler_stop(void);
+
 #ifdef __cplusplus
 }
 #endif
