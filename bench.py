@@ -729,7 +729,7 @@ def run_pendulum(args, cs, rank, world, local_rank):
     cs.build.build_library()
     cs._lib.load()
     fp64_peak = cs.module.measure_fp64_peak()
-    cp = cs.CompiledProblem(pr, m)
+    cp = cs.CompiledProblem(pr, m, precision=args.precision)
     bt = cs.Batch(cp, 1, node_capacity=4 * nodes)
     T0 = cs.module.PinnedArray((nodes,), np.float64)
     T0.array[...] = np.asarray(pr.T0, float)
@@ -790,8 +790,16 @@ def run_pendulum(args, cs, rank, world, local_rank):
     n_int = nodes - 1
     fc = flops_per_interval(m, cp.ny, cp.nz, cp.np_eff)
     fe = executed_flops_per_interval(m, cp.ny, cp.nz, cp.np_eff)
-    roof = {"bound": "fp64", "kernel": "k_condense", "achieved": fc * n_int / (ms * 1e-3) / 1e12, "peak": fp64_peak,
-            "unit": "TFLOP/s", "frac": fc * n_int / (ms * 1e-3) / 1e12 / fp64_peak, "traffic": None,
+    peak, bound = fp64_peak, "fp64"
+    if args.precision != "fp64":
+        # tensor-core condensation: against the measured dense BF16 peak
+        try:
+            peak = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["bf16_tflops"]
+        except (OSError, KeyError, ValueError):
+            peak = 1900.0
+        bound = "tensor"
+    roof = {"bound": bound, "kernel": "k_condense", "achieved": fc * n_int / (ms * 1e-3) / 1e12, "peak": peak,
+            "unit": "TFLOP/s", "frac": fc * n_int / (ms * 1e-3) / 1e12 / peak, "traffic": None,
             "ms_per_launch": ms, "flops_per_launch": fc * n_int,
             "executed_tflops": fe * n_int / (ms * 1e-3) / 1e12,
             "executed_frac": fe * n_int / (ms * 1e-3) / 1e12 / fp64_peak,
@@ -799,6 +807,19 @@ def run_pendulum(args, cs, rank, world, local_rank):
                           "executed: (2/3)s1^3 + 2 s1^2 r + 2 s1 r ny with s1 = (m-1)(ny+nz) = %d (the stage-0 "
                           "block is eliminated directly); peak of measured FP64 (DFMA microbenchmark, this run)"
                           % (m * (cp.ny + cp.nz), cp.ny + cp.np_eff + 1, (m - 1) * (cp.ny + cp.nz))}
+    # reduced precision: max-abs difference from the FP64 solve of the same problem
+    err = None
+    if args.precision != "fp64":
+        cp64 = cs.CompiledProblem(pr, m)
+        b64 = cs.Batch(cp64, 1, node_capacity=4 * nodes)
+        b64.set_guess_packed(Nh.array, T0.array, Y0.array, Z0.array, P0.array, None)
+        b64.solve(opts)
+        s64 = b64.solution()[0]
+        if s64["N"] == sol["N"]:
+            err = {"y": float(np.abs(sol["y"] - s64["y"]).max()), "z": float(np.abs(sol["z"] - s64["z"]).max()),
+                   "p": float(np.abs(sol["p"] - s64["p"]).max()), "fp64_newton_steps": s64["newton_steps"]}
+        else:
+            err = {"note": "final meshes differ (%d vs %d nodes)" % (sol["N"], s64["N"])}
     cpu = None
     if cpu_t is not None:
         t_solve = sol["newton_steps"] * cpu_t[1] * n_int + sol["residual_evals"] * cpu_t[0] * n_int
@@ -812,7 +833,8 @@ def run_pendulum(args, cs, rank, world, local_rank):
                           % (c["tol"], K),
                 "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
                 "ms_per_step": 1000 * dt / args.steps, "higher_is_better": True, "scaling": "weak",
-                "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f64 (%s condensation)" % args.precision,
+                "data": "synthetic",
                 "config": {"workload": "pendulum chain K=%d (ny %d, nz %d, np %d), Nodes=%d, m=%d, tol %g, "
                                        "theta(0)~U[-0.5,0.5] seed %d, guess theta_i(0)(1-t/T)"
                                        % (K, cp.ny, cp.nz, cp.np, nodes, m, c["tol"], c["seed"]),
@@ -823,7 +845,8 @@ def run_pendulum(args, cs, rank, world, local_rank):
                 "solve_stats": {"success": bool(sol["success"]), "N": sol["N"], "newton_steps": sol["newton_steps"],
                                 "residual_evals": sol["residual_evals"], "max_residual": sol["max_residual"]},
                 "phase_ms": {"condense": prof["condense_ms"], "babd": prof["babd_ms"],
-                             "residual": prof["residual_ms"]}}
+                             "residual": prof["residual_ms"]},
+                "precision": args.precision, "max_abs_error_vs_fp64": err}
         print(json.dumps(line))
     if dist is not None:
         dist.destroy_process_group()
@@ -839,6 +862,8 @@ def main():
     ap.add_argument("--family", default="vdp", choices=["vdp", "pendulum8"],
                     help="warm-start family (warm workload and its reference arm)")
     ap.add_argument("--pendulum", type=int, default=16, choices=[16, 32], help="chain length K (pendulum)")
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "tf32", "bf16"],
+                    help="pendulum: precision of the large-system condensation")
     ap.add_argument("--batch", type=int, default=None, help="instances per step (warm: 8192, plain: 4096)")
     ap.add_argument("--train", type=int, default=65536, help="training solutions (warm)")
     ap.add_argument("--epochs", type=int, default=150)
@@ -858,7 +883,7 @@ def main():
         cs.build.build_library()
         lib = cs._lib.load()
         pr = pendulum_problem(cs, args.pendulum)
-        cp = cs.CompiledProblem(pr, PENDULUM[args.pendulum]["m"])
+        cp = cs.CompiledProblem(pr, PENDULUM[args.pendulum]["m"], precision=args.precision)
         bt = cs.Batch(cp, 1)
         bt.set_guess([(np.asarray(pr.T0, float), np.asarray(pr.Y0, float), np.asarray(pr.Z0, float))],
                      np.asarray(pr.P0, float).reshape(1, -1))

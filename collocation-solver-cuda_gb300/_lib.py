@@ -23,7 +23,7 @@ class ModuleDesc(ctypes.Structure):
                 ("np_eff", ctypes.c_int), ("n_theta", ctypes.c_int), ("m", ctypes.c_int),
                 ("lobatto_A", _dp), ("lobatto_b", _dp), ("lobatto_c", _dp), ("gauss_w", _dp), ("gauss_L", _dp),
                 ("gauss_I", _dp), ("L0", _dp), ("L1", _dp), ("cache_dir", ctypes.c_char_p),
-                ("layout", ctypes.c_int)]
+                ("layout", ctypes.c_int), ("precision", ctypes.c_int)]
 
 
 class Opts(ctypes.Structure):

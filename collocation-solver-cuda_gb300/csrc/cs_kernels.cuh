@@ -137,6 +137,12 @@ struct CsBatch {
 #define CS_BIG_TREE 0
 #endif
 #define CS_BIG (CS_BIG_COND || CS_BIG_TREE)
+// precision of the large-system condensation: 0 FP64, 1 TF32 / 2 BF16 tensor
+// cores with FP32 storage and accumulation (an inexact Newton Jacobian; the
+// residual, line search, mesh error and BABD solve stay FP64)
+#ifndef CS_PREC
+#define CS_PREC 0
+#endif
 #ifndef CS_SMEM_MAX
 #define CS_SMEM_MAX 232448
 #endif
@@ -1404,7 +1410,9 @@ extern "C" __global__ void k_babd_cta(CsBatch bt, int recover) {}
 #define CS_LDG (((CS_NCOL1 + 3) / 4) * 4)   // row stride of the slab matrix
 #define CS_PLD (CS_NB + 1)                  // row stride of the panel (shared)
 // slab: W [S1][LDG] | stage Jacobians [M][RB][NFG] | X0 [RB][NRHS]
-#define CS_WS_COND ((long long)CS_S1 * CS_LDG + (long long)CS_M * CS_RB * CS_NFG + (long long)CS_RB * CS_NRHS)
+//       | (reduced precision) FP32 copies of the stage Jacobians and X0
+#define CS_WS_JF ((long long)CS_M * CS_RB * CS_NFG + (long long)CS_RB * CS_NRHS + CS_M * CS_M + CS_M)
+#define CS_WS_COND ((long long)CS_S1 * CS_LDG + CS_WS_JF + (CS_PREC ? (CS_WS_JF + 1) / 2 : 0ll))
 // shared: panel [S1][PLD] | U12 [NB][LDG] | fa [M RB] | hA [M M] | fb [NY] | inv [S1] | red [16] | piv [NB]
 #define CS_SM_COND (CS_S1 * CS_PLD + CS_NB * CS_LDG + CS_M * CS_RB + CS_M * CS_M + CS_NY + CS_S1 + 16 + CS_NB)
 // merge matrix and top system: in shared memory when they fit, else in the slab
@@ -1501,19 +1509,119 @@ __device__ __noinline__ void cs_stage_big(const CsBatch& bt, int slot, int b, in
 #endif
 }
 
+// element-type helpers of the large-system condensation (T = double for the
+// FP64 path, float for the mixed-precision one)
+__device__ __forceinline__ double cs_fma(double a, double b, double c) { return fma(a, b, c); }
+__device__ __forceinline__ float cs_fma(float a, float b, float c) { return fmaf(a, b, c); }
+__device__ __forceinline__ unsigned long long cs_abskey(float v) {
+  return (unsigned long long)(__float_as_uint(v) & 0x7fffffffu);
+}
+__device__ __forceinline__ bool cs_tiny(double v) { return cs_abskey(v) < 0x3ce4000000000000ull; }
+__device__ __forceinline__ bool cs_tiny(float v) { return fabsf(v) < 2.220446049250313e-15f; }
+
+// tensor-core operands: FP32 rounded to TF32 (round to nearest, ties away),
+// or two FP32 rounded to a BF16 pair (lo in the low half)
+__device__ __forceinline__ unsigned cs_tf32(float x) {
+  unsigned r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+  return r;
+}
+__device__ __forceinline__ unsigned cs_bf2(float lo, float hi) {
+  unsigned r;
+  asm("cvt.rn.bf16x2.f32 %0, %1, %2;" : "=r"(r) : "f"(hi), "f"(lo));
+  return r;
+}
+
+// A22 -= L21 U12 on the tensor cores for the mixed-precision condensation:
+// warp items of 16 rows x 32 columns (four m16n8 tiles), FP32 accumulators
+// initialised from A22, operands -L21 (panel) and U12 rounded to TF32
+// (PREC 1, m16n8k8, two k-steps per 16-column panel) or BF16 (PREC 2,
+// m16n8k16).  Fragment layouts (g = lane / 4, t = lane % 4):
+//   C  c0 (g, 2t)  c1 (g, 2t+1)  c2 (g+8, 2t)  c3 (g+8, 2t+1)
+//   TF32 A a0 (g, t) a1 (g+8, t) a2 (g, t+4) a3 (g+8, t+4); B b0 (t, g) b1 (t+4, g)
+//   BF16 A pairs (g, 2t..) (g+8, 2t..) (g, 2t+8..) (g+8, 2t+8..); B pairs (2t.., g) (2t+8.., g)
+template <int PREC>
+__device__ void cs_trailing_mma(float* W, const float* P, const float* U, int r0, int c0, int nr, int ncol, int kb) {
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const int lane = tid & 31, w = tid >> 5, nw = nt >> 5;
+  const int g = lane >> 2, t = lane & 3;
+  const int rt = (nr + 15) >> 4, ct = (ncol + 31) >> 5;
+  for (int item = w; item < rt * ct; item += nw) {
+    const int ri = item / ct, ci = item - ri * ct;
+    const int ra = ri * 16, cb = ci * 32;
+    float acc[4][4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int row = ra + g + ((q & 2) ? 8 : 0), col = cb + 8 * j + 2 * t + (q & 1);
+        acc[j][q] = (row < nr && col < ncol) ? W[(size_t)(r0 + row) * CS_LDG + c0 + col] : 0.f;
+      }
+    auto A = [&](int row, int l) -> float {
+      return (row < nr && l < kb) ? -P[(kb + row) * CS_PLD + l] : 0.f;
+    };
+    auto B = [&](int l, int col) -> float { return (l < kb && col < ncol) ? U[l * CS_LDG + col] : 0.f; };
+    if constexpr (PREC == 1) {
+#pragma unroll
+      for (int ks = 0; ks < CS_NB; ks += 8) {
+        const unsigned a0 = cs_tf32(A(ra + g, ks + t)), a1 = cs_tf32(A(ra + g + 8, ks + t));
+        const unsigned a2 = cs_tf32(A(ra + g, ks + t + 4)), a3 = cs_tf32(A(ra + g + 8, ks + t + 4));
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          const unsigned b0 = cs_tf32(B(ks + t, cb + 8 * j + g)), b1 = cs_tf32(B(ks + t + 4, cb + 8 * j + g));
+          asm volatile("mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+                       "{%0,%1,%2,%3};\n"
+                       : "+f"(acc[j][0]), "+f"(acc[j][1]), "+f"(acc[j][2]), "+f"(acc[j][3])
+                       : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+        }
+      }
+    } else {
+#pragma unroll
+      for (int ks = 0; ks < CS_NB; ks += 16) {
+        const unsigned a0 = cs_bf2(A(ra + g, ks + 2 * t), A(ra + g, ks + 2 * t + 1));
+        const unsigned a1 = cs_bf2(A(ra + g + 8, ks + 2 * t), A(ra + g + 8, ks + 2 * t + 1));
+        const unsigned a2 = cs_bf2(A(ra + g, ks + 2 * t + 8), A(ra + g, ks + 2 * t + 9));
+        const unsigned a3 = cs_bf2(A(ra + g + 8, ks + 2 * t + 8), A(ra + g + 8, ks + 2 * t + 9));
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          const int col = cb + 8 * j + g;
+          const unsigned b0 = cs_bf2(B(ks + 2 * t, col), B(ks + 2 * t + 1, col));
+          const unsigned b1 = cs_bf2(B(ks + 2 * t + 8, col), B(ks + 2 * t + 9, col));
+          asm volatile("mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+                       "{%0,%1,%2,%3};\n"
+                       : "+f"(acc[j][0]), "+f"(acc[j][1]), "+f"(acc[j][2]), "+f"(acc[j][3])
+                       : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+        }
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int row = ra + g + ((q & 2) ? 8 : 0), col = cb + 8 * j + 2 * t + (q & 1);
+        if (row < nr && col < ncol) W[(size_t)(r0 + row) * CS_LDG + c0 + col] = acc[j][q];
+      }
+  }
+}
+
+// FP64 instantiations never call the tensor-core update
+template <int PREC>
+__device__ __forceinline__ void cs_trailing_mma(double*, const double*, const double*, int, int, int, int, int) {}
+
+template <typename T, int PREC>
 __device__ void cs_condense_big(const CsBatch& bt, int slot, double* slab, double* sm) {
   constexpr int RB = CS_RB;
   const int tid = threadIdx.x, nt = blockDim.x;
-  double* W = slab;                                   // [S1][LDG]
+  T* W = reinterpret_cast<T*>(slab);                  // [S1][LDG]
   double* JG = slab + (size_t)CS_S1 * CS_LDG;         // [M][RB][NFG]: Df rows, then Dg rows
   double* X0 = JG + (size_t)CS_M * RB * CS_NFG;       // [RB][NRHS]
-  double* P = sm;                                     // [S1][PLD]
-  double* U = P + CS_S1 * CS_PLD;                     // [NB][LDG], columns relative to the panel's end
-  double* fa = U + CS_NB * CS_LDG;
+  T* P = reinterpret_cast<T*>(sm);                    // [S1][PLD]
+  T* U = P + CS_S1 * CS_PLD;                          // [NB][LDG], columns relative to the panel's end
+  double* fa = sm + ((CS_S1 * CS_PLD + CS_NB * CS_LDG) * sizeof(T) + 7) / 8;
   double* hA = fa + CS_M * RB;
   double* fb = hA + CS_M * CS_M;
-  double* inv = fb + CS_NY;
-  double* red = inv + CS_S1;
+  T* inv = reinterpret_cast<T*>(fb + CS_NY);
+  double* red = fb + CS_NY + CS_S1;
   int* piv = (int*)(red + 16);
   const int b = bt.inst_of[slot];
   const double h = bt.t[slot + 1] - bt.t[slot];
@@ -1568,11 +1676,46 @@ __device__ void cs_condense_big(const CsBatch& bt, int slot, double* slab, doubl
     }
   }
   __syncthreads();
+  // ---- reduced precision: FP32 copies of the stage Jacobians and X0, once
+  //      (conversions run on the FP64 pipe: none inside the fill's sums)
+  float* JGf = reinterpret_cast<float*>(X0 + (size_t)RB * CS_NRHS);  // [M][RB][NFG]
+  float* X0f = JGf + (size_t)CS_M * RB * CS_NFG;                      // [RB][NRHS]
+  float* hAf = X0f + (size_t)RB * CS_NRHS;                             // [M][M]
+  float* Bf = hAf + CS_M * CS_M;                                       // [M]
+  if constexpr (PREC != 0) {
+    for (int e = tid; e < CS_M * RB * CS_NFG; e += nt) JGf[e] = (float)JG[e];
+    for (int e = tid; e < RB * CS_NRHS; e += nt) X0f[e] = (float)X0[e];
+    for (int e = tid; e < CS_M * CS_M; e += nt) hAf[e] = (float)hA[e];
+    for (int e = tid; e < CS_M; e += nt) Bf[e] = (float)(h * CS_B[e]);
+    __syncthreads();
+  }
   // ---- the reduced system [W11 | R1 - W10 X0] (stages 1..M-1) into the slab
   for (int e = tid; e < CS_S1 * CS_NCOL1; e += nt) {
     const int row = e / CS_NCOL1, col = e - row * CS_NCOL1;
     const int j = 1 + row / RB, a = row - (j - 1) * RB;
     const double* J = JG + (size_t)(j * RB + a) * CS_NFG;
+    if constexpr (PREC != 0) {
+      const float* Jf = JGf + (size_t)(j * RB + a) * CS_NFG;
+      float vf;
+      if (col < CS_S1) {
+        const int k = 1 + col / RB, q = col - (k - 1) * RB;
+        if (q < CS_NY) {
+          vf = hAf[j * CS_M + k] * Jf[q];
+          if (k == j && q == a) vf -= 1.f;
+        } else {
+          vf = (k == j) ? Jf[q] : 0.f;
+        }
+      } else {
+        // the right-hand side of an inexact stage solve: FP32 suffices
+        const int c = col - CS_S1;
+        float w = 0.f;
+        for (int q = 0; q < CS_NY; ++q) w = fmaf(Jf[q], X0f[q * CS_NRHS + c], w);
+        const float r = (c < CS_NY) ? Jf[c] : ((c < CS_NY + CS_NPE) ? Jf[CS_NY + CS_NZ + (c - CS_NY)] : (float)fa[j * RB + a]);
+        vf = fmaf(-hAf[j * CS_M], w, r);
+      }
+      W[(size_t)row * CS_LDG + col] = (T)vf;
+      continue;
+    }
     double v;
     if (col < CS_S1) {
       const int k = 1 + col / RB, q = col - (k - 1) * RB;
@@ -1588,7 +1731,7 @@ __device__ void cs_condense_big(const CsBatch& bt, int slot, double* slab, doubl
       for (int q = 0; q < CS_NY; ++q) w = fma(J[q], X0[q * CS_NRHS + c], w);
       v = fma(-hA[j * CS_M], w, cs_rhs(J, fa, j, a, c));
     }
-    W[(size_t)row * CS_LDG + col] = v;
+    W[(size_t)row * CS_LDG + col] = (T)v;
   }
   __syncthreads();
   // ---- blocked LU with partial pivoting
@@ -1614,17 +1757,17 @@ __device__ void cs_condense_big(const CsBatch& bt, int slot, double* slab, doubl
       if (tid == 0) piv[kk] = brow;
       if (brow != kk)
         for (int c = tid; c < kb; c += nt) {
-          const double tmp = P[kk * CS_PLD + c];
+          const T tmp = P[kk * CS_PLD + c];
           P[kk * CS_PLD + c] = P[brow * CS_PLD + c];
           P[brow * CS_PLD + c] = tmp;
         }
       __syncthreads();
-      const double pv = P[kk * CS_PLD + kk];
-      const bool tiny = cs_abskey(pv) < 0x3ce4000000000000ull;  // |pv| < 10 * 2^-52
+      const T pv = P[kk * CS_PLD + kk];
+      const bool tiny = cs_tiny(pv);  // |pv| < 10 * 2^-52
       singular |= tiny;
-      const double ip = 1.0 / pv;
+      const T ip = (T)1 / pv;
       if (tid == 0) inv[k0 + kk] = ip;
-      const double mul = tiny ? 0.0 : ip;
+      const T mul = tiny ? (T)0 : ip;
       for (int r = kk + 1 + tid; r < pr; r += nt) P[r * CS_PLD + kk] *= mul;
       __syncthreads();
       const int nc = kb - kk - 1;
@@ -1633,7 +1776,7 @@ __device__ void cs_condense_big(const CsBatch& bt, int slot, double* slab, doubl
         for (int e = tid; e < ne; e += nt) {
           const int rr = e / nc;
           const int r = kk + 1 + rr, c = kk + 1 + (e - rr * nc);
-          P[r * CS_PLD + c] = fma(-P[r * CS_PLD + kk], P[kk * CS_PLD + c], P[r * CS_PLD + c]);
+          P[r * CS_PLD + c] = cs_fma(-P[r * CS_PLD + kk], P[kk * CS_PLD + c], P[r * CS_PLD + c]);
         }
       }
       __syncthreads();
@@ -1646,11 +1789,11 @@ __device__ void cs_condense_big(const CsBatch& bt, int slot, double* slab, doubl
     // columns right of the panel: the row swaps in order, then U12 = L11^-1 A12
     const int c0 = k0 + kb, ncol = CS_NCOL1 - c0;
     for (int c = tid; c < ncol; c += nt) {
-      double* colp = W + c0 + c;
+      T* colp = W + c0 + c;
       for (int kk = 0; kk < kb; ++kk) {
         const int pr2 = piv[kk];
         if (pr2 != kk) {
-          const double t0 = colp[(size_t)(k0 + kk) * CS_LDG];
+          const T t0 = colp[(size_t)(k0 + kk) * CS_LDG];
           colp[(size_t)(k0 + kk) * CS_LDG] = colp[(size_t)(k0 + pr2) * CS_LDG];
           colp[(size_t)(k0 + pr2) * CS_LDG] = t0;
         }
@@ -1658,8 +1801,8 @@ __device__ void cs_condense_big(const CsBatch& bt, int slot, double* slab, doubl
       // column c of U12 in shared memory (this thread's own column)
 #pragma unroll 1
       for (int i = 0; i < kb; ++i) {
-        double v = colp[(size_t)(k0 + i) * CS_LDG];
-        for (int l = 0; l < i; ++l) v = fma(-P[i * CS_PLD + l], U[l * CS_LDG + c], v);
+        T v = colp[(size_t)(k0 + i) * CS_LDG];
+        for (int l = 0; l < i; ++l) v = cs_fma(-P[i * CS_PLD + l], U[l * CS_LDG + c], v);
         colp[(size_t)(k0 + i) * CS_LDG] = v;
         U[i * CS_LDG + c] = v;
       }
@@ -1668,7 +1811,9 @@ __device__ void cs_condense_big(const CsBatch& bt, int slot, double* slab, doubl
     // trailing update A22 -= L21 U12: warp items of 16 rows x 32 columns,
     // lane owns one column (fills the lanes for any trailing width)
     const int r0 = k0 + kb, nr = CS_S1 - r0;
-    if (nr > 0 && ncol > 0) {
+    if constexpr (PREC != 0) {
+      if (nr > 0 && ncol > 0) cs_trailing_mma<PREC>(W, P, U, r0, c0, nr, ncol, kb);
+    } else if (nr > 0 && ncol > 0) {
       const int rt = (nr + 15) >> 4, ct = (ncol + 31) >> 5;
       const int lane = tid & 31, w = tid >> 5, nw = nt >> 5;
       for (int item = w; item < rt * ct; item += nw) {
@@ -1708,13 +1853,13 @@ __device__ void cs_condense_big(const CsBatch& bt, int slot, double* slab, doubl
     __syncthreads();
     // diagonal block, one thread per right-hand side, rows from the bottom
     for (int c = tid; c < CS_NRHS; c += nt) {
-      double* colp = W + CS_S1 + c;
+      T* colp = W + CS_S1 + c;
       for (int i = 0; i < kb; ++i) U[i * CS_LDG + c] = colp[(size_t)(k0 + i) * CS_LDG];
 #pragma unroll 1
       for (int i = kb - 1; i >= 0; --i) {
-        const double xi = U[i * CS_LDG + c] * inv[k0 + i];
+        const T xi = U[i * CS_LDG + c] * inv[k0 + i];
         U[i * CS_LDG + c] = xi;
-        for (int q = 0; q < i; ++q) U[q * CS_LDG + c] = fma(-P[(k0 + q) * CS_PLD + i], xi, U[q * CS_LDG + c]);
+        for (int q = 0; q < i; ++q) U[q * CS_LDG + c] = cs_fma(-P[(k0 + q) * CS_PLD + i], xi, U[q * CS_LDG + c]);
       }
       for (int i = 0; i < kb; ++i) colp[(size_t)(k0 + i) * CS_LDG] = U[i * CS_LDG + c];
     }
@@ -1722,8 +1867,8 @@ __device__ void cs_condense_big(const CsBatch& bt, int slot, double* slab, doubl
     // rows above the block: B[q] -= U[q][k0 + i] x[i], i from the last
     for (int e = tid; e < k0 * CS_NRHS; e += nt) {
       const int q = e / CS_NRHS, c = e - q * CS_NRHS;
-      double v = W[(size_t)q * CS_LDG + CS_S1 + c];
-      for (int i = kb - 1; i >= 0; --i) v = fma(-P[q * CS_PLD + i], U[i * CS_LDG + c], v);
+      T v = W[(size_t)q * CS_LDG + CS_S1 + c];
+      for (int i = kb - 1; i >= 0; --i) v = cs_fma(-P[q * CS_PLD + i], U[i * CS_LDG + c], v);
       W[(size_t)q * CS_LDG + CS_S1 + c] = v;
     }
     __syncthreads();
@@ -1732,15 +1877,22 @@ __device__ void cs_condense_big(const CsBatch& bt, int slot, double* slab, doubl
   double* X = bt.X + (size_t)slot * CS_NRHS * CS_S;
   for (int e = tid; e < CS_NRHS * CS_S; e += nt) {
     const int c = e / CS_S, r = e - c * CS_S;
-    X[e] = (r < RB) ? X0[r * CS_NRHS + c] : W[(size_t)(r - RB) * CS_LDG + CS_S1 + c];
+    X[e] = (r < RB) ? X0[r * CS_NRHS + c] : (double)W[(size_t)(r - RB) * CS_LDG + CS_S1 + c];
   }
   // ---- condensed block row: D X = h sum_j b_j X[(j, a)]
   double* row = bt.rows0 + (size_t)slot * CS_ROWSZ;
   for (int e = tid; e < CS_NRHS * CS_NY; e += nt) {
     const int c = e / CS_NY, a = e - c * CS_NY;
-    double s = CS_B[0] * X0[a * CS_NRHS + c];
-    for (int j = 1; j < CS_M; ++j) s += CS_B[j] * W[(size_t)((j - 1) * RB + a) * CS_LDG + CS_S1 + c];
-    const double dx = h * s;
+    double dx;
+    if constexpr (PREC != 0) {
+      float sf = Bf[0] * X0f[a * CS_NRHS + c];
+      for (int j = 1; j < CS_M; ++j) sf = fmaf(Bf[j], (float)W[(size_t)((j - 1) * RB + a) * CS_LDG + CS_S1 + c], sf);
+      dx = (double)sf;
+    } else {
+      double s = CS_B[0] * X0[a * CS_NRHS + c];
+      for (int j = 1; j < CS_M; ++j) s += CS_B[j] * (double)W[(size_t)((j - 1) * RB + a) * CS_LDG + CS_S1 + c];
+      dx = h * s;
+    }
     if (c < CS_NY) {
       row[c * CS_NY + a] = (a == c) ? dx - 1.0 : dx;
       row[(CS_NY + c) * CS_NY + a] = (a == c ? 1.0 : 0.0);
@@ -1765,7 +1917,11 @@ extern "C" __global__ void __launch_bounds__(256, 2) k_condense(CsBatch bt) {
     const int k = cs_find(bt.jac_pre, njac, it);
     const int b = bt.jac[k];
     const int slot = bt.off[b] + (int)(it - bt.jac_pre[k]);
-    cs_condense_big(bt, slot, slab, smem);
+#if CS_PREC == 0
+    cs_condense_big<double, 0>(bt, slot, slab, smem);
+#else
+    cs_condense_big<float, CS_PREC>(bt, slot, slab, smem);
+#endif
   }
 }
 

@@ -273,12 +273,13 @@ struct cs_module {
   int condense_grid = 1;
   // large stage systems: kernels with a global-memory slab per CTA
   bool big = false, big_cond = false, big_tree = false;
+  int prec = 0;  // large-system condensation: 0 FP64, 1 TF32, 2 BF16
   long long slab = 0;  // doubles per CTA
   int big_ctas = 0;    // CTAs with a slab (the largest grid of the slab kernels)
   int tree_grid = 0;   // k_tree_level grid (large systems)
 };
 
-static std::string build_source(const cs_module_desc* d, bool big_cond, bool big_tree, int smem_max) {
+static std::string build_source(const cs_module_desc* d, bool big_cond, bool big_tree, int prec, int smem_max) {
   std::ostringstream o;
   o << "// generated prelude\n";
   o << "#define CS_NY " << d->ny << "\n#define CS_NZ " << d->nz << "\n#define CS_NP " << d->np << "\n";
@@ -286,6 +287,7 @@ static std::string build_source(const cs_module_desc* d, bool big_cond, bool big
   if (big_cond) o << "#define CS_BIG_COND 1\n";
   if (big_tree) o << "#define CS_BIG_TREE 1\n";
   if (big_cond || big_tree) o << "#define CS_SMEM_MAX " << smem_max << "\n";
+  if (prec) o << "#define CS_PREC " << prec << "\n";
   const int m = d->m;
   o << "__constant__ double CS_A[" << m * m << "] = {" << fmt_array(d->lobatto_A, m * m) << "};\n";
   o << "__constant__ double CS_B[" << m << "] = {" << fmt_array(d->lobatto_b, m) << "};\n";
@@ -385,7 +387,16 @@ extern "C" int cs_module_load(const cs_module_desc* d, cs_module** out) {
   // layout 0: the blocked-LU condensation whenever a whole CTA would serve
   // one interval (measured faster from s1 = 102 on) or the system does not
   // fit; the CTA tree kernels only when the merge or top blocks do not fit
-  M->big_cond = d->layout == 2 || (d->layout == 0 && (!fits_cond || gl > 32));
+  if (d->precision < 0 || d->precision > 2) {
+    delete M;
+    return set_err(CS_ERR_INVALID, "cs_module_load: precision must be 0 (FP64), 1 (TF32) or 2 (BF16)");
+  }
+  if (d->precision != 0 && d->layout == 1) {
+    delete M;
+    return set_err(CS_ERR_INVALID, "cs_module_load: reduced precision needs the large-system condensation (layout 0 or 2)");
+  }
+  M->prec = d->precision;
+  M->big_cond = d->layout == 2 || d->precision != 0 || (d->layout == 0 && (!fits_cond || gl > 32));
   M->big_tree = d->layout == 2 || (d->layout == 0 && !fits_tree);
   M->big = M->big_cond || M->big_tree;
   M->cgw = gl;
@@ -396,7 +407,8 @@ extern "C" int cs_module_load(const cs_module_desc* d, cs_module** out) {
   // the kernels check what they get and report a mismatch)
   {
     const long long nb = 16, ncol1 = s1 + M->nrhs, ldg = ((ncol1 + 3) / 4) * 4, nfg = d->ny + d->nz + d->np;
-    const long long ws_cond = (long long)s1 * ldg + (long long)d->m * rb * nfg + (long long)rb * M->nrhs;
+    const long long ws_jf = (long long)d->m * rb * nfg + (long long)rb * M->nrhs + d->m * d->m + d->m;
+    const long long ws_cond = (long long)s1 * ldg + ws_jf + (d->precision ? (ws_jf + 1) / 2 : 0ll);
     const long long sm_cond = (long long)s1 * (nb + 1) + nb * ldg + (long long)d->m * rb + d->m * d->m + d->ny + s1 + 16 + nb;
     const long long qsz = (long long)qld * qc, tsz = (long long)tld * (nt + 1);
     const long long drsz = (long long)(d->ny + d->np) * (2 * d->ny + d->np);
@@ -453,7 +465,7 @@ extern "C" int cs_module_load(const cs_module_desc* d, cs_module** out) {
     M->top_smem = top_per * M->top_wpc;
   }
 
-  std::string src = build_source(d, M->big_cond, M->big_tree, smem_optin);
+  std::string src = build_source(d, M->big_cond, M->big_tree, M->prec, smem_optin);
   std::string cache = d->cache_dir ? d->cache_dir : "";
   if (cache.empty()) {
     const char* env = getenv("CS_GB300_CACHE");

@@ -56,9 +56,14 @@ class CompiledProblem:
 
     layout: 0 automatic, 1 shared-memory kernels only, 2 the large-system
     kernels (global-memory slab per CTA; chosen automatically when a stage
-    system or a BABD block does not fit in shared memory)."""
+    system or a BABD block does not fit in shared memory).
+    precision: "fp64" (default), "tf32" or "bf16": the large-system
+    condensation on the tensor cores (an inexact Newton Jacobian; residual,
+    line search, mesh error and BABD solve stay FP64)."""
 
-    def __init__(self, problem, m, cache_dir=DEFAULT_CACHE, layout=0):
+    PRECISIONS = {"fp64": 0, "tf32": 1, "bf16": 2}
+
+    def __init__(self, problem, m, cache_dir=DEFAULT_CACHE, layout=0, precision="fp64"):
         lib = _lib.load()
         self.problem = problem
         self.m = m
@@ -79,6 +84,8 @@ class CompiledProblem:
         d.cache_dir = self._cache if cache_dir else None
         d.layout = int(layout)
         self.layout = int(layout)
+        d.precision = self.PRECISIONS[precision]
+        self.precision = precision
         h = ctypes.c_void_p()
         _lib.check(lib.cs_module_load(ctypes.byref(d), ctypes.byref(h)), "cs_module_load")
         self.handle = h

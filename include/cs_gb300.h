@@ -68,6 +68,12 @@ typedef struct cs_module_desc {
                                2: large-system kernels (global-memory slab per
                                CTA, blocked LU), chosen automatically when the
                                blocks do not fit in shared memory */
+  int precision;            /* large-system condensation: 0 FP64; 1 TF32,
+                               2 BF16 tensor cores with FP32 storage and
+                               accumulation (an inexact Newton Jacobian: the
+                               residual, line search, mesh error and BABD
+                               solve stay FP64).  1 and 2 imply the
+                               large-system condensation. */
 } cs_module_desc;
 
 /* Compile (or load from the cache) and load the module on the current device. */

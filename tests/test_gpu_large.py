@@ -175,3 +175,44 @@ def test_pendulum_solve_matches_oracle(cs, K):
     np.testing.assert_allclose(s["y"], ref.y, rtol=0, atol=1e-8)
     np.testing.assert_allclose(s["z"], ref.z, rtol=0, atol=1e-8)
     np.testing.assert_allclose(s["p"], ref.p, rtol=0, atol=1e-8)
+
+
+# ------------------------------------------------------ reduced precision ---
+@pytest.mark.parametrize("prec,tol", [("tf32", 1e-3), ("bf16", 1e-2)])
+def test_reduced_precision_direction_close_to_fp64(cs, prec, tol):
+    """The TF32 / BF16 tensor-core condensation is an inexact Jacobian: its
+    blocks and Newton direction stay within `tol` (relative to the largest
+    entry) of the FP64 ones (measured: TF32 2e-5 / 4e-5, BF16 2e-4 / 5e-4)."""
+    pr = _pendulum(cs, 16, 65)
+    outs = {}
+    for p in ("fp64", prec):
+        cp = cs.CompiledProblem(pr, 5, precision=p)
+        bt = cs.Batch(cp, 1)
+        bt.set_guess([(np.asarray(pr.T0, float), np.asarray(pr.Y0, float), np.asarray(pr.Z0, float))],
+                     np.asarray(pr.P0, float).reshape(1, -1))
+        outs[p] = bt.stage_newton_direction(0.1)
+    r0, r1 = outs["fp64"]["rows"][:64], outs[prec]["rows"][:64]
+    assert np.abs(r1 - r0).max() <= tol * np.abs(r0).max()
+    d0, d1 = outs["fp64"]["dy"][:65], outs[prec]["dy"][:65]
+    assert np.abs(d1 - d0).max() <= tol * np.abs(d0).max()
+
+
+@pytest.mark.parametrize("prec", ["tf32", "bf16"])
+def test_reduced_precision_solve_reaches_fp64_oracle_solution(cs, prec):
+    """Inexact Newton with an FP64 residual, line search and mesh error: the
+    solve meets the FP64 tolerance on the oracle's mesh, and its states,
+    costates and controls are within 1e-6 max-abs of the FP64 oracle's
+    (measured: TF32 3e-10, BF16 7e-8)."""
+    pr = _pendulum(cs, 16, 9)
+    cp = cs.CompiledProblem(pr, 5, precision=prec)
+    bt = cs.Batch(cp, 1)
+    bt.set_guess([(np.asarray(pr.T0, float), np.asarray(pr.Y0, float), np.asarray(pr.Z0, float))],
+                 np.asarray(pr.P0, float).reshape(1, -1))
+    bt.solve(cs.default_opts(pr))
+    s = bt.solution()[0]
+    ref = O.solve(OracleProblem(pr), 5, cs.tables.lobatto(5), cs.tables.segment_tables(5))
+    assert s["success"] and ref.success
+    assert s["N"] == ref.N
+    assert s["last_norm"] < pr.tolerance and s["max_residual"] <= 1.0
+    for k, rk in (("y", ref.y), ("z", ref.z), ("p", ref.p)):
+        assert np.abs(s[k] - rk).max() < 1e-6, (k, np.abs(s[k] - rk).max())
