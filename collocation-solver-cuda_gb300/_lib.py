@@ -30,7 +30,8 @@ class Opts(ctypes.Structure):
     _fields_ = [("tol", ctypes.c_double), ("max_iter", ctypes.c_int), ("max_mesh", ctypes.c_int),
                 ("max_nodes", ctypes.c_int), ("min_nodes", ctypes.c_int), ("max_linesearch", ctypes.c_int),
                 ("alpha0", ctypes.c_double), ("alpha_m", ctypes.c_double), ("beta", ctypes.c_double),
-                ("check_every", ctypes.c_int), ("babd_path", ctypes.c_int)]
+                ("check_every", ctypes.c_int), ("babd_path", ctypes.c_int), ("residual_type", ctypes.c_int),
+                ("scale_by_time", ctypes.c_int), ("residual2", ctypes.c_int)]
 
 
 class Stats(ctypes.Structure):
@@ -70,6 +71,7 @@ SIGNATURES = {
     "cs_time_condense": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _dp]),
     "cs_measure_fp64_peak": (ctypes.c_int, [_dp]),
     "cs_profiler_start": (ctypes.c_int, []),
+    "cs_batch_set_opts": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
     "cs_profiler_stop": (ctypes.c_int, []),
     "cs_batch_reset": (ctypes.c_int, [ctypes.c_void_p]),
     "cs_profile_reset": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),

@@ -2209,10 +2209,34 @@ extern "C" __global__ void __launch_bounds__(256) k_top(CsBatch bt) {
 #endif  // CS_BIG
 
 // ------------------------------------------------------------------------
-// Segment residual at the M+1 Gauss points (residual_type 1, with the running
-// sum multiplied by h after each component, as the reference does), and
-// |r|_inf / tol in the last node's slot.
-extern "C" __global__ void k_segres(CsBatch bt, double tol) {
+// Segment residual at the M+1 Gauss points and |r|_inf / tol in the last
+// node's slot (compute_segment_residual_kernel, ..._kernel2 of
+// collocation_solver_parallel_2d_shared.py:1833-2013):
+//   rtype 1 (default): weighted sum of |f - y'| and |g|; 2: weighted squares,
+//   square root at the end; 0: weighted maximum, whose g part takes |f - y'|
+//   of the first nz components (as the reference does); with `scale` the
+//   running value is multiplied by h after each component.
+//   res2: max over points and components of |f - y'| / (1 + max |y'|) and
+//   |g| / (1 + max |z|) (the maxima over the interval's Gauss points).
+__device__ __forceinline__ void cs_gauss_point(const double* yi, const double* yd, const double* zz, double h, int gi,
+                                               double* yv, double* ydv, double* zv) {
+  for (int k = 0; k < CS_NY; ++k) {
+    double sl = 0.0, si = 0.0;
+    for (int q = 0; q < CS_M; ++q) {
+      sl += CS_GL[gi * CS_M + q] * yd[q * CS_NY + k];
+      si += CS_GI[gi * CS_M + q] * yd[q * CS_NY + k];
+    }
+    ydv[k] = sl;
+    yv[k] = yi[k] + h * si;
+  }
+  for (int k = 0; k < CS_NZ; ++k) {
+    double sl = 0.0;
+    for (int q = 0; q < CS_M; ++q) sl += CS_GL[gi * CS_M + q] * zz[q * CS_NZ + k];
+    zv[k] = sl;
+  }
+}
+
+extern "C" __global__ void k_segres(CsBatch bt, double tol, int rtype, int scale, int res2) {
   int slot = blockIdx.x * blockDim.x + threadIdx.x;
   if (slot >= bt.T) return;
   int b = bt.inst_of[slot];
@@ -2229,39 +2253,57 @@ extern "C" __global__ void k_segres(CsBatch bt, double tol) {
     const double* yd = bt.ydot + (size_t)slot * CS_M * CS_NY;
     const double* zz = bt.zt + (size_t)slot * CS_M * CS_NZ;
     double rho_h = 0.0, rho_g = 0.0;
+    double yv[CS_NY], ydv[CS_NY], zv[CS_NZ > 0 ? CS_NZ : 1], f[CS_NY];
+    if (res2) {
+      double ydg[CS_NY], zg[CS_NZ > 0 ? CS_NZ : 1];
+      for (int k = 0; k < CS_NY; ++k) ydg[k] = 0.0;
+      for (int k = 0; k < CS_NZ; ++k) zg[k] = 0.0;
 #pragma unroll 1
-    for (int gi = 0; gi < CS_M + 1; ++gi) {
-      double yv[CS_NY], ydv[CS_NY], zv[CS_NZ > 0 ? CS_NZ : 1], f[CS_NY];
-      for (int k = 0; k < CS_NY; ++k) {
-        double sl = 0.0, si = 0.0;
-        for (int q = 0; q < CS_M; ++q) {
-          sl += CS_GL[gi * CS_M + q] * yd[q * CS_NY + k];
-          si += CS_GI[gi * CS_M + q] * yd[q * CS_NY + k];
-        }
-        ydv[k] = sl;
-        yv[k] = yi[k] + h * si;
+      for (int gi = 0; gi < CS_M + 1; ++gi) {
+        cs_gauss_point(yi, yd, zz, h, gi, yv, ydv, zv);
+        for (int k = 0; k < CS_NY; ++k) ydg[k] = fmax(ydg[k], fabs(ydv[k]));
+        for (int k = 0; k < CS_NZ; ++k) zg[k] = fmax(zg[k], fabs(zv[k]));
       }
-      for (int k = 0; k < CS_NZ; ++k) {
-        double sl = 0.0;
-        for (int q = 0; q < CS_M; ++q) sl += CS_GL[gi * CS_M + q] * zz[q * CS_NZ + k];
-        zv[k] = sl;
-      }
-      cs_f(yv, zv, pl, th, f);
-      const double wgt = CS_GW[gi];
-      for (int k = 0; k < CS_NY; ++k) {
-        rho_h += wgt * fabs(f[k] - ydv[k]);
-        rho_h *= h;
-      }
+#pragma unroll 1
+      for (int gi = 0; gi < CS_M + 1; ++gi) {
+        cs_gauss_point(yi, yd, zz, h, gi, yv, ydv, zv);
+        cs_f(yv, zv, pl, th, f);
+        for (int k = 0; k < CS_NY; ++k) rho_h = fmax(rho_h, fabs(f[k] - ydv[k]) / (1.0 + ydg[k]));
 #if CS_NZ > 0
-      double g[CS_NZ];
-      cs_g(yv, zv, pl, th, bt.inst[b].alpha, g);
-      for (int k = 0; k < CS_NZ; ++k) {
-        rho_g += wgt * fabs(g[k]);
-        rho_g *= h;
-      }
+        double g[CS_NZ];
+        cs_g(yv, zv, pl, th, bt.inst[b].alpha, g);
+        for (int k = 0; k < CS_NZ; ++k) rho_g = fmax(rho_g, fabs(g[k]) / (1.0 + zg[k]));
 #endif
+      }
+      val = fmax(rho_h, rho_g) / tol;
+    } else {
+#pragma unroll 1
+      for (int gi = 0; gi < CS_M + 1; ++gi) {
+        cs_gauss_point(yi, yd, zz, h, gi, yv, ydv, zv);
+        cs_f(yv, zv, pl, th, f);
+        const double wgt = CS_GW[gi];
+        for (int k = 0; k < CS_NY; ++k) {
+          const double r = f[k] - ydv[k];
+          if (rtype == 2) rho_h += wgt * r * r;
+          else if (rtype == 1) rho_h += wgt * fabs(r);
+          else rho_h = fmax(rho_h, wgt * fabs(r));
+          if (scale) rho_h *= h;
+        }
+#if CS_NZ > 0
+        double g[CS_NZ];
+        cs_g(yv, zv, pl, th, bt.inst[b].alpha, g);
+        for (int k = 0; k < CS_NZ; ++k) {
+          if (rtype == 2) rho_g += wgt * g[k] * g[k];
+          else if (rtype == 1) rho_g += wgt * fabs(g[k]);
+          else rho_g = fmax(rho_g, wgt * (k < CS_NY ? fabs(f[k] - ydv[k]) : 0.0));
+          if (scale) rho_g *= h;
+        }
+#endif
+      }
+      if (rtype == 2) val = sqrt(rho_h + rho_g) / tol;
+      else if (rtype == 1) val = (fabs(rho_h) + fabs(rho_g)) / tol;
+      else val = fmax(rho_h, rho_g) / tol;
     }
-    val = (fabs(rho_h) + fabs(rho_g)) / tol;
   } else {
     double ya[CS_NY], yb[CS_NY], r[CS_NY + CS_NP];
     const int first = bt.off[b];

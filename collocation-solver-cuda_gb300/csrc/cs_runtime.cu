@@ -557,7 +557,11 @@ extern "C" void cs_opts_default(cs_opts* o) {
   o->beta = 0.9;
   o->check_every = 4;
   o->babd_path = 0;
+  o->residual_type = 1;
+  o->scale_by_time = 1;
+  o->residual2 = 0;
 }
+
 
 // =============================================================== batch ===
 struct DBuf {
@@ -868,6 +872,14 @@ static CsConsts consts_of(const cs_opts& o) {
   return c;
 }
 
+extern "C" int cs_batch_set_opts(cs_batch* bt, const cs_opts* opts) {
+  if (!bt || !opts) return set_err(CS_ERR_INVALID, "cs_batch_set_opts: null argument");
+  if (opts->residual_type < 0 || opts->residual_type > 2)
+    return set_err(CS_ERR_INVALID, "cs_batch_set_opts: residual_type must be 0, 1 or 2");
+  bt->opts = *opts;
+  return CS_OK;
+}
+
 extern "C" int cs_batch_create(cs_module* M, int batch, long long node_capacity, void* stream, cs_batch** out) {
   if (!M || !out || batch < 1) return set_err(CS_ERR_INVALID, "cs_batch_create: bad argument");
   CS_TRY(ensure_context());
@@ -1167,6 +1179,8 @@ extern "C" int cs_solve(cs_batch* bt, const cs_opts* opts) {
   cs_opts o;
   if (opts) o = *opts; else cs_opts_default(&o);
   if (o.check_every < 1) o.check_every = 1;
+  if (o.residual_type < 0 || o.residual_type > 2)
+    return set_err(CS_ERR_INVALID, "cs_solve: residual_type must be 0, 1 or 2");
   bt->opts = o;
   const CsConsts c = consts_of(o);
   std::vector<CsInst> hi;
@@ -1224,7 +1238,8 @@ extern "C" int cs_solve(cs_batch* bt, const cs_opts* opts) {
     // ---- mesh phase
     CsBatchDev v = devview(bt);
     double tol = o.tol;
-    void* as[] = {&v, &tol};
+    int rtype = o.residual_type, scale = o.scale_by_time, res2 = o.residual2;
+    void* as[] = {&v, &tol, &rtype, &scale, &res2};
     if ((rc = launch(bt, bt->M->f_segres, cdiv(bt->T, 256), 256, 0, as)) != CS_OK) break;
     CsConsts cc = c;
     void* am[] = {&v, &cc};
@@ -1409,7 +1424,8 @@ extern "C" int cs_stage_segment_residual(cs_batch* bt, double alpha, double tol,
   if (!bt || !bt->have_guess) return set_err(CS_ERR_STATE, "cs_stage_segment_residual: no state");
   CS_TRY(set_all_status(bt, ST_SEG, alpha, 0));
   CsBatchDev v = devview(bt);
-  void* as[] = {&v, &tol};
+  int rtype = bt->opts.residual_type, scale = bt->opts.scale_by_time, res2 = bt->opts.residual2;
+  void* as[] = {&v, &tol, &rtype, &scale, &res2};
   CS_TRY(launch(bt, bt->M->f_segres, cdiv(bt->T, 256), 256, 0, as));
   if (res) CS_CUDA(cudaMemcpyAsync(res, bt->res.p, (size_t)bt->T * sizeof(double), cudaMemcpyDeviceToHost, bt->stream));
   std::vector<CsInst> hi;

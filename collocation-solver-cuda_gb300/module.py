@@ -277,6 +277,10 @@ class Batch:
                    "cs_stage_newton_direction")
         return dict(rows=rows, dy=dy, dydot=dyd, dzt=dzt[:, :, :cp.nz], dp=dp[:, :cp.np])
 
+    def set_opts(self, opts):
+        """Options of the stage entry points (segment residual estimate)."""
+        _lib.check(self._lib.cs_batch_set_opts(self.handle, ctypes.byref(opts)), "cs_batch_set_opts")
+
     def stage_segment_residual(self, alpha, tol):
         _, T = self.sizes()
         res = np.zeros(T)

@@ -95,9 +95,19 @@ typedef struct cs_opts {
   int check_every;       /* Newton super-steps between host checks for completion */
   int babd_path;         /* Newton direction kernels: 0 automatic, 1 one CTA per instance,
                             2 one launch per tree level across the instances */
+  int residual_type;     /* segment residual estimate (CS:29-32): 1 weighted sum
+                            (default), 2 weighted squares, 0 weighted maximum */
+  int scale_by_time;     /* multiply the running estimate by h (default 1) */
+  int residual2;         /* 1: the residual2 estimate instead (CS:1895-2013) */
 } cs_opts;
 
 void cs_opts_default(cs_opts* o);
+
+/* Options the stage entry points use (cs_solve sets its own from its
+ * argument): the segment residual estimate of cs_stage_segment_residual and
+ * the line-search / continuation constants.  No reference counterpart (the
+ * reference reads module globals). */
+int cs_batch_set_opts(cs_batch* bt, const cs_opts* opts);
 
 /* Per-instance counters after a solve (the reference's benchmark counts). */
 typedef struct cs_stats {

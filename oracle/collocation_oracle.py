@@ -291,31 +291,70 @@ def recover_delta_k(ny, nz, m, N, delta_y, delta_p, f_a, J, V, W):
 
 
 # ------------------------------------------------------------ mesh error ----
-def segment_residual(prob, m, N, t, y, y_dot, z_tilde, p, alpha, tol, seg):
-    """Per-interval residual at the m+1 Gauss points, residual_type 1 with
-    scale_by_time (CS:1770-1892), and |r|_inf / tol at index N-1."""
+def segment_residual(prob, m, N, t, y, y_dot, z_tilde, p, alpha, tol, seg, residual_type=1, scale_by_time=True,
+                     residual2=False):
+    """Per-interval residual at the m+1 Gauss points and |r|_inf / tol at
+    index N-1 (CS:1770-1892).  residual_type 1 (default, a weighted sum of
+    |h - y'| and |g|), 2 (weighted squares, square root at the end) or 0 (a
+    weighted maximum; its g part takes |h - y'| of the first nz components,
+    as CS:1882-1883 does); with scale_by_time the running sum is multiplied
+    by h after each component (CS:1868-1869, 1883-1884).  residual2
+    (CS:1895-2013): max over the Gauss points and components of
+    |h - y'| / (1 + max |y'|) and |g| / (1 + max |z|)."""
     ny, nz = prob.ny, prob.nz
     h = t[1:] - t[:-1]
     yd = y_dot.reshape(N - 1, m, ny)
     zt = z_tilde.reshape(N - 1, m, nz)
     rho_h = np.zeros(N - 1)
     rho_g = np.zeros(N - 1)
+    pts = []
     for i in range(m + 1):
         L, I, w = seg["L"][i], seg["I"][i], seg["w"][i]
         ydot_t = np.einsum("k,ikl->il", L, yd)
         y_t = y[:-1] + h[:, None] * np.einsum("k,ikl->il", I, yd)
         z_t = np.einsum("k,ikl->il", L, zt)
-        hres = prob.f(y_t, z_t, p, prob.theta) - ydot_t
-        for k in range(ny):
-            rho_h = rho_h + w * np.abs(hres[:, k])
-            rho_h = rho_h * h
-        if nz > 0:
-            gres = prob.g(y_t, z_t, p, prob.theta, alpha)
-            for k in range(nz):
-                rho_g = rho_g + w * np.abs(gres[:, k])
-                rho_g = rho_g * h
-    residual = np.zeros(N)
-    residual[:N - 1] = (np.abs(rho_h) + np.abs(rho_g)) / tol
+        pts.append((w, ydot_t, y_t, z_t))
+    if residual2:
+        ydg = np.max([np.abs(q[1]) for q in pts], axis=0)
+        zg = np.max([np.abs(q[3]) for q in pts], axis=0) if nz else None
+        for w, ydot_t, y_t, z_t in pts:
+            hres = prob.f(y_t, z_t, p, prob.theta) - ydot_t
+            rho_h = np.maximum(rho_h, np.max(np.abs(hres) / (1.0 + ydg), axis=1))
+            if nz > 0:
+                gres = prob.g(y_t, z_t, p, prob.theta, alpha)
+                rho_g = np.maximum(rho_g, np.max(np.abs(gres) / (1.0 + zg), axis=1))
+        residual = np.zeros(N)
+        residual[:N - 1] = np.maximum(rho_h, rho_g) / tol
+    else:
+        for w, ydot_t, y_t, z_t in pts:
+            hres = prob.f(y_t, z_t, p, prob.theta) - ydot_t
+            for k in range(ny):
+                if residual_type == 2:
+                    rho_h = rho_h + w * hres[:, k] * hres[:, k]
+                elif residual_type == 1:
+                    rho_h = rho_h + w * np.abs(hres[:, k])
+                else:
+                    rho_h = np.maximum(rho_h, w * np.abs(hres[:, k]))
+                if scale_by_time:
+                    rho_h = rho_h * h
+            if nz > 0:
+                gres = prob.g(y_t, z_t, p, prob.theta, alpha)
+                for k in range(nz):
+                    if residual_type == 2:
+                        rho_g = rho_g + w * gres[:, k] * gres[:, k]
+                    elif residual_type == 1:
+                        rho_g = rho_g + w * np.abs(gres[:, k])
+                    else:
+                        rho_g = np.maximum(rho_g, w * np.abs(hres[:, k]))
+                    if scale_by_time:
+                        rho_g = rho_g * h
+        residual = np.zeros(N)
+        if residual_type == 2:
+            residual[:N - 1] = np.sqrt(rho_h + rho_g) / tol
+        elif residual_type == 1:
+            residual[:N - 1] = (np.abs(rho_h) + np.abs(rho_g)) / tol
+        else:
+            residual[:N - 1] = np.maximum(rho_h, rho_g) / tol
     if prob.ny + prob.np > 0:
         r = prob.r(y[0], y[N - 1], p, prob.theta)
         residual[N - 1] = np.max(np.abs(r)) / tol
@@ -393,7 +432,8 @@ def newton_step(prob, m, N, rk, t, y, y_dot, z_tilde, p, alpha, f_a, f_b, r_bc, 
     return dy, dyd, dzt, dp
 
 
-def solve(prob, m, rk, seg, T0=None, Y0=None, Z0=None, P0=None, verbose=False, M=8):
+def solve(prob, m, rk, seg, T0=None, Y0=None, Z0=None, P0=None, verbose=False, M=8, residual_type=1,
+          scale_by_time=True, residual2=False):
     """The reference driver (CS:36-251): alpha continuation, damped Newton with
     a halving line search, segment residual and remesh.  Returns SolveResult."""
     ny, nz, npar = prob.ny, prob.nz, prob.np
@@ -450,7 +490,8 @@ def solve(prob, m, rk, seg, T0=None, Y0=None, Z0=None, P0=None, verbose=False, M
                 or N > max_nodes or mesh_it > max_mesh or N < min_nodes:
             success = 0
             break
-        residual, max_residual = segment_residual(prob, m, N, t_span, y, y_dot, z_tilde, para, alpha, tol, seg)
+        residual, max_residual = segment_residual(prob, m, N, t_span, y, y_dot, z_tilde, para, alpha, tol, seg,
+                                                  residual_type, scale_by_time, residual2)
         res.segment_count += 1
         if max_residual > 1:
             z = recover_solution(nz, m, N, z_tilde, seg)

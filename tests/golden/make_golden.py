@@ -14,6 +14,10 @@ Outputs (all small, committed):
 * ``stage_<case>.npz`` : one call of every stage function on a seeded random
   state: residual, Jacobian blocks, condensation, partitioned BABD solve,
   recovery, segment residual, node recovery, remesh, initial input.
+* ``segres_<case>.npz``: the segment residual of a stage dump's state under
+  every estimate the reference offers (residual_type 0/1/2 with and without
+  scale_by_time, and residual2).
+* ``e2e_vdp_coarse_res2.npz``: an end-to-end solve with residual2 on.
 * ``fe_<case>.npz``    : the generated problem functions f, g, r, Df, Dg, Dr
   evaluated at seeded random points, plus the generated BvpDae attributes.
 * the OCP sources used are in ``ocp/``.
@@ -71,15 +75,22 @@ def _gen_problem(ocp_path, workdir):
 
 
 # ----------------------------------------------------------------- e2e ------
-def run_e2e(case, ocp_file, m):
+def run_e2e(case, ocp_file, m, driver=None):
+    """driver: source of a script taking m that runs the reference driver
+    (default: the reference's own command line)."""
     work = tempfile.mkdtemp(prefix="golden_e2e_")
     try:
         shutil.copy(os.path.join(OCP_DIR, ocp_file), work)
         _gen_problem(ocp_file, work)
         env = _env()
         env["PYTHONPATH"] = os.pathsep.join([work, SHIM, REF_DIR])
-        p = subprocess.run([sys.executable, os.path.join(REF_DIR, "collocation_solver_parallel_2d_shared.py"),
-                            "-m", str(m)], cwd=work, env=env, capture_output=True, text=True, timeout=7200)
+        if driver is None:
+            cmd = [sys.executable, os.path.join(REF_DIR, "collocation_solver_parallel_2d_shared.py"), "-m", str(m)]
+        else:
+            with open(os.path.join(work, "driver.py"), "w") as f:
+                f.write(driver)
+            cmd = [sys.executable, "driver.py", str(m)]
+        p = subprocess.run(cmd, cwd=work, env=env, capture_output=True, text=True, timeout=7200)
         log = p.stdout
         if p.returncode != 0:
             raise RuntimeError(p.stderr[-3000:])
@@ -198,6 +209,66 @@ def run_stage(case, ocp_file, m, N, seed):
         shutil.rmtree(work, ignore_errors=True)
 
 
+# ------------------------------------------------- segment residual modes ---
+# The reference's estimate is switched by module globals (residual_type 0/1/2,
+# scale_by_time, residual2; collocation_solver_parallel_2d_shared.py:29-32,
+# 1770-2013).  On the state of a stage dump, record every combination.
+SEGRES_SCRIPT = r'''
+import sys
+import numpy as np
+stage, out = sys.argv[1], sys.argv[2]
+import collocation_solver_parallel_2d_shared as CS
+import bvp_problem
+g = np.load(stage)
+bd = bvp_problem.BvpDae()
+ny, nz, np_ = bd.size_y, bd.size_z, bd.size_p
+m, N = int(g["m"]), int(g["N"])
+CS.global_size_y, CS.global_size_z, CS.global_size_p = ny, nz, np_
+CS.m_collocation = m
+args = (ny, nz, np_, m, N, g["t"], g["y"], g["y_dot"], g["z_tilde"], g["p"], float(g["alpha"]), float(g["tol"]))
+d = {}
+for rt in (0, 1, 2):
+    for sc in (True, False):
+        CS.residual_type, CS.scale_by_time = rt, sc
+        res, mx = CS.compute_segment_residual_parallel(*args)
+        d["res_t%d_s%d" % (rt, int(sc))] = res
+        d["max_t%d_s%d" % (rt, int(sc))] = mx
+res, mx = CS.compute_segment_residual_parallel2(*args)
+d["res2"], d["max2"] = res, mx
+np.savez_compressed(out, **d)
+print("segres ok")
+'''
+
+
+def run_segres(case, ocp_file):
+    work = tempfile.mkdtemp(prefix="golden_segres_")
+    try:
+        shutil.copy(os.path.join(OCP_DIR, ocp_file), work)
+        _gen_problem(ocp_file, work)
+        with open(os.path.join(work, "segres_dump.py"), "w") as f:
+            f.write(SEGRES_SCRIPT)
+        env = _env()
+        env["PYTHONPATH"] = os.pathsep.join([work, SHIM, REF_DIR])
+        p = subprocess.run([sys.executable, "segres_dump.py", os.path.join(HERE, "stage_%s.npz" % case),
+                            os.path.join(HERE, "segres_%s.npz" % case)], cwd=work, env=env, capture_output=True,
+                           text=True, timeout=3600)
+        if p.returncode != 0:
+            raise RuntimeError(p.stderr[-3000:])
+        print(case, p.stdout.strip().splitlines()[-1])
+    finally:
+        shutil.rmtree(work, ignore_errors=True)
+
+
+# e2e solves with the residual2 estimate (module global set before the driver)
+RES2_SCRIPT = r'''
+import sys
+import collocation_solver_parallel_2d_shared as CS
+CS.residual2 = True
+CS.collocation_solver_parallel(m=int(sys.argv[1]))
+'''
+E2E_RES2_CASES = [("vdp_coarse_res2", "vdp_coarse.ocp", 3)]
+
+
 # ------------------------------------------------------------ front end -----
 FE_SCRIPT = r'''
 import sys
@@ -312,9 +383,15 @@ def main(argv):
     for case in STAGE_CASES:
         if sel("stage_" + case[0]):
             run_stage(*case)
+    for case in STAGE_CASES:
+        if sel("segres_" + case[0]):
+            run_segres(case[0], case[1])
     for case in E2E_CASES:
         if sel("e2e_" + case[0]):
             run_e2e(*case)
+    for case in E2E_RES2_CASES:
+        if sel("e2e_" + case[0]):
+            run_e2e(*case, driver=RES2_SCRIPT)
 
 
 if __name__ == "__main__":

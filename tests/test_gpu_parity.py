@@ -194,3 +194,41 @@ def test_failing_instances_match_oracle(cs):
         assert s["success"] == ref.success
         assert (s["newton_steps"], s["residual_evals"], s["N"]) == (ref.jacobian_count, ref.residual_count, ref.N)
         assert np.abs(s["y"] - ref.y).max() < 1e-8
+
+
+@pytest.mark.parametrize("case,prob", STAGES)
+def test_stage_segment_residual_estimates(cs, case, prob):
+    """The reference's other segment-residual estimates (residual_type 0 and
+    2, without scale_by_time, residual2) against its own numbers."""
+    g = golden("stage_" + case)
+    ref = golden("segres_" + case)
+    m = int(g["m"])
+    cp = compiled(cs, prob, m)
+    bt = _batch_with_state(cs, cp, g)
+    pr = load_problem(prob)
+    for rt in (0, 1, 2):
+        for sc in (True, False):
+            bt.set_opts(cs.default_opts(pr, residual_type=rt, scale_by_time=int(sc), residual2=0))
+            res, mx = bt.stage_segment_residual(float(g["alpha"]), float(g["tol"]))
+            key = "t%d_s%d" % (rt, int(sc))
+            np.testing.assert_allclose(res[:int(g["N"])], ref["res_" + key], rtol=1e-11, atol=1e-12, err_msg=key)
+            assert abs(mx[0] - float(ref["max_" + key])) <= 1e-11 * abs(float(ref["max_" + key]))
+    bt.set_opts(cs.default_opts(pr, residual2=1))
+    res, mx = bt.stage_segment_residual(float(g["alpha"]), float(g["tol"]))
+    np.testing.assert_allclose(res[:int(g["N"])], ref["res2"], rtol=1e-11, atol=1e-12)
+    assert abs(mx[0] - float(ref["max2"])) <= 1e-11 * abs(float(ref["max2"]))
+
+
+def test_end_to_end_residual2_matches_reference(cs):
+    g = golden("e2e_vdp_coarse_res2")
+    m = int(g["m"])
+    pr = load_problem("vdp_coarse")
+    sol = cs.solver.solve_single(pr, m, opts=cs.default_opts(pr, residual2=1))
+    assert sol["success"] == bool(g["success"])
+    assert sol["N"] == g["t"].shape[0]
+    assert sol["newton_steps"] == int(g["jacobian_counts"])
+    assert sol["residual_evals"] == int(g["residual_counts"])
+    assert sol["remeshes"] == len(g["nodes_after_remesh"])
+    np.testing.assert_array_equal(sol["t"], g["t"])
+    np.testing.assert_allclose(sol["y"], g["y"], atol=1e-8, rtol=0)
+    np.testing.assert_allclose(sol["z"], g["z"], atol=1e-8, rtol=0)

@@ -131,3 +131,43 @@ def test_oracle_end_to_end_matches_reference(case, prob):
     np.testing.assert_allclose(r.y, g["y"], atol=1e-8, rtol=0)
     np.testing.assert_allclose(r.z, g["z"], atol=1e-8, rtol=0)
     np.testing.assert_allclose(r.p, g["p"], atol=1e-8, rtol=0)
+
+
+MODES = [(rt, sc) for rt in (0, 1, 2) for sc in (True, False)]
+
+
+@pytest.mark.parametrize("case,prob", STAGES)
+def test_oracle_segment_residual_estimates_match_reference(case, prob):
+    """Every estimate the reference offers (residual_type 0/1/2, with and
+    without scale_by_time, and residual2), on the state of each stage dump."""
+    cs = pkg()
+    g = golden("stage_" + case)
+    ref = golden("segres_" + case)
+    P = oracle_problem(prob)
+    m, N = int(g["m"]), int(g["N"])
+    seg = cs.tables.segment_tables(m)
+    args = (P, m, N, g["t"], g["y"], g["y_dot"], g["z_tilde"], g["p"], float(g["alpha"]), float(g["tol"]), seg)
+    for rt, sc in MODES:
+        res, mx = O.segment_residual(*args, residual_type=rt, scale_by_time=sc)
+        key = "t%d_s%d" % (rt, int(sc))
+        np.testing.assert_allclose(res, ref["res_" + key], rtol=1e-10, atol=1e-12, err_msg=key)
+        assert abs(mx - float(ref["max_" + key])) <= 1e-10 * abs(mx)
+    res, mx = O.segment_residual(*args, residual2=True)
+    np.testing.assert_allclose(res, ref["res2"], rtol=1e-10, atol=1e-12)
+    assert abs(mx - float(ref["max2"])) <= 1e-10 * abs(mx)
+
+
+def test_oracle_end_to_end_with_residual2_matches_reference():
+    cs = pkg()
+    g = golden("e2e_vdp_coarse_res2")
+    P = oracle_problem("vdp_coarse")
+    m = int(g["m"])
+    r = O.solve(P, m, cs.tables.lobatto(m), cs.tables.segment_tables(m), residual2=True)
+    assert r.success == bool(g["success"])
+    assert r.N == g["t"].shape[0]
+    assert r.jacobian_count == int(g["jacobian_counts"])
+    assert r.residual_count == int(g["residual_counts"])
+    assert r.nodes_after_remesh == list(g["nodes_after_remesh"])
+    np.testing.assert_array_equal(np.round(np.array(r.norms), 8), g["norms"])
+    np.testing.assert_array_equal(r.t, g["t"])
+    np.testing.assert_allclose(r.y, g["y"], atol=1e-8, rtol=0)
