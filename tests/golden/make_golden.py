@@ -47,6 +47,7 @@ E2E_CASES = [
     ("dint_param", "dint_param.ocp", 3),
     ("pend2", "pend2.ocp", 4),
     ("vdp_ineq", "vdp_ineq.ocp", 3),
+    ("vdp_input", "vdp_input.ocp", 4),
 ]
 # (case name, ocp file, m, N nodes, seed) for per-stage dumps
 STAGE_CASES = [
@@ -66,6 +67,13 @@ def _env():
     return env
 
 
+def _copy_inputs(workdir):
+    """Solution files that OCPs name as InputFile."""
+    for fn in os.listdir(OCP_DIR):
+        if fn.endswith(".data"):
+            shutil.copy(os.path.join(OCP_DIR, fn), workdir)
+
+
 def _gen_problem(ocp_path, workdir):
     """Run the reference's OCP2ABVP.py on an OCP file -> bvp_problem.py in workdir."""
     out = subprocess.run([sys.executable, os.path.join(REF_DIR, "OCP2ABVP.py"), ocp_path],
@@ -81,6 +89,7 @@ def run_e2e(case, ocp_file, m, driver=None):
     work = tempfile.mkdtemp(prefix="golden_e2e_")
     try:
         shutil.copy(os.path.join(OCP_DIR, ocp_file), work)
+        _copy_inputs(work)
         _gen_problem(ocp_file, work)
         env = _env()
         env["PYTHONPATH"] = os.pathsep.join([work, SHIM, REF_DIR])
@@ -316,6 +325,7 @@ def run_fe(case, ocp_path, seed):
     work = tempfile.mkdtemp(prefix="golden_fe_")
     try:
         shutil.copy(ocp_path, work)
+        _copy_inputs(work)
         _gen_problem(os.path.basename(ocp_path), work)
         with open(os.path.join(work, "fe_dump.py"), "w") as f:
             f.write(FE_SCRIPT)
@@ -373,7 +383,7 @@ def main(argv):
     sel = (lambda name: not want or name in want)
     if sel("tables"):
         run_tables()
-    for i, f in enumerate(sorted(os.listdir(OCP_DIR))):
+    for i, f in enumerate(sorted(x for x in os.listdir(OCP_DIR) if x.endswith(".ocp"))):
         name = os.path.splitext(f)[0]
         if sel("fe_" + name):
             run_fe(name, os.path.join(OCP_DIR, f), 100 + i)
