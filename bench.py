@@ -482,6 +482,9 @@ def run_warm(args, cs, rank, world, local_rank, cpu, cfg):
     _log("trained in %.1f s (loss %.3g)" % (t_train, loss))
     held = _family_batch(cs, args.family, args.batch, 7 + 100 * rank)
     runner = ws.WarmRunner(fam, solver, net, held)
+    # launch-shape tuner (set-up, untimed): condensation shape per m on the batch
+    tune = [dict(m=g["m"], **g["bt"].autotune(reps=3)) for g in runner.groups]
+    _log("tuned condensation shapes: %s" % tune)
     ws_gb = sum(g["bt"].sizes()[1] for g in runner.groups) * 8 * 300 / 1e9
     cfg["l2"] = cfg["l2"] % ("%.1f" % ws_gb)
     for _ in range(args.warmup):
@@ -584,7 +587,8 @@ def run_warm(args, cs, rank, world, local_rank, cpu, cfg):
                 "warm_start": {"solved": solved, "of": len(held), "fallbacks": n_fb, "phase_s": runner_times,
                                "fallback_rate": n_fb / len(held), "newton_steps_per_solve": float(newton_warm),
                                "train_solutions": int(len(X)), "train_data_s": t_data, "train_s": t_train,
-                               "train_loss": loss, "epochs": args.epochs}}
+                               "train_loss": loss, "epochs": args.epochs},
+                "autotune": tune}
         print(json.dumps(line))
     if dist is not None:
         dist.destroy_process_group()
@@ -596,6 +600,7 @@ def run_plain(args, cs, rank, world, local_rank, cpu, cfg, instances):
     cs._lib.load()
     fp64_peak = cs.module.measure_fp64_peak()
     W = Workload(cs, instances)
+    tune = [dict(m=g["m"], **g["bt"].autotune(reps=3)) for g in W.groups]
     ws_gb = sum(g["bt"].sizes()[1] for g in W.groups) * 8 * 300 / 1e9
     cfg["l2"] = cfg["l2"] % ("%.1f" % ws_gb)
     for _ in range(args.warmup):
@@ -627,7 +632,8 @@ def run_plain(args, cs, rank, world, local_rank, cpu, cfg, instances):
                 "e2e": e2e, "roofline": roof, "cpu_baseline": cpu, "clocks": clk.summary(),
                 "gpu_launches": int(launches),
                 "solve_stats": {"solved": succ, "of": W.n, "newton_steps_per_solve": newton / W.n,
-                                "final_nodes_per_solve": nodes / W.n}}
+                                "final_nodes_per_solve": nodes / W.n},
+                "autotune": tune}
         print(json.dumps(line))
     if dist is not None:
         dist.destroy_process_group()
@@ -743,6 +749,7 @@ def run_pendulum(args, cs, rank, world, local_rank):
     Nh.array[...] = nodes
     bt.set_guess_packed(Nh.array, T0.array, Y0.array, Z0.array, P0.array, None)
     opts = cs.default_opts(pr)
+    tune = bt.autotune(reps=2)
     for _ in range(args.warmup):
         bt.reset()
         bt.solve(opts)
@@ -846,7 +853,7 @@ def run_pendulum(args, cs, rank, world, local_rank):
                                 "residual_evals": sol["residual_evals"], "max_residual": sol["max_residual"]},
                 "phase_ms": {"condense": prof["condense_ms"], "babd": prof["babd_ms"],
                              "residual": prof["residual_ms"]},
-                "precision": args.precision, "max_abs_error_vs_fp64": err}
+                "precision": args.precision, "max_abs_error_vs_fp64": err, "autotune": tune}
         print(json.dumps(line))
     if dist is not None:
         dist.destroy_process_group()

@@ -49,6 +49,11 @@ class Profile(ctypes.Structure):
                 ("condense_ms", ctypes.c_double), ("babd_ms", ctypes.c_double), ("residual_ms", ctypes.c_double)]
 
 
+class TuneResult(ctypes.Structure):
+    _fields_ = [("lanes", ctypes.c_int), ("block", ctypes.c_int), ("grid", ctypes.c_int), ("candidates", ctypes.c_int),
+                ("ms", ctypes.c_double), ("default_ms", ctypes.c_double)]
+
+
 # every symbol declared in include/cs_gb300.h: name -> (restype, argtypes)
 SIGNATURES = {
     "cs_module_load": (ctypes.c_int, [ctypes.POINTER(ModuleDesc), ctypes.POINTER(ctypes.c_void_p)]),
@@ -72,6 +77,7 @@ SIGNATURES = {
     "cs_measure_fp64_peak": (ctypes.c_int, [_dp]),
     "cs_profiler_start": (ctypes.c_int, []),
     "cs_batch_set_opts": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "cs_autotune_condense": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(TuneResult)]),
     "cs_profiler_stop": (ctypes.c_int, []),
     "cs_batch_reset": (ctypes.c_int, [ctypes.c_void_p]),
     "cs_profile_reset": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),

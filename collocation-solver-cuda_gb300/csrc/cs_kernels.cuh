@@ -827,9 +827,9 @@ __device__ void cs_condense_group(const CsBatch& bt, int slot, bool active, doub
 // lanes per condensation group, from the size of the stage system
 #define CS_CGL ((CS_S1 > 48) ? 256 : ((CS_S1 > 16) ? 16 : 8))
 
+template <int GL>
 __device__ __forceinline__ void cs_condense_entry(const CsBatch& bt) {
   extern __shared__ double smem[];
-  constexpr int GL = CS_CGL;
   const int njac = bt.nlist[1];
   const long long total = bt.jac_pre[njac];
   if (total == 0) return;
@@ -862,7 +862,13 @@ __device__ __forceinline__ void cs_condense_entry(const CsBatch& bt) {
   }
 }
 
-extern "C" __global__ void k_condense(CsBatch bt) { cs_condense_entry(bt); }
+extern "C" __global__ void k_condense(CsBatch bt) { cs_condense_entry<CS_CGL>(bt); }
+#if CS_S1 <= 48
+// the tuner's candidates: 8, 16 or 32 lanes per interval
+extern "C" __global__ void k_condense_l8(CsBatch bt) { cs_condense_entry<8>(bt); }
+extern "C" __global__ void k_condense_l16(CsBatch bt) { cs_condense_entry<16>(bt); }
+extern "C" __global__ void k_condense_l32(CsBatch bt) { cs_condense_entry<32>(bt); }
+#endif
 #endif  // !CS_BIG_COND
 
 // ------------------------------------------------------------------------

@@ -277,6 +277,11 @@ struct cs_module {
   long long slab = 0;  // doubles per CTA
   int big_ctas = 0;    // CTAs with a slab (the largest grid of the slab kernels)
   int tree_grid = 0;   // k_tree_level grid (large systems)
+  // condensation shape tuner
+  CUfunction f_cond_l[3] = {nullptr, nullptr, nullptr};  // 8, 16, 32 lanes per interval
+  size_t grp_bytes = 0;  // shared memory of one interval group (shared-memory kernel)
+  int smem_optin = 0;
+  int tune_ver = 0;      // bumped when the tuner changes the shape (graphs re-captured)
 };
 
 static std::string build_source(const cs_module_desc* d, bool big_cond, bool big_tree, int prec, int smem_max) {
@@ -400,6 +405,8 @@ extern "C" int cs_module_load(const cs_module_desc* d, cs_module** out) {
   M->big_tree = d->layout == 2 || (d->layout == 0 && !fits_tree);
   M->big = M->big_cond || M->big_tree;
   M->cgw = gl;
+  M->grp_bytes = grp;
+  M->smem_optin = smem_optin;
   int smem_sm = 0;
   CS_CUDA(cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev));
   CS_CUDA(cudaDeviceGetAttribute(&M->sms, cudaDevAttrMultiProcessorCount, dev));
@@ -501,6 +508,11 @@ extern "C" int cs_module_load(const cs_module_desc* d, cs_module** out) {
       return set_err(CS_ERR_CUDA, std::string("missing kernel ") + e.name);
     }
   }
+  {
+    const char* names[3] = {"k_condense_l8", "k_condense_l16", "k_condense_l32"};
+    for (int k = 0; k < 3; ++k)
+      if (g_drv.moduleGetFunction(&M->f_cond_l[k], M->mod, names[k]) != CUDA_SUCCESS) M->f_cond_l[k] = nullptr;
+  }
   if (M->condense_smem > 48 * 1024)
     CS_CU(g_drv.funcSetAttribute(M->f_condense, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, (int)M->condense_smem));
   if (M->tree_smem > 48 * 1024)
@@ -593,6 +605,7 @@ struct cs_batch {
   // 1 one CTA per instance)
   cudaGraphExec_t graph[2] = {nullptr, nullptr};
   int graph_nlvl[2] = {-1, -1};
+  int graph_tune[2] = {-1, -1};
   CsBatchDev graph_view[2];
   CsConsts graph_consts[2];
   int cta_now = -1;  // automatic path choice of the running solve (-1: none)
@@ -1098,8 +1111,8 @@ static int super_step(cs_batch* bt, const CsConsts& c, int nlvl) {
 static int get_graph(cs_batch* bt, const CsConsts& c, int nlvl, int reps) {
   const CsBatchDev v = devview(bt);
   const int k = use_cta_path(bt) ? 1 : 0;
-  if (bt->graph[k] && bt->graph_nlvl[k] == nlvl && memcmp(&bt->graph_view[k], &v, sizeof(v)) == 0 &&
-      memcmp(&bt->graph_consts[k], &c, sizeof(c)) == 0)
+  if (bt->graph[k] && bt->graph_nlvl[k] == nlvl && bt->graph_tune[k] == bt->M->tune_ver &&
+      memcmp(&bt->graph_view[k], &v, sizeof(v)) == 0 && memcmp(&bt->graph_consts[k], &c, sizeof(c)) == 0)
     return CS_OK;
   if (bt->graph[k]) {
     cudaGraphExecDestroy(bt->graph[k]);
@@ -1124,6 +1137,7 @@ static int get_graph(cs_batch* bt, const CsConsts& c, int nlvl, int reps) {
   bt->graph_view[k] = v;
   bt->graph_consts[k] = c;
   bt->graph_nlvl[k] = nlvl;
+  bt->graph_tune[k] = bt->M->tune_ver;
   return CS_OK;
 }
 
@@ -1640,4 +1654,89 @@ extern "C" int cs_profiler_stop(void) {
   CS_CUDA(cudaDeviceSynchronize());
   CS_CUDA(cudaProfilerStop());
   return CS_OK;
+}
+
+extern "C" int cs_autotune_condense(cs_batch* bt, int reps, cs_tune_result* out) {
+  if (!bt || !bt->have_guess || reps < 1) return set_err(CS_ERR_INVALID, "cs_autotune_condense: bad argument");
+  cs_module* M = bt->M;
+  CS_TRY(set_all_status(bt, ST_FRESH, bt->opts.alpha0, 1));
+  CsBatchDev v = devview(bt);
+  CS_TRY(run_lists(bt, v, 1, 0));
+  struct Cand {
+    CUfunction f;
+    int lanes, block, grid;
+    size_t smem;
+  };
+  std::vector<Cand> cands;
+  cands.push_back({M->f_condense, M->big_cond ? 0 : M->cgw, M->condense_block, M->condense_grid, M->condense_smem});
+  if (!M->big_cond) {
+    const int lanes[3] = {8, 16, 32};
+    for (int k = 0; k < 3; ++k) {
+      if (!M->f_cond_l[k]) continue;
+      const int gpw = 32 / lanes[k];
+      for (int w = 1; w <= 8; w *= 2) {
+        const size_t smem = M->grp_bytes * gpw * w;
+        if (smem > (size_t)M->smem_optin) break;
+        if (smem > 48 * 1024)
+          CS_CU(g_drv.funcSetAttribute(M->f_cond_l[k], CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, (int)smem));
+        int per_sm = 0;
+        CS_CU(g_drv.occupancy(&per_sm, M->f_cond_l[k], 32 * w, smem));
+        if (per_sm < 1) continue;
+        cands.push_back({M->f_cond_l[k], lanes[k], 32 * w, M->sms * per_sm, smem});
+      }
+    }
+  } else {
+    // one CTA per interval: CTA size; the grid stays within the CTAs that
+    // have a slab in this batch
+    for (int block = 128; block <= 256; block *= 2) {
+      int per_sm = 0;
+      CS_CU(g_drv.occupancy(&per_sm, M->f_condense, block, M->condense_smem));
+      const int grid = std::min(M->sms * std::max(1, per_sm), M->big_ctas);
+      cands.push_back({M->f_condense, 0, block, grid, M->condense_smem});
+    }
+  }
+  cudaEvent_t e0, e1;
+  CS_CUDA(cudaEventCreate(&e0));
+  CS_CUDA(cudaEventCreate(&e1));
+  double best = 1e300, first = 0.0;
+  size_t bi = 0;
+  for (size_t i = 0; i < cands.size(); ++i) {
+    const Cand& c = cands[i];
+    void* args[] = {&v};
+    CS_CU(g_drv.launchKernel(c.f, c.grid, 1, 1, c.block, 1, 1, (unsigned)c.smem, (CUstream)bt->stream, args, nullptr));
+    CS_CUDA(cudaEventRecord(e0, bt->stream));
+    for (int r = 0; r < reps; ++r)
+      CS_CU(g_drv.launchKernel(c.f, c.grid, 1, 1, c.block, 1, 1, (unsigned)c.smem, (CUstream)bt->stream, args, nullptr));
+    CS_CUDA(cudaEventRecord(e1, bt->stream));
+    CS_CUDA(cudaEventSynchronize(e1));
+    float t = 0.f;
+    CS_CUDA(cudaEventElapsedTime(&t, e0, e1));
+    const double ms = (double)t / reps;
+    if (i == 0) first = ms;
+    if (ms < best) {
+      best = ms;
+      bi = i;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  CS_TRY(check_config(bt));
+  const Cand& b = cands[bi];
+  if (bi != 0) {
+    M->f_condense = b.f;
+    M->condense_block = b.block;
+    M->condense_grid = b.grid;
+    M->condense_smem = b.smem;
+    if (!M->big_cond) M->cgw = b.lanes;
+    M->tune_ver += 1;
+  }
+  if (out) {
+    out->lanes = b.lanes;
+    out->block = b.block;
+    out->grid = b.grid;
+    out->candidates = (int)cands.size();
+    out->ms = best;
+    out->default_ms = first;
+  }
+  return set_all_status(bt, ST_FRESH, bt->opts.alpha0, 0);
 }

@@ -302,6 +302,14 @@ class Batch:
         _lib.check(self._lib.cs_batch_warm_start(self.handle, int(n_nodes), ctypes.c_void_p(ptr), int(stride)),
                    "cs_batch_warm_start")
 
+    def autotune(self, reps=3):
+        """Time the condensation's launch shapes on this batch's intervals and
+        keep the fastest for the compiled problem (all its batches)."""
+        r = _lib.TuneResult()
+        _lib.check(self._lib.cs_autotune_condense(self.handle, int(reps), ctypes.byref(r)), "cs_autotune_condense")
+        return dict(lanes=r.lanes, block=r.block, grid=r.grid, candidates=r.candidates, ms=r.ms,
+                    default_ms=r.default_ms)
+
     def time_condense(self, reps=10):
         ms = ctypes.c_double()
         _lib.check(self._lib.cs_time_condense(self.handle, int(reps), ctypes.byref(ms)), "cs_time_condense")

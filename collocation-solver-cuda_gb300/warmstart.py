@@ -153,6 +153,32 @@ def pendulum_family(K=8):
                   final_time=lambda i: i.T, plain_guess=lambda i: i.guess(ny, nz, npar), name="pendulum%d" % K)
 
 
+def write_guess_file(family, mlp, instance, path, n_nodes=None):
+    """The network's trajectory for one instance, on its plain mesh (or
+    n_nodes equispaced nodes), as a BVPDAEReadWriteData file: an OCP names it
+    as InputFile to start from the learned guess.  Returns the status of the
+    writer (0 on success)."""
+    from .io import bvpdae_write_data
+    X = np.array([family.features(instance)], np.float32)
+    v = mlp.predict(X)[0].astype(np.float64)
+    T = family.final_time(instance)
+    t = family.plain_guess(instance)[0] if n_nodes is None else np.linspace(0.0, T, n_nodes)
+    y, z, p = guess_from_vector(v, t, T, family.ny, family.nz, family.np)
+    return bvpdae_write_data(path, len(t), family.ny, family.nz, family.np, t, y, z, p)
+
+
+def write_solution_files(batch, path_fmt):
+    """Every instance's solution of a solved Batch as a BVPDAEReadWriteData
+    file: path_fmt % b names instance b's file.  Returns the list of writer
+    statuses."""
+    from .io import bvpdae_write_data
+    cp = batch.cp
+    out = []
+    for b, s in enumerate(batch.solution()):
+        out.append(bvpdae_write_data(path_fmt % b, s["N"], cp.ny, cp.nz, cp.np, s["t"], s["y"], s["z"], s["p"]))
+    return out
+
+
 def pack_family(family, instances):
     """Packed host arrays (N, t, y, z, p, theta) of the plain guesses."""
     parts = [family.plain_guess(i) for i in instances]

@@ -305,6 +305,22 @@ int cs_last_error(char* buf, size_t len);
  * milliseconds, with CUDA events on the batch's stream (for roofline figures). */
 int cs_time_condense(cs_batch* bt, int reps, double* ms);
 
+/* Launch-shape tuner of the condensation (the per-(m, ny) tile shape):
+ * times every candidate on the batch's current intervals -- 8, 16 or 32
+ * lanes per interval x 1..8 warps per CTA for shared-memory stage systems,
+ * 128 or 256 threads per CTA for the large-system kernel -- and makes the
+ * fastest the module's shape for all its batches.  No reference
+ * counterpart. */
+typedef struct cs_tune_result {
+  int lanes;          /* lanes per interval, 0: one CTA per interval */
+  int block;          /* threads per CTA */
+  int grid;           /* CTAs of the persistent grid */
+  int candidates;     /* shapes timed */
+  double ms;          /* one condensation of the batch, chosen shape */
+  double default_ms;  /* ... with the shape chosen from occupancy rules */
+} cs_tune_result;
+int cs_autotune_condense(cs_batch* bt, int reps, cs_tune_result* out);
+
 /* FP64 FMA throughput of this GPU, measured by a register-resident DFMA loop
  * (TFLOP/s, counting an FMA as 2 flops); the denominator of FP64 roofline
  * fractions. */

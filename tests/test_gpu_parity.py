@@ -232,3 +232,28 @@ def test_end_to_end_residual2_matches_reference(cs):
     np.testing.assert_array_equal(sol["t"], g["t"])
     np.testing.assert_allclose(sol["y"], g["y"], atol=1e-8, rtol=0)
     np.testing.assert_allclose(sol["z"], g["z"], atol=1e-8, rtol=0)
+
+
+def test_autotuned_condensation_gives_identical_solves(cs):
+    """The shape tuner times its candidates on the batch and keeps the
+    fastest; every candidate performs the same per-entry elimination, so the
+    tuned solve is bit-identical to the untuned one."""
+    pr = load_problem("vdp_family")
+    cp = cs.CompiledProblem(pr, 4)
+    insts = cs.workloads.vdp_batch(64, seed=21, n_range=(32, 400), m_choices=(4,))
+    fam = cs.warmstart.vdp_family()
+    N, t, y, z, p, th = cs.warmstart.pack_family(fam, insts)
+    bt = cs.Batch(cp, len(insts))
+    bt.set_guess_packed(N, t, y, z, p, th)
+    opts = cs.default_opts(pr, max_nodes=20000)
+    bt.solve(opts)
+    before = bt.solution()
+    bt.reset()
+    r = bt.autotune(reps=2)
+    assert r["candidates"] >= 2 and r["lanes"] in (8, 16, 32) and r["ms"] <= r["default_ms"]
+    bt.reset()
+    bt.solve(opts)
+    after = bt.solution()
+    for s0, s1 in zip(before, after):
+        assert (s0["newton_steps"], s0["residual_evals"], s0["N"]) == (s1["newton_steps"], s1["residual_evals"], s1["N"])
+        np.testing.assert_array_equal(s0["y"], s1["y"])

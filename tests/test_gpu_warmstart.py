@@ -109,3 +109,35 @@ def test_pendulum_family_warm_start_gains_over_plain_guess():
     for s in final:
         if s["success"]:
             assert s["last_norm"] < 1e-6 and s["max_residual"] <= 1.0
+
+
+def test_guess_and_solution_files_round_trip(tmp_path):
+    """An MLP guess written as a solution file is read back by the OCP front
+    end as InputFile; a batch's solutions written per instance read back
+    exactly (the reference's reader format)."""
+    cs = pkg()
+    ws = cs.warmstart
+    fam = ws.vdp_family()
+    inst = cs.workloads.vdp_batch(1, seed=3, n_range=(40, 40), m_choices=(4,))[0]
+    net = ws.Mlp(4, fam.n_out, width=64, depth=3, seed=0)
+    path = str(tmp_path / "guess.data")
+    assert ws.write_guess_file(fam, net, inst, path) == 0
+    err, t, y, z, p = cs.io.bvpdae_read_data(path)
+    assert err == 0 and t.shape == (41,) and y.shape == (41, fam.ny) and z.shape == (41, fam.nz)
+    text = open(cs.workloads.VDP_FAMILY_OCP).read().replace("OutputFile", 'InputFile = "%s";\nOutputFile' % path)
+    pr = cs.ocp.Problem(text, name="vdp_from_guess")
+    np.testing.assert_array_equal(pr.T0, t)
+    # per-instance solution files of a solved batch
+    solver = ws.BatchSolver(fam)
+    insts = cs.workloads.vdp_batch(3, seed=4, n_range=(32, 48), m_choices=(4,))
+    N, tt, yy, zz, pp, th = ws.pack_family(fam, insts)
+    bt = cs.Batch(solver.cp(4), 3)
+    bt.set_guess_packed(N, tt, yy, zz, pp, th)
+    bt.solve(solver.opts)
+    st = ws.write_solution_files(bt, str(tmp_path / "sol_%d.data"))
+    assert st == [0, 0, 0]
+    for b, s in enumerate(bt.solution()):
+        err, t2, y2, z2, p2 = cs.io.bvpdae_read_data(str(tmp_path / ("sol_%d.data" % b)))
+        assert err == 0
+        np.testing.assert_array_equal(t2, s["t"])
+        np.testing.assert_array_equal(y2, s["y"])
