@@ -869,7 +869,7 @@ def main():
     ap.add_argument("--family", default="vdp", choices=["vdp", "pendulum8"],
                     help="warm-start family (warm workload and its reference arm)")
     ap.add_argument("--pendulum", type=int, default=16, choices=[16, 32], help="chain length K (pendulum)")
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "tf32", "bf16"],
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "tf32", "bf16", "tf32-tree", "bf16-tree"],
                     help="pendulum: precision of the large-system condensation")
     ap.add_argument("--batch", type=int, default=None, help="instances per step (warm: 8192, plain: 4096)")
     ap.add_argument("--train", type=int, default=65536, help="training solutions (warm)")

@@ -143,6 +143,12 @@ struct CsBatch {
 #ifndef CS_PREC
 #define CS_PREC 0
 #endif
+// precision of the large-system tree merges: 0 FP64, 1 TF32, 2 BF16 (an
+// option only: the merges' rounding makes the Newton direction too inexact,
+// measured on the pendulum chains)
+#ifndef CS_PREC_TREE
+#define CS_PREC_TREE 0
+#endif
 #ifndef CS_SMEM_MAX
 #define CS_SMEM_MAX 232448
 #endif
@@ -1433,7 +1439,28 @@ extern "C" __global__ void k_babd_cta(CsBatch bt, int recover) {}
 #define CS_WS_TREE (CS_Q_SMEM ? 0ll : (long long)CS_QSZ)
 #define CS_WS_TOP ((CS_T_SMEM ? 0ll : (long long)CS_TSZ) + (long long)CS_DRSZ)
 #define CS_SM_TREE ((CS_Q_SMEM ? CS_QSZ : 0) + CS_SM_HB)
+// reduced precision (CS_PREC_TREE != 0): FP32 merge matrix; shared floats V [HB][QLD] |
+// T, G [HB][HB] | tau [HB] | W [QC][HB], then red [32] doubles
+#define CS_SHF (CS_HB * CS_QLD + 2 * CS_HB * CS_HB + CS_HB + CS_QC * CS_HB)
+#define CS_SM_HB_LP ((CS_SHF + 1) / 2 + 32)
+#define CS_QSZ_LP ((CS_QSZ + 1) / 2)
+#define CS_Q_SMEM_LP (((long long)CS_QSZ_LP + CS_SM_HB_LP) * 8 <= CS_SMEM_MAX)
+#define CS_WS_TREE_LP (CS_Q_SMEM_LP ? 0ll : (long long)CS_QSZ_LP)
+#define CS_SM_TREE_LP ((CS_Q_SMEM_LP ? CS_QSZ_LP : 0) + CS_SM_HB_LP)
 #define CS_SM_TOP ((CS_T_SMEM ? CS_TSZ : 0) + 32)
+
+// tensor-core operands: FP32 rounded to TF32 (round to nearest, ties away),
+// or two FP32 rounded to a BF16 pair (lo in the low half)
+__device__ __forceinline__ unsigned cs_tf32(float x) {
+  unsigned r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+  return r;
+}
+__device__ __forceinline__ unsigned cs_bf2(float lo, float hi) {
+  unsigned r;
+  asm("cvt.rn.bf16x2.f32 %0, %1, %2;" : "=r"(r) : "f"(hi), "f"(lo));
+  return r;
+}
 
 __device__ __forceinline__ unsigned cs_dyn_smem_bytes() {
   unsigned r;
@@ -1524,19 +1551,6 @@ __device__ __forceinline__ unsigned long long cs_abskey(float v) {
 }
 __device__ __forceinline__ bool cs_tiny(double v) { return cs_abskey(v) < 0x3ce4000000000000ull; }
 __device__ __forceinline__ bool cs_tiny(float v) { return fabsf(v) < 2.220446049250313e-15f; }
-
-// tensor-core operands: FP32 rounded to TF32 (round to nearest, ties away),
-// or two FP32 rounded to a BF16 pair (lo in the low half)
-__device__ __forceinline__ unsigned cs_tf32(float x) {
-  unsigned r;
-  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
-  return r;
-}
-__device__ __forceinline__ unsigned cs_bf2(float lo, float hi) {
-  unsigned r;
-  asm("cvt.rn.bf16x2.f32 %0, %1, %2;" : "=r"(r) : "f"(hi), "f"(lo));
-  return r;
-}
 
 // A22 -= L21 U12 on the tensor cores for the mixed-precision condensation:
 // warp items of 16 rows x 32 columns (four m16n8 tiles), FP32 accumulators
@@ -2110,11 +2124,229 @@ __device__ void cs_merge_cta(const double* ra, const double* rb, double* out_row
   __syncthreads();
 }
 
+#if CS_PREC_TREE != 0
+// sum over the CTA in FP32 (red: 8 doubles of scratch)
+__device__ __forceinline__ float cs_cta_sumf(float v, double* red) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  float* rf = reinterpret_cast<float*>(red);
+  if ((threadIdx.x & 31) == 0) rf[threadIdx.x >> 5] = v;
+  __syncthreads();
+  float s = 0.f;
+  for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += rf[w];
+  __syncthreads();
+  return s;
+}
+
+// The merge of cs_merge_cta in reduced precision: FP32 merge matrix and
+// reflectors, the two products of each panel's WY update on the tensor cores
+// (FP32 accumulators): W = V^T C (k = the rows), then C -= V (T^T W) (k = the
+// panel's 16 reflectors); operands rounded to TF32 (PREC 1) or BF16 (PREC 2).
+// The top system and the back substitution stay FP64.
+template <int PREC>
+__device__ void cs_merge_cta_lp(const double* ra, const double* rb, double* out_row, double* rec, float* Q, double* sh) {
+  const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, w = tid >> 5, nw = nt >> 5;
+  const int g = lane >> 2, t = lane & 3;
+  constexpr int n = 2 * CS_NY;
+  float* V = reinterpret_cast<float*>(sh);  // [HB][QLD]
+  float* Tm = V + CS_HB * CS_QLD;           // T[j][i] at Tm[i * HB + j]
+  float* G = Tm + CS_HB * CS_HB;
+  float* tau = G + CS_HB * CS_HB;
+  float* Wm = tau + CS_HB;                  // [QC][HB]
+  double* red = sh + (CS_SHF + 1) / 2;
+  for (int e = tid; e < CS_QC * CS_NY; e += nt) {
+    const int c = e / CS_NY, r = e - c * CS_NY;
+    double top, bot;
+    if (c < CS_NY) { top = ra[(CS_NY + c) * CS_NY + r]; bot = rb[c * CS_NY + r]; }
+    else if (c < 2 * CS_NY) { top = ra[(c - CS_NY) * CS_NY + r]; bot = 0.0; }
+    else if (c < 3 * CS_NY) { top = 0.0; bot = rb[(CS_NY + c - 2 * CS_NY) * CS_NY + r]; }
+    else if (c < 3 * CS_NY + CS_NPE) { top = ra[(2 * CS_NY + c - 3 * CS_NY) * CS_NY + r]; bot = rb[(2 * CS_NY + c - 3 * CS_NY) * CS_NY + r]; }
+    else { top = ra[(2 * CS_NY + CS_NPE) * CS_NY + r]; bot = rb[(2 * CS_NY + CS_NPE) * CS_NY + r]; }
+    Q[(size_t)c * CS_QLD + r] = (float)top;
+    Q[(size_t)c * CS_QLD + CS_NY + r] = (float)bot;
+  }
+  __syncthreads();
+#pragma unroll 1
+  for (int k0 = 0; k0 < CS_NY; k0 += CS_HB) {
+    const int kb = min(CS_HB, CS_NY - k0);
+    const int pe = k0 + kb;
+    // ---- panel (FP32, as cs_merge_cta)
+#pragma unroll 1
+    for (int kk = 0; kk < kb; ++kk) {
+      const int k = k0 + kk;
+      float* vk = Q + (size_t)k * CS_QLD;
+      float ss = 0.f;
+      for (int r = k + tid; r < n; r += nt) ss = fmaf(vk[r], vk[r], ss);
+      ss = cs_cta_sumf(ss, red);
+      const float x0 = vk[k];
+      const float gg = (x0 >= 0.f) ? -sqrtf(ss) : sqrtf(ss);
+      const float v0 = x0 - gg;
+      const float vs = ss - x0 * x0 + v0 * v0;
+      float* Vi = V + kk * CS_QLD;
+      if ((double)vs < CS_EPS) {
+        for (int r = tid; r < n; r += nt) Vi[r] = 0.f;
+        if (tid == 0) tau[kk] = 0.f;
+        __syncthreads();
+        continue;
+      }
+      const float beta = -2.f / vs;
+      for (int r = tid; r < n; r += nt) Vi[r] = (r < k) ? 0.f : ((r == k) ? v0 : vk[r]);
+      if (tid == 0) tau[kk] = 2.f / vs;
+      for (int c = k + 1 + w; c < pe; c += nw) {
+        float* col = Q + (size_t)c * CS_QLD;
+        float wv = (lane == 0) ? v0 * col[k] : 0.f;
+        for (int r = k + 1 + lane; r < n; r += 32) wv = fmaf(vk[r], col[r], wv);
+        for (int o = 16; o > 0; o >>= 1) wv += __shfl_xor_sync(0xffffffffu, wv, o);
+        const float bw = beta * wv;
+        if (lane == 0) col[k] = fmaf(bw, v0, col[k]);
+        for (int r = k + 1 + lane; r < n; r += 32) col[r] = fmaf(bw, vk[r], col[r]);
+      }
+      __syncthreads();
+      if (tid == 0) vk[k] = gg;
+      for (int r = k + 1 + tid; r < n; r += nt) vk[r] = 0.f;
+      __syncthreads();
+    }
+    for (int e = tid; e < (CS_HB - kb) * CS_QLD; e += nt) V[kb * CS_QLD + e] = 0.f;
+    for (int e = tid; e < (CS_HB - kb) * CS_HB; e += nt) Tm[kb * CS_HB + e] = 0.f;
+    for (int e = tid; e < kb * kb; e += nt) {
+      const int i = e / kb, j = e - i * kb;
+      if (j < i) {
+        const float* vi = V + i * CS_QLD;
+        const float* vj = V + j * CS_QLD;
+        float d = 0.f;
+        for (int r = k0 + i; r < n; ++r) d = fmaf(vj[r], vi[r], d);
+        G[i * CS_HB + j] = d;
+      }
+    }
+    __syncthreads();
+    if (tid == 0) {
+      for (int i = 0; i < kb; ++i) {
+        const float ti = tau[i];
+        for (int j = 0; j < i; ++j) {
+          float sj = 0.f;
+          for (int q = j; q < i; ++q) sj = fmaf(Tm[q * CS_HB + j], G[i * CS_HB + q], sj);
+          Tm[i * CS_HB + j] = -ti * sj;
+        }
+        Tm[i * CS_HB + i] = ti;
+      }
+    }
+    __syncthreads();
+    const int nc = CS_QC - pe;
+    // ---- W = V^T C: 16 reflectors x 8-column tiles, k over the rows
+    auto Va = [&](int i, int r) -> float { return (r < n) ? V[i * CS_QLD + r] : 0.f; };
+    auto Cb = [&](int r, int c) -> float { return (r < n && c < nc) ? Q[(size_t)(pe + c) * CS_QLD + r] : 0.f; };
+    for (int tile = w; tile < (nc + 7) / 8; tile += nw) {
+      const int cb = tile * 8;
+      float acc[4] = {0.f, 0.f, 0.f, 0.f};
+      if constexpr (PREC == 1) {
+        for (int r0 = k0; r0 < n; r0 += 8) {
+          const unsigned a0 = cs_tf32(Va(g, r0 + t)), a1 = cs_tf32(Va(g + 8, r0 + t));
+          const unsigned a2 = cs_tf32(Va(g, r0 + t + 4)), a3 = cs_tf32(Va(g + 8, r0 + t + 4));
+          const unsigned b0 = cs_tf32(Cb(r0 + t, cb + g)), b1 = cs_tf32(Cb(r0 + t + 4, cb + g));
+          asm volatile("mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+                       "{%0,%1,%2,%3};\n"
+                       : "+f"(acc[0]), "+f"(acc[1]), "+f"(acc[2]), "+f"(acc[3])
+                       : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+        }
+      } else {
+        for (int r0 = k0; r0 < n; r0 += 16) {
+          const unsigned a0 = cs_bf2(Va(g, r0 + 2 * t), Va(g, r0 + 2 * t + 1));
+          const unsigned a1 = cs_bf2(Va(g + 8, r0 + 2 * t), Va(g + 8, r0 + 2 * t + 1));
+          const unsigned a2 = cs_bf2(Va(g, r0 + 2 * t + 8), Va(g, r0 + 2 * t + 9));
+          const unsigned a3 = cs_bf2(Va(g + 8, r0 + 2 * t + 8), Va(g + 8, r0 + 2 * t + 9));
+          const unsigned b0 = cs_bf2(Cb(r0 + 2 * t, cb + g), Cb(r0 + 2 * t + 1, cb + g));
+          const unsigned b1 = cs_bf2(Cb(r0 + 2 * t + 8, cb + g), Cb(r0 + 2 * t + 9, cb + g));
+          asm volatile("mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+                       "{%0,%1,%2,%3};\n"
+                       : "+f"(acc[0]), "+f"(acc[1]), "+f"(acc[2]), "+f"(acc[3])
+                       : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int i = g + ((q & 2) ? 8 : 0), c = cb + 2 * t + (q & 1);
+        if (c < nc) Wm[c * CS_HB + i] = acc[q];
+      }
+    }
+    __syncthreads();
+    // ---- W <- T^T W, a column per thread
+    for (int c = tid; c < nc; c += nt) {
+      float wv[CS_HB];
+#pragma unroll
+      for (int i = 0; i < CS_HB; ++i) wv[i] = Wm[c * CS_HB + i];
+#pragma unroll
+      for (int i = 0; i < CS_HB; ++i) {
+        float sacc = 0.f;
+#pragma unroll
+        for (int j = 0; j <= i; ++j) sacc = fmaf(Tm[i * CS_HB + j], wv[j], sacc);
+        Wm[c * CS_HB + i] = sacc;
+      }
+    }
+    __syncthreads();
+    // ---- C -= V W: 16-row x 8-column tiles over rows k0.. and the columns
+    const int nr = n - k0;
+    const int rt = (nr + 15) / 16, ct = (nc + 7) / 8;
+    auto Am = [&](int r, int i) -> float { return (r < nr) ? -V[i * CS_QLD + k0 + r] : 0.f; };
+    auto Bw = [&](int i, int c) -> float { return (c < nc) ? Wm[c * CS_HB + i] : 0.f; };
+    for (int item = w; item < rt * ct; item += nw) {
+      const int ri = item / ct, ci = item - ri * ct;
+      const int ra = ri * 16, cb = ci * 8;
+      float acc[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int r = ra + g + ((q & 2) ? 8 : 0), c = cb + 2 * t + (q & 1);
+        acc[q] = (r < nr && c < nc) ? Q[(size_t)(pe + c) * CS_QLD + k0 + r] : 0.f;
+      }
+      if constexpr (PREC == 1) {
+#pragma unroll
+        for (int ks = 0; ks < CS_HB; ks += 8) {
+          const unsigned a0 = cs_tf32(Am(ra + g, ks + t)), a1 = cs_tf32(Am(ra + g + 8, ks + t));
+          const unsigned a2 = cs_tf32(Am(ra + g, ks + t + 4)), a3 = cs_tf32(Am(ra + g + 8, ks + t + 4));
+          const unsigned b0 = cs_tf32(Bw(ks + t, cb + g)), b1 = cs_tf32(Bw(ks + t + 4, cb + g));
+          asm volatile("mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+                       "{%0,%1,%2,%3};\n"
+                       : "+f"(acc[0]), "+f"(acc[1]), "+f"(acc[2]), "+f"(acc[3])
+                       : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+        }
+      } else {
+        const unsigned a0 = cs_bf2(Am(ra + g, 2 * t), Am(ra + g, 2 * t + 1));
+        const unsigned a1 = cs_bf2(Am(ra + g + 8, 2 * t), Am(ra + g + 8, 2 * t + 1));
+        const unsigned a2 = cs_bf2(Am(ra + g, 2 * t + 8), Am(ra + g, 2 * t + 9));
+        const unsigned a3 = cs_bf2(Am(ra + g + 8, 2 * t + 8), Am(ra + g + 8, 2 * t + 9));
+        const unsigned b0 = cs_bf2(Bw(2 * t, cb + g), Bw(2 * t + 1, cb + g));
+        const unsigned b1 = cs_bf2(Bw(2 * t + 8, cb + g), Bw(2 * t + 9, cb + g));
+        asm volatile("mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+                     "{%0,%1,%2,%3};\n"
+                     : "+f"(acc[0]), "+f"(acc[1]), "+f"(acc[2]), "+f"(acc[3])
+                     : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+      }
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int r = ra + g + ((q & 2) ? 8 : 0), c = cb + 2 * t + (q & 1);
+        if (r < nr && c < nc) Q[(size_t)(pe + c) * CS_QLD + k0 + r] = acc[q];
+      }
+    }
+    __syncthreads();
+  }
+  for (int e = tid; e < CS_QC * CS_NY; e += nt) {
+    const int c = e / CS_NY, r = e - c * CS_NY;
+    rec[e] = (double)Q[(size_t)c * CS_QLD + r];
+    if (c >= CS_NY) out_row[(size_t)(c - CS_NY) * CS_NY + r] = (double)Q[(size_t)c * CS_QLD + CS_NY + r];
+  }
+  __syncthreads();
+}
+#endif  // CS_PREC_TREE != 0
+
 extern "C" __global__ void __launch_bounds__(256) k_tree_level(CsBatch bt, int l) {
   extern __shared__ double smem[];
+#if CS_PREC_TREE == 0
   if (!cs_big_ok(bt, CS_WS_TREE, CS_SM_TREE)) return;
   double* Q = CS_Q_SMEM ? smem : bt.wsp + (size_t)blockIdx.x * bt.wsp_stride;
   double* sh = CS_Q_SMEM ? smem + CS_QSZ : smem;
+#else
+  if (!cs_big_ok(bt, CS_WS_TREE_LP, CS_SM_TREE_LP)) return;
+  float* Q = reinterpret_cast<float*>(CS_Q_SMEM_LP ? smem : bt.wsp + (size_t)blockIdx.x * bt.wsp_stride);
+  double* sh = CS_Q_SMEM_LP ? smem + CS_QSZ_LP : smem;
+#endif
   const int njac = bt.nlist[1];
   const long long* pre = bt.lvl_pre + (size_t)l * (bt.B + 1);
   const long long total = pre[njac];
@@ -2130,8 +2362,14 @@ extern "C" __global__ void __launch_bounds__(256) k_tree_level(CsBatch bt, int l
     const double* src = srcb + (size_t)off * CS_ROWSZ;
     double* dst = dstb + (size_t)off * CS_ROWSZ;
     if (mi < merges) {
+#if CS_PREC_TREE == 0
       cs_merge_cta(src + (size_t)(2 * mi) * CS_ROWSZ, src + (size_t)(2 * mi + 1) * CS_ROWSZ, dst + (size_t)mi * CS_ROWSZ,
                    bt.tree + (size_t)(off + ((2 * mi + 1) << l)) * CS_TREESZ, Q, sh);
+#else
+      cs_merge_cta_lp<CS_PREC_TREE>(src + (size_t)(2 * mi) * CS_ROWSZ, src + (size_t)(2 * mi + 1) * CS_ROWSZ,
+                               dst + (size_t)mi * CS_ROWSZ, bt.tree + (size_t)(off + ((2 * mi + 1) << l)) * CS_TREESZ, Q,
+                               sh);
+#endif
     } else {
       const double* sr = src + (size_t)(nl - 1) * CS_ROWSZ;
       double* dr = dst + (size_t)merges * CS_ROWSZ;

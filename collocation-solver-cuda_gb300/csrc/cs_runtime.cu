@@ -273,7 +273,8 @@ struct cs_module {
   int condense_grid = 1;
   // large stage systems: kernels with a global-memory slab per CTA
   bool big = false, big_cond = false, big_tree = false;
-  int prec = 0;  // large-system condensation: 0 FP64, 1 TF32, 2 BF16
+  int prec = 0;       // large-system condensation: 0 FP64, 1 TF32, 2 BF16
+  int prec_tree = 0;  // large-system tree merges: 0 FP64, 1 TF32, 2 BF16
   long long slab = 0;  // doubles per CTA
   int big_ctas = 0;    // CTAs with a slab (the largest grid of the slab kernels)
   int tree_grid = 0;   // k_tree_level grid (large systems)
@@ -284,7 +285,8 @@ struct cs_module {
   int tune_ver = 0;      // bumped when the tuner changes the shape (graphs re-captured)
 };
 
-static std::string build_source(const cs_module_desc* d, bool big_cond, bool big_tree, int prec, int smem_max) {
+static std::string build_source(const cs_module_desc* d, bool big_cond, bool big_tree, int prec, int prec_tree,
+                                int smem_max) {
   std::ostringstream o;
   o << "// generated prelude\n";
   o << "#define CS_NY " << d->ny << "\n#define CS_NZ " << d->nz << "\n#define CS_NP " << d->np << "\n";
@@ -293,6 +295,7 @@ static std::string build_source(const cs_module_desc* d, bool big_cond, bool big
   if (big_tree) o << "#define CS_BIG_TREE 1\n";
   if (big_cond || big_tree) o << "#define CS_SMEM_MAX " << smem_max << "\n";
   if (prec) o << "#define CS_PREC " << prec << "\n";
+  if (prec_tree) o << "#define CS_PREC_TREE " << prec_tree << "\n";
   const int m = d->m;
   o << "__constant__ double CS_A[" << m * m << "] = {" << fmt_array(d->lobatto_A, m * m) << "};\n";
   o << "__constant__ double CS_B[" << m << "] = {" << fmt_array(d->lobatto_b, m) << "};\n";
@@ -392,15 +395,16 @@ extern "C" int cs_module_load(const cs_module_desc* d, cs_module** out) {
   // layout 0: the blocked-LU condensation whenever a whole CTA would serve
   // one interval (measured faster from s1 = 102 on) or the system does not
   // fit; the CTA tree kernels only when the merge or top blocks do not fit
-  if (d->precision < 0 || d->precision > 2) {
+  if (d->precision < 0 || d->precision > 4) {
     delete M;
-    return set_err(CS_ERR_INVALID, "cs_module_load: precision must be 0 (FP64), 1 (TF32) or 2 (BF16)");
+    return set_err(CS_ERR_INVALID, "cs_module_load: precision must be 0 (FP64), 1 (TF32), 2 (BF16), 3 or 4 (with the tree)");
   }
   if (d->precision != 0 && d->layout == 1) {
     delete M;
     return set_err(CS_ERR_INVALID, "cs_module_load: reduced precision needs the large-system condensation (layout 0 or 2)");
   }
-  M->prec = d->precision;
+  M->prec = (d->precision == 0) ? 0 : ((d->precision == 1 || d->precision == 3) ? 1 : 2);
+  M->prec_tree = (d->precision == 3) ? 1 : ((d->precision == 4) ? 2 : 0);
   M->big_cond = d->layout == 2 || d->precision != 0 || (d->layout == 0 && (!fits_cond || gl > 32));
   M->big_tree = d->layout == 2 || (d->layout == 0 && !fits_tree);
   M->big = M->big_cond || M->big_tree;
@@ -435,7 +439,18 @@ extern "C" int cs_module_load(const cs_module_desc* d, cs_module** out) {
       M->condense_block = (s1 <= 128) ? 128 : 256;
       M->condense_per_cta = 1;
     }
-    if (M->big_tree) {
+    if (M->big_tree && d->precision >= 3) {
+      // reduced-precision merges: FP32 merge matrix and shared floats
+      // (CS_SHF .. CS_SM_TREE_LP in cs_kernels.cuh)
+      const long long shf = hb * qld + 2 * hb * hb + hb + (long long)qc * hb, sm_hb_lp = (shf + 1) / 2 + 32;
+      const long long qsz_lp = (qsz + 1) / 2;
+      const bool q_smem_lp = (qsz_lp + sm_hb_lp) * 8 <= smem_optin;
+      M->slab = std::max(M->slab, std::max(q_smem_lp ? 0ll : qsz_lp, (t_smem ? 0ll : tsz) + drsz));
+      M->tree_smem = (size_t)((q_smem_lp ? qsz_lp : 0) + sm_hb_lp) * 8;
+      M->top_smem = (size_t)((t_smem ? tsz : 0) + 32) * 8;
+      M->top_wpc = 8;
+      M->babd_cta_smem = 0;
+    } else if (M->big_tree) {
       M->tree_smem = (size_t)((q_smem ? qsz : 0) + sm_hb) * 8;
       M->top_smem = (size_t)((t_smem ? tsz : 0) + 32) * 8;
       M->top_wpc = 8;
@@ -472,7 +487,7 @@ extern "C" int cs_module_load(const cs_module_desc* d, cs_module** out) {
     M->top_smem = top_per * M->top_wpc;
   }
 
-  std::string src = build_source(d, M->big_cond, M->big_tree, M->prec, smem_optin);
+  std::string src = build_source(d, M->big_cond, M->big_tree, M->prec, M->big_tree ? M->prec_tree : 0, smem_optin);
   std::string cache = d->cache_dir ? d->cache_dir : "";
   if (cache.empty()) {
     const char* env = getenv("CS_GB300_CACHE");

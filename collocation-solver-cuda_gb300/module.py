@@ -59,9 +59,10 @@ class CompiledProblem:
     system or a BABD block does not fit in shared memory).
     precision: "fp64" (default), "tf32" or "bf16": the large-system
     condensation on the tensor cores (an inexact Newton Jacobian; residual,
-    line search, mesh error and BABD solve stay FP64)."""
+    line search, mesh error and BABD solve stay FP64); "tf32-tree" /
+    "bf16-tree" also run the tree merges' block updates on them."""
 
-    PRECISIONS = {"fp64": 0, "tf32": 1, "bf16": 2}
+    PRECISIONS = {"fp64": 0, "tf32": 1, "bf16": 2, "tf32-tree": 3, "bf16-tree": 4}
 
     def __init__(self, problem, m, cache_dir=DEFAULT_CACHE, layout=0, precision="fp64"):
         lib = _lib.load()

@@ -72,8 +72,10 @@ typedef struct cs_module_desc {
                                2 BF16 tensor cores with FP32 storage and
                                accumulation (an inexact Newton Jacobian: the
                                residual, line search, mesh error and BABD
-                               solve stay FP64).  1 and 2 imply the
-                               large-system condensation. */
+                               solve stay FP64); 3 / 4: TF32 / BF16 also for
+                               the tree merges' block updates (slower to
+                               converge: see the design notes).  Nonzero
+                               implies the large-system condensation. */
 } cs_module_desc;
 
 /* Compile (or load from the cache) and load the module on the current device. */

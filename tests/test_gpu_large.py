@@ -216,3 +216,20 @@ def test_reduced_precision_solve_reaches_fp64_oracle_solution(cs, prec):
     assert s["last_norm"] < pr.tolerance and s["max_residual"] <= 1.0
     for k, rk in (("y", ref.y), ("z", ref.z), ("p", ref.p)):
         assert np.abs(s[k] - rk).max() < 1e-6, (k, np.abs(s[k] - rk).max())
+
+
+def test_tensor_core_tree_option_converges_on_small_chain(cs):
+    """The opt-in TF32 tree merges (precision "tf32-tree"): a more inexact
+    direction (measured ~1e-2 relative), so more Newton steps, but the FP64
+    residual still drives the solve to the tolerance: K = 16 from a coarse
+    9-node guess lands within 1e-5 of the FP64 oracle (measured 5e-7)."""
+    pr = _pendulum(cs, 16, 9)
+    cp = cs.CompiledProblem(pr, 5, precision="tf32-tree")
+    bt = cs.Batch(cp, 1)
+    bt.set_guess([(np.asarray(pr.T0, float), np.asarray(pr.Y0, float), np.asarray(pr.Z0, float))],
+                 np.asarray(pr.P0, float).reshape(1, -1))
+    bt.solve(cs.default_opts(pr))
+    s = bt.solution()[0]
+    ref = O.solve(OracleProblem(pr), 5, cs.tables.lobatto(5), cs.tables.segment_tables(5))
+    assert s["success"] and s["N"] == ref.N
+    assert np.abs(s["y"] - ref.y).max() < 1e-5
