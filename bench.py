@@ -348,6 +348,25 @@ def bytes_per_interval(m, ny=4, nz=1, npe=0):
     return 8 * (2 + 2 * ny + m * (ny + nz) + r * s + ny * (2 * ny + npe + 1))
 
 
+def _rank_device(env, local_rank, world):
+    """CUDA_VISIBLE_DEVICES for a rank under torchrun: its own GPU among the
+    visible ones (the library works on the current device, so each rank sees
+    exactly one)."""
+    if world <= 1:
+        return env.get("CUDA_VISIBLE_DEVICES")
+    vis = env.get("CUDA_VISIBLE_DEVICES")
+    devs = [d for d in vis.split(",") if d.strip()] if vis else [str(i) for i in range(world)]
+    return devs[local_rank % len(devs)]
+
+
+_GPU_ID = [None]
+
+
+def _gpu_index(local_rank):
+    """nvidia-smi index of this rank's GPU (physical, from CUDA_VISIBLE_DEVICES)."""
+    return _GPU_ID[0] if _GPU_ID[0] is not None else local_rank
+
+
 def _dist_setup(world, local_rank):
     if world <= 1:
         return None
@@ -493,7 +512,7 @@ def run_warm(args, cs, rank, world, local_rank, cpu, cfg):
         g["bt"].profile_reset(timing=False)
     _log("warm-up done; timed warm-started steps")
     _barrier(dist)
-    with ClockSampler(local_rank) as clk:
+    with ClockSampler(_gpu_index(local_rank)) as clk:
         t0 = time.perf_counter()
         for _ in range(args.steps):
             solved, n_fb, sols = runner.run(warm=True)
@@ -608,7 +627,7 @@ def run_plain(args, cs, rank, world, local_rank, cpu, cfg, instances):
     for g in W.groups:
         g["bt"].profile_reset(timing=False)
     _barrier(dist)
-    with ClockSampler(local_rank) as clk:
+    with ClockSampler(_gpu_index(local_rank)) as clk:
         t0 = time.perf_counter()
         for _ in range(args.steps):
             W.step_resident()
@@ -755,7 +774,7 @@ def run_pendulum(args, cs, rank, world, local_rank):
         bt.solve(opts)
     bt.profile_reset(timing=False)
     _barrier(dist)
-    with ClockSampler(local_rank) as clk:
+    with ClockSampler(_gpu_index(local_rank)) as clk:
         t0 = time.perf_counter()
         for _ in range(args.steps):
             bt.reset()
@@ -936,6 +955,14 @@ def main():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:  # before any CUDA call of this process
+        dev = _rank_device(os.environ, local_rank, world)
+        os.environ["CUDA_VISIBLE_DEVICES"] = dev
+        _GPU_ID[0] = int(dev) if dev.isdigit() else local_rank
+    else:
+        vis = os.environ.get("CUDA_VISIBLE_DEVICES", "")
+        first = vis.split(",")[0].strip() if vis else ""
+        _GPU_ID[0] = int(first) if first.isdigit() else 0
     cs = _pkg()
     cores = os.cpu_count() or 1
     if args.workload == "pendulum":
