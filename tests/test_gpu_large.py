@@ -233,3 +233,22 @@ def test_tensor_core_tree_option_converges_on_small_chain(cs):
     ref = O.solve(OracleProblem(pr), 5, cs.tables.lobatto(5), cs.tables.segment_tables(5))
     assert s["success"] and s["N"] == ref.N
     assert np.abs(s["y"] - ref.y).max() < 1e-5
+
+
+def test_pendulum8_hybrid_layout_matches_oracle(cs):
+    """K = 8 (s1 = 102): blocked-LU condensation with the warp-per-merge
+    tree, the automatic layout for this size; a whole solve from a coarse
+    guess against the oracle."""
+    th = np.random.default_rng(4).uniform(-0.5, 0.5, 8)
+    pr = cs.ocp.Problem(cs.workloads.pendulum_ocp(8, th, nodes=9), name="pend8")
+    cp = cs.CompiledProblem(pr, 4)
+    bt = cs.Batch(cp, 1)
+    bt.set_guess([(np.asarray(pr.T0, float), np.asarray(pr.Y0, float), np.asarray(pr.Z0, float))],
+                 np.asarray(pr.P0, float).reshape(1, -1))
+    bt.solve(cs.default_opts(pr))
+    s = bt.solution()[0]
+    ref = O.solve(OracleProblem(pr), 4, cs.tables.lobatto(4), cs.tables.segment_tables(4))
+    assert s["success"] == ref.success
+    assert (s["N"], s["newton_steps"], s["residual_evals"]) == (ref.N, ref.jacobian_count, ref.residual_count)
+    np.testing.assert_allclose(s["y"], ref.y, rtol=0, atol=1e-8)
+    np.testing.assert_allclose(s["z"], ref.z, rtol=0, atol=1e-8)

@@ -257,3 +257,74 @@ def test_autotuned_condensation_gives_identical_solves(cs):
     for s0, s1 in zip(before, after):
         assert (s0["newton_steps"], s0["residual_evals"], s0["N"]) == (s1["newton_steps"], s1["residual_evals"], s1["N"])
         np.testing.assert_array_equal(s0["y"], s1["y"])
+
+
+@pytest.mark.parametrize("m", [2, 10])
+def test_extreme_collocation_orders_match_oracle(cs, m):
+    """The smallest and largest m of the tables (the reference's CLI allows
+    3..10): stage residual, Newton direction and a whole solve against the
+    oracle (with the tables computed here; the reference's m = 10 table has
+    a known missing entry)."""
+    pr = load_problem("vdp")
+    cp = compiled(cs, "vdp", m)
+    ref = O.solve(oracle_problem("vdp"), m, cs.tables.lobatto(m), cs.tables.segment_tables(m))
+    sol = cs.solver.solve_single(pr, m)
+    assert sol["success"] == ref.success
+    assert (sol["N"], sol["newton_steps"], sol["residual_evals"]) == (ref.N, ref.jacobian_count, ref.residual_count)
+    np.testing.assert_allclose(sol["y"], ref.y, rtol=0, atol=1e-8)
+
+
+def _dense_direction(ny, npar, N, A, C, H, b, B_0, B_n, V_n, r_bc):
+    """The condensed Newton system solved densely (the mathematical answer)."""
+    n = N - 1
+    sz = N * ny + npar
+    M = np.zeros((sz, sz))
+    rhs = np.zeros(sz)
+    for i in range(n):
+        rows = slice(i * ny, (i + 1) * ny)
+        M[rows, i * ny:(i + 1) * ny] = A[rows]
+        M[rows, (i + 1) * ny:(i + 2) * ny] = C[rows]
+        M[rows, N * ny:] = H[rows]
+        rhs[rows] = b[i]
+    M[n * ny:, :ny], M[n * ny:, n * ny:N * ny], M[n * ny:, N * ny:] = B_0, B_n, V_n
+    rhs[n * ny:] = -r_bc
+    x = np.linalg.solve(M, rhs)
+    return x[:N * ny].reshape(N, ny), x[N * ny:]
+
+
+@pytest.mark.parametrize("N", [2, 5])
+def test_short_meshes_solve_the_newton_system_exactly(cs, N):
+    """Meshes with fewer than 9 nodes (one interval: no tree level at all).
+    The reference's partitioned BABD solve (8 partitions of (N-1)//8 nodes,
+    solve_babd_system.py:93-106) is wrong there -- its partition indices
+    collapse to 0 -- and so is the oracle that restates it; the tree solve
+    here is checked against a dense solve of the same condensed system."""
+    m = 4
+    cp = compiled(cs, "vdp", m)
+    P = oracle_problem("vdp")
+    rk = cs.tables.lobatto(m)
+    t = np.linspace(0.0, 2.0, N)
+    rng = np.random.default_rng(2)
+    y0 = 0.3 * rng.standard_normal((N, cp.ny))
+    z0 = 0.3 * rng.standard_normal((N, cp.nz))
+    p = 0.5 + 0.3 * rng.random(cp.np)
+    y, yd, zt = O.form_initial_input(P, m, N, y0, z0, p, rk)
+    bt = cs.Batch(cp, 1)
+    bt.set_state([(t, y, yd, zt)], p.reshape(1, -1))
+    out = bt.stage_newton_direction(0.1)
+    f_q, y_tilde, f_a, f_b, r_bc = O.compute_f_q(P, m, N, rk, t, y, yd, zt, p, 0.1)
+    J, V, D, W, B_0, B_n, V_n = O.construct_jacobian(P, m, N, rk, t, y, y_tilde, zt, p, 0.1)
+    A, C, H, b = O.reduce_jacobian(cp.ny, cp.nz, cp.np, m, N, W, D, J, V, f_a, f_b)
+    dy, dp = _dense_direction(cp.ny, cp.np, N, A, C, H, b, B_0, B_n, V_n, r_bc)
+    scale = max(1.0, np.abs(dy).max())
+    np.testing.assert_allclose(out["dy"][:N], dy, rtol=0, atol=1e-10 * scale)
+    np.testing.assert_allclose(out["dp"][0], dp, rtol=0, atol=1e-10 * scale)
+    # the reference's partitioned solve misses it on these meshes
+    dy_ref, _ = O.solve_babd(cp.ny, cp.np, N, A, C, H, b, B_0, B_n, V_n, r_bc)
+    assert np.abs(dy_ref - dy).max() > 1e-3 * scale
+
+
+def test_empty_batch_is_refused(cs):
+    cp = compiled(cs, "vdp", 4)
+    with pytest.raises(Exception):
+        cs.Batch(cp, 0)
