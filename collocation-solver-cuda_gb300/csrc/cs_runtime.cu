@@ -623,7 +623,6 @@ struct cs_batch {
   int graph_tune[2] = {-1, -1};
   CsBatchDev graph_view[2];
   CsConsts graph_consts[2];
-  int cta_now = -1;  // automatic path choice of the running solve (-1: none)
   // device copy of the last initial guess (cs_batch_reset)
   DBuf iN, ioff, it, iy, iz, ip;
   std::vector<int> ihN, ihoff;
@@ -830,17 +829,15 @@ static int tree_levels(const cs_batch* bt) {
 }
 
 // Newton direction: one launch per tree level across the instances (spreads
-// every level over all SMs; measured faster for batches, also for their
-// stragglers), or one CTA per instance for the whole direction (one launch
-// per super-step; for a few small instances, where launches dominate).
+// every level over all SMs), or, on request (opts.babd_path = 1), one CTA per
+// instance for tree, top and back substitution in one launch.  Measured on
+// the warm-started Van der Pol batch, the per-instance CTA is the slower one
+// even when few instances are left (611 us per launch in the tail against
+// ~100-350 us for the per-level launches it replaces: one SM walks every
+// level of an instance's tree), so the automatic choice is per level.
 static bool use_cta_path(const cs_batch* bt) {
   if (bt->M->babd_cta_smem == 0) return false;
-  if (bt->opts.babd_path == 1) return true;
-  if (bt->opts.babd_path == 2) return false;
-  if (bt->cta_now >= 0) return bt->cta_now != 0;
-  int mx = 0;
-  for (int n : bt->hN) mx = std::max(mx, n);
-  return bt->B <= 8 && mx <= 1024;
+  return bt->opts.babd_path == 1;
 }
 
 static int run_lists(cs_batch* bt, CsBatchDev& v, int mode, int nlvl) {
@@ -1224,12 +1221,6 @@ extern "C" int cs_solve(cs_batch* bt, const cs_opts* opts) {
   const long long max_super = 10000000;
   long long steps = 0;
   const int per_launch_steps = 1;
-  // automatic Newton-direction path: per-level kernels while many instances
-  // iterate, one CTA per instance once at most one SM's worth of them is left
-  // (the per-level path then costs ~2 nlvl dependent launches per super-step)
-  const bool auto_path = o.babd_path == 0 && bt->M->babd_cta_smem > 0;
-  const int cta_max = bt->M->sms;
-  if (auto_path) bt->cta_now = bt->B <= cta_max ? 1 : 0;
   for (int outer = 0; outer < 1000000 && rc == CS_OK; ++outer) {
     // ---- Newton phase: device state machine, work lists, graph replays
     const int nlvl = tree_levels(bt);
@@ -1257,7 +1248,6 @@ extern "C" int cs_solve(cs_batch* bt, const cs_opts* opts) {
         break;
       }
       if (bt->h_n[0] == 0) break;
-      if (auto_path) bt->cta_now = bt->h_n[0] <= cta_max ? 1 : 0;
       if (steps > max_super) {
         rc = set_err(CS_ERR_STATE, "Newton phase did not terminate");
         break;
@@ -1300,7 +1290,6 @@ extern "C" int cs_solve(cs_batch* bt, const cs_opts* opts) {
     }
     if (!any_newton) break;
   }
-  bt->cta_now = -1;
   if (rc == CS_OK) rc = check_config(bt);
   if (rc == CS_OK) CS_CUDA(cudaStreamSynchronize(bt->stream));
   return rc;

@@ -95,8 +95,8 @@ typedef struct cs_opts {
   double alpha_m;        /* final continuation parameter (0.1, or 1e-6 with inequalities) */
   double beta;           /* continuation factor */
   int check_every;       /* Newton super-steps between host checks for completion */
-  int babd_path;         /* Newton direction kernels: 0 automatic, 1 one CTA per instance,
-                            2 one launch per tree level across the instances */
+  int babd_path;         /* Newton direction kernels: 0 automatic (per level), 1 one CTA
+                            per instance, 2 one launch per tree level across the instances */
   int residual_type;     /* segment residual estimate (CS:29-32): 1 weighted sum
                             (default), 2 weighted squares, 0 weighted maximum */
   int scale_by_time;     /* multiply the running estimate by h (default 1) */
