@@ -1034,6 +1034,74 @@ __device__ __forceinline__ void cs_backsub_thread(const double* __restrict__ rec
 }
 #endif
 
+#if CS_TREE_THREAD && CS_QC <= 32
+// The same merge with a column per lane (CS_TL lanes per merge, column in
+// registers): the pivot lane forms the reflector, shuffles hand it to the
+// other lanes, each lane updates its own column.  Every column sees the fma
+// sequence of cs_merge_thread, so the results are the same bits; the chain of
+// FP64 instructions per lane is ~4x shorter, which is what a level with few
+// merges waits for (a warp-wide FP64 instruction occupies a sub-partition's
+// FP64 pipe for ~76 cycles on this GPU).
+#define CS_TL ((CS_QC <= 16) ? 16 : 32)
+__device__ __forceinline__ void cs_merge_lanes(const double* __restrict__ ra, const double* __restrict__ rb,
+                                               double* __restrict__ out_row, double* __restrict__ rec, bool active) {
+  const int c = threadIdx.x & (CS_TL - 1);
+  // the group's own lanes: two groups of a warp may take different branches
+  const unsigned gm = (CS_TL == 32) ? 0xffffffffu : (0xffffu << (threadIdx.x & 16));
+  double Q[2 * CS_NY];
+#pragma unroll
+  for (int r = 0; r < CS_NY; ++r) {
+    double top = 0.0, bot = 0.0;
+    if (c < CS_NY) { top = ra[(CS_NY + c) * CS_NY + r]; bot = rb[c * CS_NY + r]; }
+    else if (c < 2 * CS_NY) { top = ra[(c - CS_NY) * CS_NY + r]; }
+    else if (c < 3 * CS_NY) { bot = rb[(CS_NY + c - 2 * CS_NY) * CS_NY + r]; }
+    else if (c < 3 * CS_NY + CS_NPE) { top = ra[(2 * CS_NY + c - 3 * CS_NY) * CS_NY + r]; bot = rb[(2 * CS_NY + c - 3 * CS_NY) * CS_NY + r]; }
+    else if (c < CS_QC) { top = ra[(2 * CS_NY + CS_NPE) * CS_NY + r]; bot = rb[(2 * CS_NY + CS_NPE) * CS_NY + r]; }
+    Q[r] = top;
+    Q[CS_NY + r] = bot;
+  }
+#pragma unroll
+  for (int k = 0; k < CS_NY; ++k) {
+    // pivot lane k: the reflector of column k
+    double ss = 0.0;
+#pragma unroll
+    for (int r = k; r < 2 * CS_NY; ++r) ss = fma(Q[r], Q[r], ss);
+    const double x0 = Q[k];
+    const double gk = (x0 >= 0.0) ? -sqrt(ss) : sqrt(ss);
+    const double v0k = x0 - gk;
+    const double vsk = ss - x0 * x0 + v0k * v0k;
+    const double v0 = __shfl_sync(gm, v0k, k, CS_TL);
+    const double vs = __shfl_sync(gm, vsk, k, CS_TL);
+    double v[2 * CS_NY];
+#pragma unroll
+    for (int r = k + 1; r < 2 * CS_NY; ++r) v[r] = __shfl_sync(gm, Q[r], k, CS_TL);
+    if (vs >= CS_EPS) {
+      if (c > k) {
+        const double beta = -2.0 / vs;
+        double w = v0 * Q[k];
+#pragma unroll
+        for (int r = k + 1; r < 2 * CS_NY; ++r) w = fma(v[r], Q[r], w);
+        const double bw = beta * w;
+        Q[k] = fma(bw, v0, Q[k]);
+#pragma unroll
+        for (int r = k + 1; r < 2 * CS_NY; ++r) Q[r] = fma(bw, v[r], Q[r]);
+      } else if (c == k) {
+        Q[k] = gk;
+#pragma unroll
+        for (int r = k + 1; r < 2 * CS_NY; ++r) Q[r] = 0.0;
+      }
+    }
+  }
+  if (!active || c >= CS_QC) return;
+#pragma unroll
+  for (int r = 0; r < CS_NY; ++r) rec[c * CS_NY + r] = Q[r];
+  if (c >= CS_NY) {
+#pragma unroll
+    for (int r = 0; r < CS_NY; ++r) out_row[(c - CS_NY) * CS_NY + r] = Q[CS_NY + r];
+  }
+}
+#endif
+
 // y_m = R^-1 (d - G y_l - E y_r - J p), one warp, lanes over rows
 __device__ void cs_backsub_warp(const double* rec, const double* yl, const double* yr, const double* dpv, double* ym) {
   const int lane = threadIdx.x & 31;
@@ -1081,6 +1149,32 @@ extern "C" __global__ void k_tree_level(CsBatch bt, int l) {
     const long long total = pre[njac];
     const double* srcb = (l & 1) ? bt.rows1 : bt.rows0;
     double* dstb = (l & 1) ? bt.rows0 : bt.rows1;
+#if CS_QC <= 32
+    // few merges (all fit in one round of lane groups): CS_TL lanes per merge
+    if (total * CS_TL <= (long long)gridDim.x * blockDim.x) {
+      const long long it0 = ((long long)blockIdx.x * blockDim.x + threadIdx.x) / CS_TL;
+      if ((long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31) >= total * CS_TL) return;  // warp-uniform
+      const bool active = it0 < total;
+      const long long it = active ? it0 : total - 1;
+      const int k = cs_find(pre, njac, it);
+      const int b = bt.jac[k];
+      const int mi = (int)(it - pre[k]);
+      const int off = bt.off[b];
+      const int nl = cs_rows_at(bt.N[b] - 1, l);
+      const int merges = nl >> 1;
+      const double* src = srcb + (size_t)off * CS_ROWSZ;
+      double* dst = dstb + (size_t)off * CS_ROWSZ;
+      if (mi < merges) {  // uniform within the lane group
+        cs_merge_lanes(src + (size_t)(2 * mi) * CS_ROWSZ, src + (size_t)(2 * mi + 1) * CS_ROWSZ,
+                       dst + (size_t)mi * CS_ROWSZ, bt.tree + (size_t)(off + ((2 * mi + 1) << l)) * CS_TREESZ, active);
+      } else if (active) {
+        const double* sr = src + (size_t)(nl - 1) * CS_ROWSZ;
+        double* dr = dst + (size_t)merges * CS_ROWSZ;
+        for (int q = threadIdx.x & (CS_TL - 1); q < CS_ROWSZ; q += CS_TL) dr[q] = sr[q];
+      }
+      return;
+    }
+#endif
     for (long long it = (long long)blockIdx.x * blockDim.x + threadIdx.x; it < total; it += (long long)gridDim.x * blockDim.x) {
       const int k = cs_find(pre, njac, it);
       const int b = bt.jac[k];
