@@ -35,7 +35,7 @@
 //                                                      solve_babd_system.py:161-572, collocation_solver_parallel_2d_shared.py:1619-1650
 //   k_lists          (none: compacts the work of the batch every super-step)
 //   k_decide/k_accept  Newton loop and line search    collocation_solver_parallel_2d_shared.py:105-180
-//   k_segres         compute_segment_residual_kernel   collocation_solver_parallel_2d_shared.py:1833-1892
+//   k_segres         compute_segment_residual_kernel(2) collocation_solver_parallel_2d_shared.py:1833-2013
 //   k_remesh_*       recover_solution_kernel + remesh  collocation_solver_parallel_2d_shared.py:2049-2311
 
 #define CS_S (CS_M * (CS_NY + CS_NZ))          // stage unknowns per interval
@@ -1499,18 +1499,20 @@ extern "C" __global__ void k_babd_cta(CsBatch bt, int recover) {}
 
 #if CS_BIG
 // ========================================================================
-// Large stage systems (pendulum chains of K >= 16: s = m (ny + nz) in the
-// hundreds, blocks of ny = 64 .. 128).  The matrices no longer fit in shared
-// memory, so each CTA owns a slab of global memory (bt.wsp; L2 resident) and
-// the kernels below replace k_condense, k_tree_level and k_top:
+// Large stage systems (pendulum chains: K = 8 takes the condensation only,
+// K = 16 and 32 both; s = m (ny + nz) in the hundreds, blocks of ny = 32 ..
+// 128).  The matrices no longer fit in shared memory, so each CTA owns a slab
+// of global memory (bt.wsp; L2 resident) and the kernels below replace
+// k_condense (CS_BIG_COND), k_tree_level and k_top (CS_BIG_TREE):
 //   k_condense    one CTA per interval, right-looking blocked LU of the
 //                 augmented system [W11 | R1] with panels of CS_NB columns in
 //                 shared memory.  Same operations in the same order as the
 //                 unblocked elimination of cs_condense_group (pivot rule,
 //                 multipliers, the fma chain of every entry), so both give
-//                 the same bits.
-//   k_tree_level  one CTA per merge, a warp per column of the Householder
-//                 updates (lanes over rows).
+//                 the same bits.  CS_PREC 1 / 2: FP32 storage, trailing
+//                 updates on the tensor cores (TF32 / BF16).
+//   k_tree_level  one CTA per merge, compact-WY Householder in panels of
+//                 CS_HB reflectors (CS_PREC_TREE: on the tensor cores).
 //   k_top         one CTA per instance.
 #define CS_NB 16
 #define CS_LDG (((CS_NCOL1 + 3) / 4) * 4)   // row stride of the slab matrix
