@@ -328,3 +328,38 @@ def test_empty_batch_is_refused(cs):
     cp = compiled(cs, "vdp", 4)
     with pytest.raises(Exception):
         cs.Batch(cp, 0)
+
+
+def test_nan_instance_fails_alone(cs):
+    """An instance whose guess holds a NaN fails (its residual norm is NaN, so
+    no line-search trial is accepted) without touching its batch-mates, which
+    solve exactly as they do alone."""
+    pr = cs.workloads.vdp_family_problem()
+    insts = [i for i in cs.workloads.vdp_batch(64, seed=31) if i.m == 4][:4]
+    cp = compiled(cs, "vdp_family", 4)
+    opts = cs.default_opts(pr, max_nodes=20000)
+    guesses = [inst.guess() for inst in insts]
+    alone = []
+    for inst, (t, y, z, p) in zip(insts, guesses):
+        b1 = cs.Batch(cp, 1)
+        b1.set_guess([(t, y, z)], p.reshape(1, -1), inst.theta.reshape(1, -1))
+        b1.solve(opts)
+        alone.append(b1.solution()[0])
+    meshes = [(t, y.copy(), z) for t, y, z, _ in guesses]
+    meshes[2][1][3, 1] = np.nan
+    bt = cs.Batch(cp, len(insts))
+    bt.set_guess(meshes, np.stack([g[3] for g in guesses]), np.stack([i.theta for i in insts]))
+    bt.solve(opts)
+    sols = bt.solution()
+    assert not sols[2]["success"]
+    from conftest import OracleProblem
+    P = OracleProblem(pr)
+    P.maximum_nodes = 20000
+    P.theta = insts[2].theta
+    t, y, z, p = meshes[2] + (guesses[2][3],)
+    ref = O.solve(P, 4, cs.tables.lobatto(4), cs.tables.segment_tables(4), T0=t, Y0=y, Z0=z, P0=p)
+    assert (sols[2]["newton_steps"], sols[2]["residual_evals"]) == (ref.jacobian_count, ref.residual_count)
+    for k in (0, 1, 3):
+        assert sols[k]["success"] == alone[k]["success"]
+        assert (sols[k]["newton_steps"], sols[k]["N"]) == (alone[k]["newton_steps"], alone[k]["N"])
+        np.testing.assert_array_equal(sols[k]["y"], alone[k]["y"])
