@@ -507,7 +507,7 @@ def run_warm(args, cs, rank, world, local_rank, cpu, cfg):
     ws_gb = sum(g["bt"].sizes()[1] for g in runner.groups) * 8 * 300 / 1e9
     cfg["l2"] = cfg["l2"] % ("%.1f" % ws_gb)
     for _ in range(args.warmup):
-        runner.run(warm=True)
+        runner.run(warm=True, speculate=args.speculate)
     for g in runner.groups:
         g["bt"].profile_reset(timing=False)
     _log("warm-up done; timed warm-started steps")
@@ -515,7 +515,7 @@ def run_warm(args, cs, rank, world, local_rank, cpu, cfg):
     with ClockSampler(_gpu_index(local_rank)) as clk:
         t0 = time.perf_counter()
         for _ in range(args.steps):
-            solved, n_fb, sols = runner.run(warm=True)
+            solved, n_fb, sols = runner.run(warm=True, speculate=args.speculate)
         dt = time.perf_counter() - t0
     dt = _max_over_ranks(dist, dt)
     runner_times = dict(runner.times)
@@ -894,6 +894,9 @@ def main():
     ap.add_argument("--train", type=int, default=65536, help="training solutions (warm)")
     ap.add_argument("--epochs", type=int, default=150)
     ap.add_argument("--single-sample", type=int, default=64)
+    ap.add_argument("--speculate", type=float, default=0.0,
+                    help="warm: start the plain-guess solves of the instances still iterating once at most this "
+                         "fraction of an m-group is (0: fallbacks only after the warm solve)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--babd-path", type=int, default=0, help="0 automatic, 1 one CTA per instance, 2 per level")
     ap.add_argument("--layout", type=int, default=0,
@@ -934,9 +937,9 @@ def main():
         runner = ws.WarmRunner(fam, solver, net, _family_batch(cs, args.family, 2048, 7))
         # the m-groups one after another on this thread (profilers serialise
         # kernels anyway, and a single host thread keeps the capture simple)
-        runner.run(warm=True, threads=False)
+        runner.run(warm=True, threads=False, speculate=0)
         cs._lib.check(lib.cs_profiler_start(), "cs_profiler_start")
-        solved, n_fb, _ = runner.run(warm=True, threads=False)
+        solved, n_fb, _ = runner.run(warm=True, threads=False, speculate=0)
         cs._lib.check(lib.cs_profiler_stop(), "cs_profiler_stop")
         print("profile case ok: solved %d of 2048, %d fallbacks" % (solved, n_fb))
         return
@@ -992,6 +995,13 @@ def main():
                "batch_per_gpu": args.batch, "tol": 1e-6, "precision": "fp64 solver, bf16/fp32 network",
                "warm_start": "MLP 4x256 GELU, 64 normalised-time nodes, fallback to the plain guess",
                "l2": "working set %s GB per step, larger than L2 (129 MB)"}
+    else:
+        cfg = None
+    if cfg is not None:
+        cfg["fallback"] = ("every instance that fails from its warm guess is solved again from the plain guess; "
+                           "those still iterating once at most %g of an m-group is are started early on a second "
+                           "thread (same results, shorter wall time)" % args.speculate
+                           if args.speculate > 0 else "after the warm solve of each m-group")
     else:
         instances = cs.workloads.vdp_batch(args.batch, seed=SEED + rank)
         cfg = {"workload": "plain batched solve: Van der Pol batch, %d instances (x0~U[-2,2]^2, T~U[2,8], "

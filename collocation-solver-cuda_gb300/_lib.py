@@ -54,6 +54,10 @@ class TuneResult(ctypes.Structure):
                 ("ms", ctypes.c_double), ("default_ms", ctypes.c_double)]
 
 
+# cs_progress_fn: void (*)(void* user, int active, long long super_steps)
+PROGRESS_FN = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ctypes.c_int, ctypes.c_longlong)
+
+
 # every symbol declared in include/cs_gb300.h: name -> (restype, argtypes)
 SIGNATURES = {
     "cs_module_load": (ctypes.c_int, [ctypes.POINTER(ModuleDesc), ctypes.POINTER(ctypes.c_void_p)]),
@@ -65,6 +69,7 @@ SIGNATURES = {
     "cs_batch_set_guess": (ctypes.c_int, [ctypes.c_void_p, _ip, _dp, _dp, _dp, _dp, _dp]),
     "cs_batch_set_state": (ctypes.c_int, [ctypes.c_void_p, _ip, _dp, _dp, _dp, _dp, _dp, _dp]),
     "cs_solve": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Opts)]),
+    "cs_batch_set_progress": (ctypes.c_int, [ctypes.c_void_p, PROGRESS_FN, ctypes.c_void_p]),
     "cs_batch_sizes": (ctypes.c_int, [ctypes.c_void_p, _ip, ctypes.POINTER(ctypes.c_longlong)]),
     "cs_get_solution": (ctypes.c_int, [ctypes.c_void_p, _dp, _dp, _dp, _dp, ctypes.POINTER(Stats)]),
     "cs_stage_residual": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double, _dp, _dp, _dp]),

@@ -61,7 +61,6 @@
 #define FAIL_ITER 1
 #define FAIL_NODES 2
 #define FAIL_MESH 3
-#define FAIL_NAN 4
 
 // Line-search trials evaluated in one super-step once the first trial of a
 // direction was rejected (alpha, alpha/2, ...; the decision walks them in

@@ -616,6 +616,8 @@ struct cs_batch {
   // work lists
   DBuf l_act, l_jac, l_acc, l_actp, l_jacp, l_accp, l_lvlp, l_n;
   int* h_n = nullptr;  // pinned copy of nlist
+  cs_progress_fn progress = nullptr;
+  void* progress_user = nullptr;
   // captured super-step, one graph per Newton-direction path (0 per level,
   // 1 one CTA per instance)
   cudaGraphExec_t graph[2] = {nullptr, nullptr};
@@ -1247,6 +1249,7 @@ extern "C" int cs_solve(cs_batch* bt, const cs_opts* opts) {
         rc = set_err(CS_ERR_CUDA, std::string("Newton phase: ") + cudaGetErrorString(cudaGetLastError()));
         break;
       }
+      if (bt->progress) bt->progress(bt->progress_user, bt->h_n[0], steps);
       if (bt->h_n[0] == 0) break;
       if (steps > max_super) {
         rc = set_err(CS_ERR_STATE, "Newton phase did not terminate");
@@ -1293,6 +1296,13 @@ extern "C" int cs_solve(cs_batch* bt, const cs_opts* opts) {
   if (rc == CS_OK) rc = check_config(bt);
   if (rc == CS_OK) CS_CUDA(cudaStreamSynchronize(bt->stream));
   return rc;
+}
+
+extern "C" int cs_batch_set_progress(cs_batch* bt, cs_progress_fn fn, void* user) {
+  if (!bt) return set_err(CS_ERR_INVALID, "cs_batch_set_progress: null batch");
+  bt->progress = fn;
+  bt->progress_user = user;
+  return CS_OK;
 }
 
 extern "C" int cs_batch_sizes(cs_batch* bt, int* N_out, long long* total_out) {

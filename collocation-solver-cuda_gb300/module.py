@@ -206,6 +206,28 @@ class Batch:
         o = opts if opts is not None else default_opts(self.cp.problem)
         _lib.check(self._lib.cs_solve(self.handle, ctypes.byref(o)), "cs_solve")
 
+    def set_progress(self, fn):
+        """fn(active, super_steps) is called on the solving thread after each
+        check of the Newton phase (instances still iterating, super-steps so
+        far); the batch may be read from it (statuses()), not solved.  None
+        removes it."""
+        if fn is None:
+            self._progress = None
+            cb = ctypes.cast(None, _lib.PROGRESS_FN)
+        else:
+            def tramp(_user, active, steps):
+                fn(int(active), int(steps))
+            cb = _lib.PROGRESS_FN(tramp)
+            self._progress = cb  # keeps the ctypes thunk alive
+        _lib.check(self._lib.cs_batch_set_progress(self.handle, cb, None), "cs_batch_set_progress")
+
+    def statuses(self):
+        """Per-instance status codes (0 fresh, 1 line search, 2 segment
+        residual, 3 done, 4 failed, 5 remesh) without copying the solution."""
+        st = (_lib.Stats * self.B)()
+        _lib.check(self._lib.cs_get_solution(self.handle, None, None, None, None, st), "cs_get_solution")
+        return np.array([s.status for s in st], dtype=np.int32)
+
     # ---- data out
     def sizes(self):
         N = np.zeros(self.B, dtype=np.int32)

@@ -301,9 +301,20 @@ class WarmRunner:
             self.groups.append(dict(m=m, first=start, n=len(idx), bt=bt))
             start += len(idx)
 
-    def run(self, warm=True, fallback=True, threads=True):
+    def run(self, warm=True, fallback=True, threads=True, speculate=0.0):
         """One solve of every instance; returns (solved, fallback count, stats).
-        self.times holds the seconds of the phases of the last run."""
+        self.times holds the seconds of the phases of the last run.
+
+        speculate: once no more than this fraction of a group is still in the
+        Newton iteration, the instances still iterating are solved from the
+        plain guess on a second thread while the warm solve goes on; an
+        instance that then fails from its warm guess takes that solution,
+        one that succeeds drops it.  Each instance's result is independent
+        of its batch-mates, so the outcome is the one of solving the failed
+        instances again afterwards; only the wall time changes.  0 (the
+        default) falls back after the warm solve: on the Van der Pol batch
+        the overlapped chains of small launches contend for the GPU and the
+        step is slower (0.66 s against 0.55 s at 0.03)."""
         import threading
         import time
         t0 = time.perf_counter()
@@ -311,24 +322,60 @@ class WarmRunner:
             self.mlp.predict_device(self.dX, len(self.instances), self.dY)
         t1 = time.perf_counter()
 
+        def plain_solve(g, ks):
+            return self.solver.solve([self.instances[g["first"] + k] for k in ks])
+
         def one(g):
             bt = g["bt"]
             bt.reset()
             if warm:
                 bt.warm_start(self.dY.ptr + 4 * g["first"] * self.mlp.n_out, N_NODES, self.mlp.n_out)
-            bt.solve(self.solver.opts)
+            spec = {}
+            if warm and fallback and speculate > 0:
+                limit = max(1, int(speculate * g["n"]))
+
+                def side(ks):
+                    try:
+                        spec["sols"] = plain_solve(g, ks)
+                    except BaseException as e:  # re-raised on the group's thread
+                        spec["error"] = e
+
+                def hook(active, steps):
+                    if "ks" in spec or active > limit:
+                        return
+                    st = bt.statuses()
+                    spec["ks"] = [int(k) for k in np.flatnonzero((st == 0) | (st == 1))]
+                    spec["t"] = time.perf_counter() - t1
+                    if spec["ks"]:
+                        spec["thread"] = threading.Thread(target=side, args=(spec["ks"],))
+                        spec["thread"].start()
+                bt.set_progress(hook)
+            try:
+                bt.solve(self.solver.opts)
+            except BaseException:
+                if "thread" in spec:
+                    spec["thread"].join()
+                raise
+            finally:
+                bt.set_progress(None)
             g["t_solve"] = time.perf_counter() - t1
             g["sols"] = bt.solution()
+            if "thread" in spec:
+                spec["thread"].join()
             g["fallback"] = []
+            g["speculated"] = len(spec.get("ks", []))
+            g["t_spec"] = spec.get("t")
+            if "error" in spec:
+                raise spec["error"]
             if warm and fallback:
-                # this group's failed instances again from the plain guess,
-                # overlapping with the other groups' solves
                 failed = [k for k, s in enumerate(g["sols"]) if not s["success"]]
-                if failed:
-                    plain = self.solver.solve([self.instances[g["first"] + k] for k in failed])
-                    for k, s in zip(failed, plain):
-                        g["sols"][k] = dict(s, fallback=True)
-                    g["fallback"] = failed
+                have = dict(zip(spec.get("ks", []), spec.get("sols", [])))
+                rest = [k for k in failed if k not in have]
+                if rest:
+                    have.update(zip(rest, plain_solve(g, rest)))
+                for k in failed:
+                    g["sols"][k] = dict(have[k], fallback=True)
+                g["fallback"] = failed
             g["t_done"] = time.perf_counter() - t1
 
         if threads:
@@ -347,6 +394,8 @@ class WarmRunner:
             sols += g["sols"]
             n_fb += len(g["fallback"])
         self.times = {"predict_s": t1 - t0, "solve_and_fallback_s": t2 - t1,
-                      "groups": [(g["m"], round(g["t_solve"], 4), round(g["t_done"], 4)) for g in self.groups]}
+                      "groups": [(g["m"], round(g["t_solve"], 4), round(g["t_done"], 4)) for g in self.groups],
+                      "speculated": [(g["m"], g["speculated"], None if g["t_spec"] is None else round(g["t_spec"], 4))
+                                     for g in self.groups]}
         solved = sum(int(s["success"]) for s in sols)
         return solved, n_fb, sols

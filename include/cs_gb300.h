@@ -121,7 +121,8 @@ typedef struct cs_stats {
   int remeshes;
   int continuation_steps;
   int singular;          /* singular pivots met */
-  int fail_reason;
+  int fail_reason;       /* 0 none, 1 Newton/continuation iteration limit,
+                            2 node count outside [min, max], 3 mesh limit */
   double alpha;          /* final continuation parameter */
   double max_residual;   /* last maximum segment residual */
   double last_norm;      /* last residual infinity norm */
@@ -153,6 +154,16 @@ int cs_batch_set_state(cs_batch* bt, const int* N, const double* t, const double
  * segment residual, remesh.
  * Replaces: collocation_solver_parallel (CS:36-251). */
 int cs_solve(cs_batch* bt, const cs_opts* opts);
+
+/* Progress hook of cs_solve: called on the solving thread after every check
+ * of the Newton phase (every opts.check_every super-steps), with the number of
+ * instances still in the Newton iteration and the super-steps run so far in
+ * this solve.  The batch's stream is idle during the call, so the hook may
+ * read the batch (cs_get_solution with null arrays returns the statuses); it
+ * must not launch work on it.  fn = NULL removes the hook.  No counterpart in
+ * the reference, which prints its progress (CS:60-251). */
+typedef void (*cs_progress_fn)(void* user, int active, long long super_steps);
+int cs_batch_set_progress(cs_batch* bt, cs_progress_fn fn, void* user);
 
 /* Current node counts (batch ints) and total node slots. */
 int cs_batch_sizes(cs_batch* bt, int* N_out, long long* total_out);

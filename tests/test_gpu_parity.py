@@ -331,9 +331,8 @@ def test_empty_batch_is_refused(cs):
 
 
 def test_nan_instance_fails_alone(cs):
-    """An instance whose guess holds a NaN fails (its residual norm is NaN, so
-    no line-search trial is accepted) without touching its batch-mates, which
-    solve exactly as they do alone."""
+    """An instance whose guess holds a NaN fails at the iteration limit
+    without touching its batch-mates, which solve exactly as they do alone."""
     pr = cs.workloads.vdp_family_problem()
     insts = [i for i in cs.workloads.vdp_batch(64, seed=31) if i.m == 4][:4]
     cp = compiled(cs, "vdp_family", 4)
@@ -351,14 +350,12 @@ def test_nan_instance_fails_alone(cs):
     bt.set_guess(meshes, np.stack([g[3] for g in guesses]), np.stack([i.theta for i in insts]))
     bt.solve(opts)
     sols = bt.solution()
+    # the NaN never leaves the instance: every trial norm is NaN, no step is
+    # accepted, and it stops at the Newton iteration limit (numpy's dense solve
+    # in the oracle raises or returns on a NaN matrix depending on the LAPACK
+    # build, so the oracle is not asked here)
     assert not sols[2]["success"]
-    from conftest import OracleProblem
-    P = OracleProblem(pr)
-    P.maximum_nodes = 20000
-    P.theta = insts[2].theta
-    t, y, z, p = meshes[2] + (guesses[2][3],)
-    ref = O.solve(P, 4, cs.tables.lobatto(4), cs.tables.segment_tables(4), T0=t, Y0=y, Z0=z, P0=p)
-    assert (sols[2]["newton_steps"], sols[2]["residual_evals"]) == (ref.jacobian_count, ref.residual_count)
+    assert sols[2]["fail_reason"] == 1 and sols[2]["newton_steps"] == opts.max_iter
     for k in (0, 1, 3):
         assert sols[k]["success"] == alone[k]["success"]
         assert (sols[k]["newton_steps"], sols[k]["N"]) == (alone[k]["newton_steps"], alone[k]["N"])

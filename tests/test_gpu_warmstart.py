@@ -141,3 +141,33 @@ def test_guess_and_solution_files_round_trip(tmp_path):
         assert err == 0
         np.testing.assert_array_equal(t2, s["t"])
         np.testing.assert_array_equal(y2, s["y"])
+
+
+def test_speculative_fallback_gives_the_sequential_results():
+    """Starting the plain-guess solves early (for every instance still
+    iterating, at the first check or once 3 % of a group is) changes no
+    instance's result against falling back after the warm solve."""
+    cs = pkg()
+    ws = cs.warmstart
+    fam = ws.vdp_family()
+    insts = cs.workloads.vdp_batch(96, seed=23, n_range=(32, 128))
+    # an untrained network with a wide output scale: poor guesses, so that a
+    # good part of the batch fails warm and falls back
+    net = ws.Mlp(4, fam.n_out, width=64, depth=3, seed=2)
+    X = np.array([fam.features(i) for i in insts], np.float32)
+    rng = np.random.default_rng(0)
+    net.fit_normalization(X, (1.5 * rng.standard_normal((len(insts), fam.n_out))).astype(np.float32))
+    solver = ws.BatchSolver(fam)
+    runner = ws.WarmRunner(fam, solver, net, insts)
+    base = runner.run(warm=True, speculate=0)
+    assert base[1] > 0
+    for frac in (1.0, 0.03):
+        got = runner.run(warm=True, speculate=frac)
+        assert got[:2] == base[:2]
+        if frac == 1.0:
+            assert sum(n for _, n, _ in runner.times["speculated"]) >= base[1]
+        for a, b in zip(got[2], base[2]):
+            assert (a["success"], a.get("fallback", False), a["newton_steps"], a["residual_evals"], a["N"]) == \
+                   (b["success"], b.get("fallback", False), b["newton_steps"], b["residual_evals"], b["N"])
+            np.testing.assert_array_equal(a["y"], b["y"])
+            np.testing.assert_array_equal(a["t"], b["t"])
