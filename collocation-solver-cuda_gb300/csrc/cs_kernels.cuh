@@ -1372,6 +1372,62 @@ extern "C" __global__ void k_backsub_level(CsBatch bt, int l) {
   }
 }
 
+#if !CS_BIG_TREE && CS_TREE_THREAD && CS_QC <= 32
+// The upper tree levels l >= l_lo of every instance on the jac list, its top
+// system and the back substitution of those levels, one CTA per instance:
+// levels with at most a few merges each, which as launches of their own cost
+// a launch and a work-list lookup apiece for a few dependent merges.  Merges
+// by groups of CS_TL lanes (cs_merge_lanes), back substitution by thread
+// (cs_backsub_thread): the per-level kernels' arithmetic, so the same bits.
+// Levels below l_lo go through k_tree_level / k_backsub_level before and
+// after this launch.
+extern "C" __global__ void __launch_bounds__(128) k_upper(CsBatch bt, int l_lo) {
+  extern __shared__ double smem[];
+  const int groups = blockDim.x / CS_TL, grp = threadIdx.x / CS_TL, c = threadIdx.x & (CS_TL - 1);
+  const int njac = bt.nlist[1];
+  for (int k = blockIdx.x; k < njac; k += gridDim.x) {
+    const int b = bt.jac[k];
+    const int off = bt.off[b];
+    const int n0 = bt.N[b] - 1;
+    const int L = cs_levels(n0);
+    for (int l = l_lo; l < L; ++l) {
+      const int nl = cs_rows_at(n0, l);
+      const int merges = nl >> 1, items = (nl + 1) >> 1;
+      const double* src = ((l & 1) ? bt.rows1 : bt.rows0) + (size_t)off * CS_ROWSZ;
+      double* dst = ((l & 1) ? bt.rows0 : bt.rows1) + (size_t)off * CS_ROWSZ;
+      for (int mi = grp; mi < items; mi += groups) {  // uniform within a lane group
+        if (mi < merges) {
+          cs_merge_lanes(src + (size_t)(2 * mi) * CS_ROWSZ, src + (size_t)(2 * mi + 1) * CS_ROWSZ,
+                         dst + (size_t)mi * CS_ROWSZ, bt.tree + (size_t)(off + ((2 * mi + 1) << l)) * CS_TREESZ, true);
+        } else {
+          const double* sr = src + (size_t)(nl - 1) * CS_ROWSZ;
+          double* dr = dst + (size_t)merges * CS_ROWSZ;
+          for (int q = c; q < CS_ROWSZ; q += CS_TL) dr[q] = sr[q];
+        }
+      }
+      __syncthreads();
+    }
+    if (threadIdx.x < 32) cs_top_warp(bt, b, smem);
+    __syncthreads();
+    const double* dpv = bt.dp + (size_t)b * CS_NP;
+    for (int l = L - 1; l >= l_lo; --l) {
+      const int merges = cs_rows_at(n0, l) >> 1;
+      for (int mi = threadIdx.x; mi < merges; mi += blockDim.x) {
+        const int mid = (2 * mi + 1) << l, left = (2 * mi) << l;
+        int right = (2 * mi + 2) << l;
+        if (right > n0) right = n0;
+        cs_backsub_thread(bt.tree + (size_t)(off + mid) * CS_TREESZ, bt.dy + (size_t)(off + left) * CS_NY,
+                          bt.dy + (size_t)(off + right) * CS_NY, dpv, bt.dy + (size_t)(off + mid) * CS_NY);
+      }
+      __syncthreads();
+    }
+  }
+}
+#else
+// needs lane merges on small block rows; the host never launches it otherwise
+extern "C" __global__ void k_upper(CsBatch bt, int l_lo) {}
+#endif
+
 // Stage steps: dk = -(X_f + X_J dy_i + X_V dp), warp per interval, lanes
 // over stage rows (the reference re-factorises W instead,
 // collocation_solver_parallel_2d_shared.py:1619-1650).

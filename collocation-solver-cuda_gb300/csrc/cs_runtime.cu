@@ -262,8 +262,12 @@ struct cs_module {
   CUmodule mod = nullptr;
   CUfunction f_form_initial, f_residual, f_decide, f_accept, f_condense, f_segres, f_mesh_decide,
       f_remesh_count, f_remesh_write, f_repack, f_znodes, f_lists, f_tree_level, f_top, f_backsub_level, f_recover,
-      f_babd_cta;
+      f_babd_cta, f_upper;
   size_t babd_cta_smem;
+  // k_upper (upper tree levels, top and their back substitution, CTA per
+  // instance): 0 when the block rows are too large for lane merges
+  size_t upper_smem = 0;
+  int upper_grid = 0;
   int condense_block, condense_per_cta;
   size_t condense_smem;
   size_t tree_smem;   // per CTA of 4 warps
@@ -485,6 +489,8 @@ extern "C" int cs_module_load(const cs_module_desc* d, cs_module** out) {
     M->top_wpc = (int)std::max<size_t>(1, std::min<size_t>(4, (size_t)smem_optin / top_per));
     M->babd_cta_smem = top_per + (size_t)8 * qld * qc * sizeof(double);
     M->top_smem = top_per * M->top_wpc;
+    // CS_TREE_THREAD && CS_QC <= 32 in cs_kernels.cuh (lane merges)
+    if (2 * M->ny * qc <= 128 && qc <= 32 && top_per <= (size_t)smem_optin) M->upper_smem = top_per;
   }
 
   std::string src = build_source(d, M->big_cond, M->big_tree, M->prec, M->big_tree ? M->prec_tree : 0, smem_optin);
@@ -514,7 +520,8 @@ extern "C" int cs_module_load(const cs_module_desc* d, cs_module** out) {
              {&M->f_repack, "k_repack"},             {&M->f_znodes, "k_znodes"},
              {&M->f_lists, "k_lists"},               {&M->f_tree_level, "k_tree_level"},
              {&M->f_top, "k_top"},                   {&M->f_backsub_level, "k_backsub_level"},
-             {&M->f_recover, "k_recover"},           {&M->f_babd_cta, "k_babd_cta"}};
+             {&M->f_recover, "k_recover"},           {&M->f_babd_cta, "k_babd_cta"},
+             {&M->f_upper, "k_upper"}};
   for (auto& e : fns) {
     CUresult rr = g_drv.moduleGetFunction(e.f, M->mod, e.name);
     if (rr != CUDA_SUCCESS) {
@@ -549,6 +556,13 @@ extern "C" int cs_module_load(const cs_module_desc* d, cs_module** out) {
       M->tree_grid = M->sms * std::max(1, pt);
       M->big_ctas = std::max(M->big_ctas, M->tree_grid);
     }
+  }
+  if (M->upper_smem) {
+    if (M->upper_smem > 48 * 1024)
+      CS_CU(g_drv.funcSetAttribute(M->f_upper, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, (int)M->upper_smem));
+    int pu = 0;
+    CS_CU(g_drv.occupancy(&pu, M->f_upper, 128, M->upper_smem));
+    M->upper_grid = M->sms * std::max(1, std::min(pu, 16));
   }
   if (M->babd_cta_smem > (size_t)smem_optin) M->babd_cta_smem = 0;  // per-level kernels only
   else if (M->babd_cta_smem > 48 * 1024)
@@ -623,6 +637,7 @@ struct cs_batch {
   cudaGraphExec_t graph[2] = {nullptr, nullptr};
   int graph_nlvl[2] = {-1, -1};
   int graph_tune[2] = {-1, -1};
+  int graph_lo[2] = {-1, -1};  // first k_upper level the graph was captured with
   CsBatchDev graph_view[2];
   CsConsts graph_consts[2];
   // device copy of the last initial guess (cs_batch_reset)
@@ -842,6 +857,15 @@ static bool use_cta_path(const cs_batch* bt) {
   return bt->opts.babd_path == 1;
 }
 
+// First tree level handled by k_upper: the top 4 levels (at most 8 merges per
+// instance at the first of them), or nlvl (k_upper not used: large block rows,
+// or babd_path 2 asks for one launch per level).
+static const int kUpperLevels = 4;
+static int upper_levels(const cs_batch* bt, int nlvl) {
+  if (!bt->M->upper_smem || bt->opts.babd_path == 2) return nlvl;
+  return std::max(0, nlvl - kUpperLevels);
+}
+
 static int run_lists(cs_batch* bt, CsBatchDev& v, int mode, int nlvl) {
   void* args[] = {&v, &mode, &nlvl};
   return launch(bt, bt->M->f_lists, 1, 1024, 0, args);
@@ -859,17 +883,24 @@ static int run_direction(cs_batch* bt, CsBatchDev& v, int nlvl) {
     return launch_k(bt, M->f_recover, (unsigned)(M->sms * 8), 128, 0, ar, 1);
   }
   const unsigned g = (unsigned)(M->sms * 8);
-  for (int l = 0; l < nlvl; ++l) {
+  // levels from l_lo up (at most 8 merges per instance there) and the top
+  // system in one launch, CTA per instance
+  const int l_lo = upper_levels(bt, nlvl);
+  for (int l = 0; l < l_lo; ++l) {
     void* a[] = {&v, &l};
     if (M->big_tree) CS_TRY(launch_k(bt, M->f_tree_level, (unsigned)M->tree_grid, 256, M->tree_smem, a, 1));
     else CS_TRY(launch_k(bt, M->f_tree_level, g, 128, M->tree_smem, a, 1));
   }
-  {
+  if (M->upper_smem && bt->opts.babd_path != 2) {
+    int lo = l_lo;
+    void* a[] = {&v, &lo};
+    CS_TRY(launch_k(bt, M->f_upper, (unsigned)std::min(M->upper_grid, bt->B), 128, M->upper_smem, a, 1));
+  } else {
     void* a[] = {&v};
     if (M->big_tree) CS_TRY(launch_k(bt, M->f_top, (unsigned)std::min(M->big_ctas, bt->B), 256, M->top_smem, a, 1));
     else CS_TRY(launch_k(bt, M->f_top, (unsigned)(M->sms * 4), 32 * M->top_wpc, M->top_smem, a, 1));
   }
-  for (int l = nlvl - 1; l >= 0; --l) {
+  for (int l = l_lo - 1; l >= 0; --l) {
     void* a[] = {&v, &l};
     CS_TRY(launch_k(bt, M->f_backsub_level, g, 128, 0, a, 1));
   }
@@ -1125,7 +1156,8 @@ static int super_step(cs_batch* bt, const CsConsts& c, int nlvl) {
 static int get_graph(cs_batch* bt, const CsConsts& c, int nlvl, int reps) {
   const CsBatchDev v = devview(bt);
   const int k = use_cta_path(bt) ? 1 : 0;
-  if (bt->graph[k] && bt->graph_nlvl[k] == nlvl && bt->graph_tune[k] == bt->M->tune_ver &&
+  const int lo = upper_levels(bt, nlvl);
+  if (bt->graph[k] && bt->graph_nlvl[k] == nlvl && bt->graph_tune[k] == bt->M->tune_ver && bt->graph_lo[k] == lo &&
       memcmp(&bt->graph_view[k], &v, sizeof(v)) == 0 && memcmp(&bt->graph_consts[k], &c, sizeof(c)) == 0)
     return CS_OK;
   if (bt->graph[k]) {
@@ -1152,6 +1184,7 @@ static int get_graph(cs_batch* bt, const CsConsts& c, int nlvl, int reps) {
   bt->graph_consts[k] = c;
   bt->graph_nlvl[k] = nlvl;
   bt->graph_tune[k] = bt->M->tune_ver;
+  bt->graph_lo[k] = lo;
   return CS_OK;
 }
 
@@ -1236,7 +1269,7 @@ extern "C" int cs_solve(cs_batch* bt, const cs_opts* opts) {
         if (use_graph) {
           cudaError_t e = cudaGraphLaunch(bt->graph[cta ? 1 : 0], bt->stream);
           if (e != cudaSuccess) rc = set_err(CS_ERR_CUDA, std::string("graph launch: ") + cudaGetErrorString(e));
-          bt->launches += cta ? 7 : 9 + 2 * nlvl;
+          bt->launches += cta ? 7 : 9 + 2 * upper_levels(bt, nlvl);
           bt->super_steps += 1;
         } else {
           rc = super_step(bt, c, nlvl);

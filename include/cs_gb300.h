@@ -95,8 +95,10 @@ typedef struct cs_opts {
   double alpha_m;        /* final continuation parameter (0.1, or 1e-6 with inequalities) */
   double beta;           /* continuation factor */
   int check_every;       /* Newton super-steps between host checks for completion */
-  int babd_path;         /* Newton direction kernels: 0 automatic (per level), 1 one CTA
-                            per instance, 2 one launch per tree level across the instances */
+  int babd_path;         /* Newton direction kernels: 0 automatic (one launch per tree
+                            level, the top 4 levels and the top system in one CTA per
+                            instance where the block rows allow), 1 one CTA per instance
+                            for everything, 2 one launch per tree level and for the top */
   int residual_type;     /* segment residual estimate (CS:29-32): 1 weighted sum
                             (default), 2 weighted squares, 0 weighted maximum */
   int scale_by_time;     /* multiply the running estimate by h (default 1) */

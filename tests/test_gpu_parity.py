@@ -360,3 +360,28 @@ def test_nan_instance_fails_alone(cs):
         assert sols[k]["success"] == alone[k]["success"]
         assert (sols[k]["newton_steps"], sols[k]["N"]) == (alone[k]["newton_steps"], alone[k]["N"])
         np.testing.assert_array_equal(sols[k]["y"], alone[k]["y"])
+
+
+def test_fused_upper_levels_give_the_per_level_bits(cs):
+    """The upper tree levels, top system and their back substitution in one
+    CTA per instance (automatic path) give bit for bit the solves of one
+    launch per tree level (babd_path 2): counts, meshes, solutions."""
+    pr = cs.workloads.vdp_family_problem()
+    insts = [i for i in cs.workloads.vdp_batch(96, seed=41, n_range=(2, 700)) if i.m == 4][:24]
+    cp = compiled(cs, "vdp_family", 4)
+    guesses = [inst.guess() for inst in insts]
+    meshes = [(t, y, z) for t, y, z, _ in guesses]
+    P = np.stack([g[3] for g in guesses])
+    TH = np.stack([i.theta for i in insts])
+    out = []
+    for path in (0, 2):
+        bt = cs.Batch(cp, len(insts))
+        bt.set_guess(meshes, P, TH)
+        bt.solve(cs.default_opts(pr, max_nodes=20000, babd_path=path))
+        out.append(bt.solution())
+    assert sum(s["success"] for s in out[0]) >= len(insts) // 2
+    for a, b in zip(*out):
+        assert (a["success"], a["newton_steps"], a["residual_evals"], a["N"]) == \
+               (b["success"], b["newton_steps"], b["residual_evals"], b["N"])
+        np.testing.assert_array_equal(a["y"], b["y"])
+        np.testing.assert_array_equal(a["z"], b["z"])
