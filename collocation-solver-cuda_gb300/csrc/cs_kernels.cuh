@@ -1149,27 +1149,32 @@ extern "C" __global__ void k_tree_level(CsBatch bt, int l) {
     const double* srcb = (l & 1) ? bt.rows1 : bt.rows0;
     double* dstb = (l & 1) ? bt.rows0 : bt.rows1;
 #if CS_QC <= 32
-    // few merges (all fit in one round of lane groups): CS_TL lanes per merge
-    if (total * CS_TL <= (long long)gridDim.x * blockDim.x) {
-      const long long it0 = ((long long)blockIdx.x * blockDim.x + threadIdx.x) / CS_TL;
-      if ((long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31) >= total * CS_TL) return;  // warp-uniform
-      const bool active = it0 < total;
-      const long long it = active ? it0 : total - 1;
-      const int k = cs_find(pre, njac, it);
-      const int b = bt.jac[k];
-      const int mi = (int)(it - pre[k]);
-      const int off = bt.off[b];
-      const int nl = cs_rows_at(bt.N[b] - 1, l);
-      const int merges = nl >> 1;
-      const double* src = srcb + (size_t)off * CS_ROWSZ;
-      double* dst = dstb + (size_t)off * CS_ROWSZ;
-      if (mi < merges) {  // uniform within the lane group
-        cs_merge_lanes(src + (size_t)(2 * mi) * CS_ROWSZ, src + (size_t)(2 * mi + 1) * CS_ROWSZ,
-                       dst + (size_t)mi * CS_ROWSZ, bt.tree + (size_t)(off + ((2 * mi + 1) << l)) * CS_TREESZ, active);
-      } else if (active) {
-        const double* sr = src + (size_t)(nl - 1) * CS_ROWSZ;
-        double* dr = dst + (size_t)merges * CS_ROWSZ;
-        for (int q = threadIdx.x & (CS_TL - 1); q < CS_ROWSZ; q += CS_TL) dr[q] = sr[q];
+    // few merges (at most 4 rounds of lane groups over the grid): CS_TL lanes
+    // per merge; the grid is one wave of resident CTAs
+    const long long lanes = total * CS_TL, stride = (long long)gridDim.x * blockDim.x;
+    if (lanes <= 4 * stride) {
+      for (long long base = (long long)blockIdx.x * blockDim.x; base < lanes; base += stride) {
+        if (base + (threadIdx.x & ~31) >= lanes) break;  // warp-uniform, and so for later rounds
+        const long long it0 = (base + threadIdx.x) / CS_TL;
+        const bool active = it0 < total;
+        const long long it = active ? it0 : total - 1;
+        const int k = cs_find(pre, njac, it);
+        const int b = bt.jac[k];
+        const int mi = (int)(it - pre[k]);
+        const int off = bt.off[b];
+        const int nl = cs_rows_at(bt.N[b] - 1, l);
+        const int merges = nl >> 1;
+        const double* src = srcb + (size_t)off * CS_ROWSZ;
+        double* dst = dstb + (size_t)off * CS_ROWSZ;
+        if (mi < merges) {  // uniform within the lane group
+          cs_merge_lanes(src + (size_t)(2 * mi) * CS_ROWSZ, src + (size_t)(2 * mi + 1) * CS_ROWSZ,
+                         dst + (size_t)mi * CS_ROWSZ, bt.tree + (size_t)(off + ((2 * mi + 1) << l)) * CS_TREESZ,
+                         active);
+        } else if (active) {
+          const double* sr = src + (size_t)(nl - 1) * CS_ROWSZ;
+          double* dr = dst + (size_t)merges * CS_ROWSZ;
+          for (int q = threadIdx.x & (CS_TL - 1); q < CS_ROWSZ; q += CS_TL) dr[q] = sr[q];
+        }
       }
       return;
     }

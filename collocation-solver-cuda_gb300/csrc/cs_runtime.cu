@@ -268,6 +268,10 @@ struct cs_module {
   // instance): 0 when the block rows are too large for lane merges
   size_t upper_smem = 0;
   int upper_grid = 0;
+  // one wave of resident CTAs: grids of the grid-stride kernels k_residual and
+  // k_tree_level (small block rows), so that launches with little work do not
+  // dispatch waves of idle CTAs
+  int res_grid = 1, tree_small_grid = 1;
   int condense_block, condense_per_cta;
   size_t condense_smem;
   size_t tree_smem;   // per CTA of 4 warps
@@ -555,6 +559,16 @@ extern "C" int cs_module_load(const cs_module_desc* d, cs_module** out) {
       CS_CU(g_drv.occupancy(&pt, M->f_tree_level, 256, M->tree_smem));
       M->tree_grid = M->sms * std::max(1, pt);
       M->big_ctas = std::max(M->big_ctas, M->tree_grid);
+    }
+  }
+  {
+    int pr = 0;
+    CS_CU(g_drv.occupancy(&pr, M->f_residual, 256, 0));
+    M->res_grid = M->sms * std::max(1, std::min(pr, 8));
+    if (!M->big_tree) {
+      int pt = 0;
+      CS_CU(g_drv.occupancy(&pt, M->f_tree_level, 128, M->tree_smem));
+      M->tree_small_grid = M->sms * std::max(1, std::min(pt, 8));
     }
   }
   if (M->upper_smem) {
@@ -889,7 +903,7 @@ static int run_direction(cs_batch* bt, CsBatchDev& v, int nlvl) {
   for (int l = 0; l < l_lo; ++l) {
     void* a[] = {&v, &l};
     if (M->big_tree) CS_TRY(launch_k(bt, M->f_tree_level, (unsigned)M->tree_grid, 256, M->tree_smem, a, 1));
-    else CS_TRY(launch_k(bt, M->f_tree_level, g, 128, M->tree_smem, a, 1));
+    else CS_TRY(launch_k(bt, M->f_tree_level, (unsigned)M->tree_small_grid, 128, M->tree_smem, a, 1));
   }
   if (M->upper_smem && bt->opts.babd_path != 2) {
     int lo = l_lo;
@@ -1136,7 +1150,7 @@ static int super_step(cs_batch* bt, const CsConsts& c, int nlvl) {
   const unsigned g = (unsigned)(M->sms * 8);
   {
     void* args[] = {&v};
-    CS_TRY(launch_k(bt, M->f_residual, g, 256, 0, args, 2));
+    CS_TRY(launch_k(bt, M->f_residual, (unsigned)M->res_grid, 256, 0, args, 2));
   }
   bt->super_steps += 1;
   CsConsts cc = c;
@@ -1435,7 +1449,7 @@ extern "C" int cs_stage_residual(cs_batch* bt, double alpha, double* norms, doub
   int rc = run_lists(bt, v, 0, 0);
   if (rc == CS_OK) {
     void* args[] = {&v};
-    rc = launch(bt, M->f_residual, (unsigned)(M->sms * 8), 256, 0, args);
+    rc = launch(bt, M->f_residual, (unsigned)M->res_grid, 256, 0, args);
   }
   std::vector<CsInst> hi;
   if (rc == CS_OK) rc = read_inst(bt, hi);
