@@ -9,7 +9,7 @@ import pytest
 from conftest import GOLDEN, golden, pkg
 
 REF_NB = ["exContainerTransfer", "exFreespaceRocket", "exTrolley", "exUnderwaterVehicle"]
-OCP_CASES = ["vdp", "vdp_coarse", "dint_param", "pend2", "vdp_ineq", "eqcon", "vdp_input"]
+OCP_CASES = ["vdp", "vdp_coarse", "dint_param", "pend2", "vdp_ineq", "eqcon", "vdp_input", "vdp_svineq"]
 # the reference's example OCP sources are read in place (never copied); these
 # cases run only where the reference checkout is mounted
 NB_TEXT_DIR = os.path.join(os.environ.get("REF_DIR", "/root/reference"), "Notebook", "source")

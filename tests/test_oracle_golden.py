@@ -10,7 +10,7 @@ from oracle import collocation_oracle as O
 STAGES = [("vdp_n21_m4", "vdp"), ("vdp_n33_m5", "vdp"), ("dint_n33_m3", "dint_param"),
           ("pend2_n21_m5", "pend2"), ("econ_n17_m3", "eqcon")]
 E2E = [("vdp_cfg1", "vdp"), ("vdp_coarse", "vdp_coarse"), ("dint_param", "dint_param"), ("vdp_input", "vdp_input"),
-       ("pend2", "pend2"), ("vdp_ineq", "vdp_ineq")]
+       ("pend2", "pend2"), ("vdp_ineq", "vdp_ineq"), ("vdp_svineq", "vdp_svineq")]
 
 
 def test_lobatto_and_gauss_tables_match_reference():
@@ -128,9 +128,9 @@ def test_oracle_end_to_end_matches_reference(case, prob):
     # the reference prints the norms with 8 decimals
     np.testing.assert_array_equal(np.round(np.array(r.norms), 8), g["norms"])
     np.testing.assert_array_equal(r.t, g["t"])
-    np.testing.assert_allclose(r.y, g["y"], atol=1e-8, rtol=0)
-    np.testing.assert_allclose(r.z, g["z"], atol=1e-8, rtol=0)
-    np.testing.assert_allclose(r.p, g["p"], atol=1e-8, rtol=0)
+    # 1e-8 of each array's scale (a state constraint's multiplier reaches ~300)
+    for k, got in (("y", r.y), ("z", r.z), ("p", r.p)):
+        np.testing.assert_allclose(got, g[k], atol=1e-8 * max(1.0, np.abs(g[k]).max(initial=0.0)), rtol=0)
 
 
 MODES = [(rt, sc) for rt in (0, 1, 2) for sc in (True, False)]
