@@ -1039,8 +1039,9 @@ __device__ __forceinline__ void cs_backsub_thread(const double* __restrict__ rec
 // other lanes, each lane updates its own column.  Every column sees the fma
 // sequence of cs_merge_thread, so the results are the same bits; the chain of
 // FP64 instructions per lane is ~4x shorter, which is what a level with few
-// merges waits for (a warp-wide FP64 instruction occupies a sub-partition's
-// FP64 pipe for ~76 cycles on this GPU).
+// merges waits for (on this GPU a dependent FP64 instruction waits ~64 cycles,
+// and the SM's FP64 unit takes one warp instruction per ~19 cycles whatever
+// the number of active lanes).
 #define CS_TL ((CS_QC <= 16) ? 16 : 32)
 __device__ __forceinline__ void cs_merge_lanes(const double* __restrict__ ra, const double* __restrict__ rb,
                                                double* __restrict__ out_row, double* __restrict__ rec, bool active) {
