@@ -19,7 +19,7 @@ pytestmark = pytest.mark.gpu
 STAGES = [("vdp_n21_m4", "vdp"), ("vdp_n33_m5", "vdp"), ("dint_n33_m3", "dint_param"),
           ("pend2_n21_m5", "pend2"), ("econ_n17_m3", "eqcon")]
 E2E = [("vdp_cfg1", "vdp"), ("vdp_coarse", "vdp_coarse"), ("dint_param", "dint_param"), ("vdp_input", "vdp_input"),
-       ("pend2", "pend2"), ("vdp_ineq", "vdp_ineq"), ("vdp_svineq", "vdp_svineq")]
+       ("pend2", "pend2"), ("vdp_ineq", "vdp_ineq"), ("vdp_svineq", "vdp_svineq"), ("vdp_m7", "vdp")]
 
 
 @pytest.fixture(scope="module")
@@ -259,12 +259,12 @@ def test_autotuned_condensation_gives_identical_solves(cs):
         np.testing.assert_array_equal(s0["y"], s1["y"])
 
 
-@pytest.mark.parametrize("m", [2, 10])
+@pytest.mark.parametrize("m", [2, 6, 8, 9, 10])
 def test_extreme_collocation_orders_match_oracle(cs, m):
-    """The smallest and largest m of the tables (the reference's CLI allows
-    3..10): stage residual, Newton direction and a whole solve against the
-    oracle (with the tables computed here; the reference's m = 10 table has
-    a known missing entry)."""
+    """The orders not pinned by a reference solve (3, 4, 5 and 7 are; the
+    reference's CLI allows 3..10, the tables go down to 2): a whole solve
+    against the oracle, with the tables computed here (the reference's m = 10
+    table has a known missing entry)."""
     pr = load_problem("vdp")
     cp = compiled(cs, "vdp", m)
     ref = O.solve(oracle_problem("vdp"), m, cs.tables.lobatto(m), cs.tables.segment_tables(m))
