@@ -385,3 +385,61 @@ def test_fused_upper_levels_give_the_per_level_bits(cs):
                (b["success"], b["newton_steps"], b["residual_evals"], b["N"])
         np.testing.assert_array_equal(a["y"], b["y"])
         np.testing.assert_array_equal(a["z"], b["z"])
+
+
+def test_fused_upper_levels_on_mixed_mesh_sizes(cs):
+    """One batch with meshes of 2 to 700 nodes: instances whose whole tree is
+    inside the fused levels (or has no level at all) next to ones with levels
+    below them; same bits as one launch per level."""
+    pr = load_problem("vdp_family")
+    cp = compiled(cs, "vdp_family", 3)
+    rng = np.random.default_rng(8)
+    sizes = [2, 3, 5, 9, 17, 33, 65, 300, 700, 4]
+    meshes, thetas = [], []
+    for N in sizes:
+        t = np.linspace(0.0, float(rng.uniform(2, 5)), N)
+        meshes.append((t, np.zeros((N, cp.ny)), np.zeros((N, cp.nz))))
+        thetas.append([rng.uniform(-1, 1), rng.uniform(-1, 1), float(np.exp(rng.uniform(np.log(0.5), np.log(2))))])
+    out = []
+    for path in (0, 2):
+        bt = cs.Batch(cp, len(sizes))
+        bt.set_guess(meshes, np.ones((len(sizes), cp.np)), np.array(thetas))
+        bt.solve(cs.default_opts(pr, max_nodes=20000, babd_path=path))
+        out.append(bt.solution())
+    for a, b in zip(*out):
+        assert (a["success"], a["newton_steps"], a["residual_evals"], a["N"]) == \
+               (b["success"], b["newton_steps"], b["residual_evals"], b["N"])
+        np.testing.assert_array_equal(a["y"], b["y"])
+        np.testing.assert_array_equal(a["p"], b["p"])
+
+
+def test_progress_hook_sees_every_check(cs):
+    """cs_batch_set_progress: called after every check of the Newton phase
+    with the instances still iterating; the statuses may be read from it; the
+    solve's results do not change."""
+    pr = load_problem("vdp_family")
+    cp = compiled(cs, "vdp_family", 4)
+    insts = [i for i in cs.workloads.vdp_batch(32, seed=3, n_range=(32, 200)) if i.m == 4][:6]
+    guesses = [inst.guess() for inst in insts]
+    meshes = [(t, y, z) for t, y, z, _ in guesses]
+    P, TH = np.stack([g[3] for g in guesses]), np.stack([i.theta for i in insts])
+    opts = cs.default_opts(pr, max_nodes=20000)
+    seen = []
+    bt = cs.Batch(cp, len(insts))
+    bt.set_guess(meshes, P, TH)
+    bt.set_progress(lambda active, steps: seen.append((active, steps, tuple(bt.statuses()))))
+    bt.solve(opts)
+    hooked = bt.solution()
+    bt.set_progress(None)
+    assert seen and all(0 <= a <= len(insts) for a, _, _ in seen)
+    steps = [s for _, s, _ in seen]
+    assert steps == sorted(steps) and steps[-1] > 0
+    # the last check ends the last Newton phase: nobody is iterating any more
+    # (converged ones may still await their segment residual)
+    assert seen[-1][0] == 0 and all(st not in (0, 1) for st in seen[-1][2])
+    bt2 = cs.Batch(cp, len(insts))
+    bt2.set_guess(meshes, P, TH)
+    bt2.solve(opts)
+    for a, b in zip(hooked, bt2.solution()):
+        assert (a["success"], a["newton_steps"], a["N"]) == (b["success"], b["newton_steps"], b["N"])
+        np.testing.assert_array_equal(a["y"], b["y"])
