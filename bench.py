@@ -16,7 +16,8 @@ from the plain guess.
 
   value  solves/s (instances reaching the tolerance), inputs resident in HBM
   e2e    the same through the C ABI from pinned host buffers: features and
-         plain guesses H2D, solutions D2H, inside the timed region
+         plain guesses H2D, solutions D2H, inside the timed region (one host
+         thread per m-group, as for value)
   plain_batched      the same batch from the plain (zero) guess
   plain_single_gpu   the plain solver one instance at a time (a random sample)
 
@@ -561,33 +562,41 @@ def run_warm(args, cs, rank, world, local_rank, cpu, cfg):
         hosts.append((hh, out))
     h2d = Xh.array.nbytes + sum(sum(a.array.nbytes for a in hh.values()) for hh, _ in hosts)
     d2h = 0
+    def e2e_group(g, hh, out, res):
+        # one m-group on its own host thread, as in the device-resident run:
+        # guesses from pinned host memory, warm start, solve, solutions back to
+        # pinned host memory, the failed instances again from the plain guess
+        bt = g["bt"]
+        bt.set_guess_packed(hh["N"].array, hh["t"].array, hh["y"].array, hh["z"].array, hh["p"].array,
+                            hh["th"].array)
+        bt.warm_start(runner.dY.ptr + 4 * g["first"] * net.n_out, ws.N_NODES, net.n_out)
+        bt.solve(solver.opts)
+        Nn, T = bt.sizes()
+        st = (cs._lib.Stats * bt.B)()
+        cs._lib.check(bt._lib.cs_get_solution(bt.handle, cs._lib.dptr(out["t"].array), cs._lib.dptr(out["y"].array),
+                                              cs._lib.dptr(out["z"].array), cs._lib.dptr(out["p"].array), st),
+                      "cs_get_solution")
+        failed = [runner.instances[g["first"] + b] for b in range(bt.B) if st[b].status != 3]
+        n_ok = bt.B - len(failed)
+        if failed:
+            n_ok += sum(int(s["success"]) for s in solver.solve(failed))
+        res[g["m"]] = (n_ok, 8 * T * (1 + fam.ny + fam.nz) + 8 * bt.B * fam.np + bt.B * 64)
+
     _barrier(dist)
     t0 = time.perf_counter()
     for _ in range(args.steps):
         runner.dX.upload(Xh.array)
         net.predict_device(runner.dX, len(runner.instances), runner.dY)
-        d2h = 0
-        n_e2e = 0
-        failed = []
-        for g, (hh, out) in zip(runner.groups, hosts):
-            bt = g["bt"]
-            bt.set_guess_packed(hh["N"].array, hh["t"].array, hh["y"].array, hh["z"].array, hh["p"].array,
-                                hh["th"].array)
-            bt.warm_start(runner.dY.ptr + 4 * g["first"] * net.n_out, ws.N_NODES, net.n_out)
-            bt.solve(solver.opts)
-            Nn, T = bt.sizes()
-            st = (cs._lib.Stats * bt.B)()
-            cs._lib.check(bt._lib.cs_get_solution(bt.handle, cs._lib.dptr(out["t"].array), cs._lib.dptr(out["y"].array),
-                                                  cs._lib.dptr(out["z"].array), cs._lib.dptr(out["p"].array), st),
-                          "cs_get_solution")
-            d2h += 8 * T * (1 + fam.ny + fam.nz) + 8 * bt.B * fam.np + bt.B * 64
-            for b in range(bt.B):
-                if st[b].status == 3:
-                    n_e2e += 1
-                else:
-                    failed.append(runner.instances[g["first"] + b])
-        if failed:
-            n_e2e += sum(int(s["success"]) for s in solver.solve(failed))
+        res = {}
+        ths = [threading.Thread(target=e2e_group, args=(g, hh, out, res)) for g, (hh, out) in zip(runner.groups, hosts)]
+        for th in ths:
+            th.start()
+        for th in ths:
+            th.join()
+        if len(res) != len(runner.groups):
+            raise RuntimeError("end-to-end step: an m-group failed")
+        n_e2e = sum(v[0] for v in res.values())
+        d2h = sum(v[1] for v in res.values())
     dte = _max_over_ranks(dist, time.perf_counter() - t0)
     e2e = {"value": _sum_over_ranks(dist, args.steps * n_e2e) / dte, "unit": "solves/s", "h2d_bytes_per_step": h2d,
            "d2h_bytes_per_step": d2h}
