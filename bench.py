@@ -572,6 +572,8 @@ def run_warm(args, cs, rank, world, local_rank, cpu, cfg):
         bt.warm_start(runner.dY.ptr + 4 * g["first"] * net.n_out, ws.N_NODES, net.n_out)
         bt.solve(solver.opts)
         Nn, T = bt.sizes()
+        if T > out["t"].array.shape[0]:
+            raise RuntimeError("solution larger than the pinned output buffers")
         st = (cs._lib.Stats * bt.B)()
         cs._lib.check(bt._lib.cs_get_solution(bt.handle, cs._lib.dptr(out["t"].array), cs._lib.dptr(out["y"].array),
                                               cs._lib.dptr(out["z"].array), cs._lib.dptr(out["p"].array), st),
