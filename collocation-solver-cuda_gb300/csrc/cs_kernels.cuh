@@ -29,7 +29,7 @@
 //                    assembly and norm                 collocation_solver_parallel_2d_shared.py:399-559, 116
 //   k_condense       construct_jacobian_kernel + reduce_jacobian_parallel_kernel
 //                                                      collocation_solver_parallel_2d_shared.py:680-1001
-//   k_tree_level, k_top, k_backsub_level, k_recover
+//   k_tree_level, k_upper, k_top, k_backsub_level, k_recover
 //                    partition_factorization_kernel, the host reduced solve,
 //                    partition_backward_substitution_kernel, recover_delta_k_kernel
 //                                                      solve_babd_system.py:161-572, collocation_solver_parallel_2d_shared.py:1619-1650
