@@ -50,6 +50,7 @@ E2E_CASES = [
     ("vdp_input", "vdp_input.ocp", 4),
     ("vdp_svineq", "vdp_svineq.ocp", 3),
     ("vdp_m7", "vdp.ocp", 7),
+    ("eqcon", "eqcon.ocp", 3),
 ]
 # (case name, ocp file, m, N nodes, seed) for per-stage dumps
 STAGE_CASES = [

@@ -10,7 +10,8 @@ from oracle import collocation_oracle as O
 STAGES = [("vdp_n21_m4", "vdp"), ("vdp_n33_m5", "vdp"), ("dint_n33_m3", "dint_param"),
           ("pend2_n21_m5", "pend2"), ("econ_n17_m3", "eqcon")]
 E2E = [("vdp_cfg1", "vdp"), ("vdp_coarse", "vdp_coarse"), ("dint_param", "dint_param"), ("vdp_input", "vdp_input"),
-       ("pend2", "pend2"), ("vdp_ineq", "vdp_ineq"), ("vdp_svineq", "vdp_svineq"), ("vdp_m7", "vdp")]
+       ("pend2", "pend2"), ("vdp_ineq", "vdp_ineq"), ("vdp_svineq", "vdp_svineq"), ("vdp_m7", "vdp"),
+       ("eqcon", "eqcon")]
 
 
 def test_lobatto_and_gauss_tables_match_reference():
