@@ -53,7 +53,12 @@ size_t scratch_doubles(const BabdDims& d) {
   return 2 * (size_t)d.n * d.rowsz + (size_t)(d.n + 1) * d.treesz;
 }
 
-constexpr double kEps = 2.220446049250313e-16;
+// A reflection is skipped only for a column that is zero below (and on) the
+// diagonal (entries under about 1e-145): any other column is reflected whatever its scale, so a system
+// multiplied by any factor gives the same solution (an absolute cut-off of
+// the order of eps would leave the columns of a system scaled by 1e-9
+// unreduced and the back substitution wrong).
+constexpr double kZeroVs = 1e-290;
 
 __device__ __forceinline__ int rows_at(int n0, int l) {
   int n = n0;
@@ -118,7 +123,7 @@ __global__ void kb_level(BabdDims d, int l, const double* src, double* dst, doub
       const double v0 = x0 - g;
       const double vs = ss - x0 * x0 + v0 * v0;
       __syncwarp();
-      if (vs < kEps) continue;
+      if (vs < kZeroVs) continue;
       const double beta = -2.0 / vs;
       for (int c = k + 1 + lane; c < d.qc; c += 32) {
         double* col = Q + (size_t)c * d.qld;
@@ -178,7 +183,7 @@ __global__ void kb_top(BabdDims d, const double* row, const double* B0, const do
     const double v0 = x0 - g;
     const double vs = ss - x0 * x0 + v0 * v0;
     __syncwarp();
-    if (vs < kEps) continue;
+    if (vs < kZeroVs) continue;
     const double beta = -2.0 / vs;
     for (int c = k + 1 + lane; c < nt + 1; c += 32) {
       double* col = top + (size_t)c * tld;

@@ -226,8 +226,7 @@ int cs_babd_solve(int ny, int np, int n, const double* A, const double* C, const
 
 /* cs_babd_solve without any device allocation, for callers that cannot call
  * cudaMalloc: code that runs inside a memory pool or allocator it must not
- * re-enter, inside a CUDA graph being built, or under a framework that owns
- * all device memory.  It has no counterpart in the reference (whose stage
+ * re-enter, or under a framework that owns all device memory.  It has no counterpart in the reference (whose stage
  * functions allocate device arrays on every call).
  * Same arguments and results as cs_babd_solve.  Its scratch is a fixed 32 MiB
  * array compiled into this library, held by every GPU that loads the library

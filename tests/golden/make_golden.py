@@ -22,8 +22,8 @@ Outputs (all small, committed):
   evaluated at seeded random points, plus the generated BvpDae attributes.
 * the OCP sources used are in ``ocp/``.
 
-Usage:  python tests/golden/make_golden.py [case ...]
-Needs /root/reference (read-only) and sympy; runs in a few minutes.
+Usage:  REF_DIR=<reference checkout> python tests/golden/make_golden.py [case ...]
+Needs the reference checkout (read-only) and sympy; runs in a few minutes.
 """
 import json
 import os
@@ -35,7 +35,9 @@ import tempfile
 
 import numpy as np
 
-REF_DIR = os.environ.get("REF_DIR", "/root/reference")
+REF_DIR = os.environ.get("REF_DIR")
+if not REF_DIR and __name__ == "__main__":
+    sys.exit("set REF_DIR to the reference checkout (read-only), e.g. REF_DIR=/root/reference")
 HERE = os.path.dirname(os.path.abspath(__file__))
 SHIM = os.path.join(HERE, "refshim")
 OCP_DIR = os.path.join(HERE, "ocp")

@@ -80,3 +80,20 @@ def test_babd_solve_rejects_bad_sizes():
     nul = [None] * 10
     assert lib.cs_babd_solve(40, 0, 10, *nul, None, None) == 1
     assert "ny" in cs._lib.last_error()
+
+
+@pytest.mark.parametrize("fn", ["cs_babd_solve", "cs_babd_solve_noalloc"])
+@pytest.mark.parametrize("scale", [1e-9, 1e9])
+def test_babd_solve_is_scale_invariant(fn, scale):
+    """Every equation multiplied by the same factor leaves the solution
+    unchanged: no reflection may be skipped because its column is small in
+    absolute terms (a system scaled by 1e-9 has columns of norm ~1e-9)."""
+    cs = pkg()
+    ny, npar, n = 4, 2, 300
+    A, C, H, b, B0, Bn, Vn, r = random_babd(ny, npar, n, seed=77)
+    dy0, dp0, s0 = babd_gpu(cs, fn, ny, npar, n, A, C, H, b, B0, Bn, Vn, r)
+    dy1, dp1, s1 = babd_gpu(cs, fn, ny, npar, n, *[scale * x for x in (A, C, H, b, B0, Bn, Vn, r)])
+    assert s0 == s1 == 0
+    sc = max(1.0, np.abs(dy0).max())
+    np.testing.assert_allclose(dy1, dy0, rtol=0, atol=1e-10 * sc)
+    np.testing.assert_allclose(dp1, dp0, rtol=0, atol=1e-10 * sc)

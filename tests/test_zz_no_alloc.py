@@ -72,6 +72,54 @@ def test_noalloc_matches_allocating_solve_on_consecutive_calls():
     np.testing.assert_allclose(dy1, g["delta_y"], rtol=0, atol=1e-8 * max(1.0, np.abs(g["delta_y"]).max()))
 
 
+def test_noalloc_without_parameters():
+    """np = 0 with H, Vn and dp passed as NULL, which the entry point
+    accepts: same solution as the allocating solve."""
+    cs = pkg()
+    lib = cs._lib.load()
+    ny, n = 6, 257
+    A, C, _, b, B0, Bn, _, r = _random_system(ny, 0, n, seed=5)
+    ins = [_dev(x) for x in (A, C, b, B0, Bn, r)]
+    outs = []
+    for fn in ("cs_babd_solve", "cs_babd_solve_noalloc"):
+        dy = torch.zeros((n + 1) * ny, dtype=torch.float64, device="cuda")
+        sing = ctypes.c_int(-1)
+        torch.cuda.synchronize()
+        a, c, bb, b0, bn, rr = [ctypes.c_void_p(t.data_ptr()) for t in ins]
+        rc = getattr(lib, fn)(ny, 0, n, a, c, None, bb, b0, bn, None, rr, ctypes.c_void_p(dy.data_ptr()), None,
+                              ctypes.byref(sing), None)
+        torch.cuda.synchronize()
+        assert rc == 0, cs._lib.last_error()
+        assert sing.value == 0
+        outs.append(dy.cpu().numpy())
+    np.testing.assert_allclose(outs[1], outs[0], rtol=0, atol=1e-8 * max(1.0, np.abs(outs[0]).max()))
+
+
+def test_noalloc_leaves_free_device_memory_unchanged():
+    """A call near the size limit (ny = 4, np = 2: 25,000 intervals, where the
+    allocating solve takes about 30 MB) changes the free device memory by
+    nothing once the library is loaded."""
+    cs = pkg()
+    lib = cs._lib.load()
+    ny, npar, n = 4, 2, 25000
+    system = _random_system(ny, npar, n, seed=9)
+    rc, dy0, _, _ = _solve(lib, "cs_babd_solve_noalloc", ny, npar, n, system)  # loads the library's module
+    assert rc == 0, cs._lib.last_error()
+    A, C, H, b, B0, Bn, Vn, r = [_dev(x) for x in system]
+    dy = torch.zeros((n + 1) * ny, dtype=torch.float64, device="cuda")
+    dp = torch.zeros(npar, dtype=torch.float64, device="cuda")
+    sing = ctypes.c_int(-1)
+    args = [ctypes.c_void_p(t.data_ptr()) for t in (A, C, H, b, B0, Bn, Vn, r, dy, dp)]
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    rc = lib.cs_babd_solve_noalloc(ny, npar, n, *args, ctypes.byref(sing), None)
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert rc == 0, cs._lib.last_error()
+    assert free1 == free0
+    np.testing.assert_array_equal(dy.cpu().numpy().reshape(n + 1, ny), dy0)
+
+
 def test_noalloc_rejects_systems_beyond_its_scratch():
     cs = pkg()
     lib = cs._lib.load()
