@@ -670,13 +670,12 @@ def run_plain(args, cs, rank, world, local_rank, cpu, cfg, instances):
 
 
 # ------------------------------------------------ large single instances ---
-PENDULUM = {16: dict(m=5, nodes=8193, tol=1e-6, seed=0), 32: dict(m=4, nodes=16385, tol=1e-8, seed=2)}
+def _pendulum_configs():
+    return _pkg().workloads.PENDULUM_CHAINS
 
 
 def pendulum_problem(cs, K):
-    c = PENDULUM[K]
-    theta0 = np.random.default_rng(c["seed"]).uniform(-0.5, 0.5, K)
-    return cs.ocp.Problem(cs.workloads.pendulum_ocp(K, theta0, nodes=c["nodes"], tol=c["tol"]), name="pend%d" % K)
+    return cs.workloads.pendulum_chain_problem(K)
 
 
 def executed_flops_per_interval(m, ny, nz, npe):
@@ -726,7 +725,7 @@ def run_pendulum_reference(args, cs, cores):
     is one residual and one Newton step on 256 intervals, scaled to the
     full mesh and the solve's counts (3 Newton steps, 7 residuals, as the
     GPU solve of this configuration takes)."""
-    c = PENDULUM[args.pendulum]
+    c = _pendulum_configs()[args.pendulum]
     pr = pendulum_problem(cs, args.pendulum)
     n_int = c["nodes"] - 1
     for _ in range(args.warmup):
@@ -754,7 +753,7 @@ def run_pendulum(args, cs, rank, world, local_rank):
     """One large instance per step (pendulum chain, FP64): solves/s, e2e from
     host buffers, roofline of the condensation, the oracle extrapolated."""
     K = args.pendulum
-    c = PENDULUM[K]
+    c = _pendulum_configs()[K]
     m, nodes = c["m"], c["nodes"]
     cores = os.cpu_count() or 1
     pr = pendulum_problem(cs, K)
@@ -923,7 +922,7 @@ def main():
         cs.build.build_library()
         lib = cs._lib.load()
         pr = pendulum_problem(cs, args.pendulum)
-        cp = cs.CompiledProblem(pr, PENDULUM[args.pendulum]["m"], precision=args.precision)
+        cp = cs.CompiledProblem(pr, _pendulum_configs()[args.pendulum]["m"], precision=args.precision)
         bt = cs.Batch(cp, 1)
         bt.set_guess([(np.asarray(pr.T0, float), np.asarray(pr.Y0, float), np.asarray(pr.Z0, float))],
                      np.asarray(pr.P0, float).reshape(1, -1))

@@ -8,6 +8,10 @@ vdp_batch       Van der Pol family: x0 ~ U[-2,2]^2, T ~ U[2,8], control weight
 pendulum_ocp    OCP text of a chain of K pendulums (coupling k, free ends,
                 every 4th pendulum actuated, cost |theta|^2 + |theta'|^2 +
                 0.1 |u|^2 on [0, T]); initial angles are instance constants.
+pendulum_chain_problem
+                the single large instances: K = 16 (Nodes 8193, m = 5,
+                tol 1e-6, theta(0) seed 0) and K = 32 (Nodes 16385, m = 4,
+                tol 1e-8, seed 2).
 """
 import os
 
@@ -150,3 +154,17 @@ def pendulum_ocp(K, theta0, T=10.0, k=0.5, nodes=101, actuated_every=4, ctrl_wei
         'OutputFile = "pendulum%d.data";' % K,
     ]
     return "\n".join(lines) + "\n"
+
+
+# the single large instances: chain length K -> collocation points, nodes,
+# tolerance and the seed of theta(0) ~ U[-0.5, 0.5]^K
+PENDULUM_CHAINS = {16: dict(m=5, nodes=8193, tol=1e-6, seed=0), 32: dict(m=4, nodes=16385, tol=1e-8, seed=2)}
+
+
+def pendulum_chain_problem(K, nodes=None):
+    """The large pendulum-chain instance of length K (16 or 32) with its
+    initial guess theta_i(t) = theta_i(0) (1 - t/T), other values 0, on a
+    uniform mesh of `nodes` (default: the stated size)."""
+    c = PENDULUM_CHAINS[K]
+    theta0 = np.random.default_rng(c["seed"]).uniform(-0.5, 0.5, K)
+    return Problem(pendulum_ocp(K, theta0, nodes=nodes or c["nodes"], tol=c["tol"]), name="pend%d" % K)

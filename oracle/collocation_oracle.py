@@ -86,24 +86,25 @@ def compute_f_q(prob, m, N, rk, t, y, y_dot, z_tilde, p, alpha):
 
 
 # --------------------------------------------------------------- jacobian ---
-def construct_jacobian(prob, m, N, rk, t, y, y_tilde, z_tilde, p, alpha):
-    """J, V, D, W per interval and B_0, B_n, V_n (CS:611-797)."""
+def interval_jacobian(prob, m, rk, h, y_tilde, z_tilde, p, alpha):
+    """J, V, D, W of the intervals of widths h, from the stage values of
+    those intervals (CS:680-797); every interval is computed on its own."""
     ny, nz, npar = prob.ny, prob.nz, prob.np
+    n = len(h)
     s = m * (ny + nz)
-    h = t[1:] - t[:-1]
-    Df = prob.Df(y_tilde, z_tilde, p, prob.theta).reshape(N - 1, m, ny, ny + nz + npar)
-    Dg = prob.Dg(y_tilde, z_tilde, p, prob.theta, alpha).reshape(N - 1, m, nz, ny + nz + npar)
-    J = np.zeros((N - 1, m, ny + nz, ny))
-    V = np.zeros((N - 1, m, ny + nz, npar))
+    Df = prob.Df(y_tilde, z_tilde, p, prob.theta).reshape(n, m, ny, ny + nz + npar)
+    Dg = prob.Dg(y_tilde, z_tilde, p, prob.theta, alpha).reshape(n, m, nz, ny + nz + npar)
+    J = np.zeros((n, m, ny + nz, ny))
+    V = np.zeros((n, m, ny + nz, npar))
     J[:, :, :ny, :] = Df[:, :, :, :ny]
     J[:, :, ny:, :] = Dg[:, :, :, :ny]
     V[:, :, :ny, :] = Df[:, :, :, ny + nz:]
     V[:, :, ny:, :] = Dg[:, :, :, ny + nz:]
-    D = np.zeros((N - 1, ny, m, ny + nz))
+    D = np.zeros((n, ny, m, ny + nz))
     for j in range(m):
         for k in range(ny):
             D[:, k, j, k] = h * rk.b[j]
-    W = np.zeros((N - 1, m, ny + nz, m, ny + nz))
+    W = np.zeros((n, m, ny + nz, m, ny + nz))
     for j in range(m):
         for k in range(m):
             hA = (h * rk.A[j, k])[:, None, None]
@@ -113,12 +114,21 @@ def construct_jacobian(prob, m, N, rk, t, y, y_tilde, z_tilde, p, alpha):
                 W[:, j, :ny, k, :ny] -= np.eye(ny)[None]
                 W[:, j, :ny, k, ny:] = Df[:, j, :, ny:ny + nz]
                 W[:, j, ny:, k, ny:] = Dg[:, j, :, ny:ny + nz]
+    return J.reshape(n * s, ny), V.reshape(n * s, npar), D.reshape(n * ny, s), W.reshape(n * s, s)
+
+
+def boundary_jacobian(prob, N, y, p):
+    """B_0, B_n, V_n: the columns of Dr for y_0, y_n and p (CS:611-797)."""
+    ny = prob.ny
     dr = prob.Dr(y[0], y[N - 1], p, prob.theta)
-    B_0 = dr[:, 0:ny].copy()
-    B_n = dr[:, ny:2 * ny].copy()
-    V_n = dr[:, 2 * ny:].copy()
-    return (J.reshape((N - 1) * s, ny), V.reshape((N - 1) * s, npar), D.reshape((N - 1) * ny, s),
-            W.reshape((N - 1) * s, s), B_0, B_n, V_n)
+    return dr[:, 0:ny].copy(), dr[:, ny:2 * ny].copy(), dr[:, 2 * ny:].copy()
+
+
+def construct_jacobian(prob, m, N, rk, t, y, y_tilde, z_tilde, p, alpha):
+    """J, V, D, W per interval and B_0, B_n, V_n (CS:611-797)."""
+    J, V, D, W = interval_jacobian(prob, m, rk, t[1:] - t[:-1], y_tilde, z_tilde, p, alpha)
+    B_0, B_n, V_n = boundary_jacobian(prob, N, y, p)
+    return J, V, D, W, B_0, B_n, V_n
 
 
 def reduce_jacobian(ny, nz, npar, m, N, W, D, J, V, f_a, f_b):
@@ -421,21 +431,51 @@ class SolveResult:
     pass
 
 
-def newton_step(prob, m, N, rk, t, y, y_dot, z_tilde, p, alpha, f_a, f_b, r_bc, y_tilde, M=8):
+def newton_step(prob, m, N, rk, t, y, y_dot, z_tilde, p, alpha, f_a, f_b, r_bc, y_tilde, M=8, chunk=None):
     """Jacobian, condensation, partitioned BABD solve and recovery: the Newton
-    direction (CS:121-152)."""
+    direction (CS:121-152).
+
+    chunk: intervals per pass of the Jacobian, condensation and recovery
+    (default: all at once).  Each interval is computed on its own, so any
+    chunk gives the same numbers; a chunk bounds the memory of the stage
+    matrices W (s x s per interval: 38 GB for 16,384 intervals of s = 544),
+    which the recovery forms again, as the reference re-factorises them."""
     ny, nz, npar = prob.ny, prob.nz, prob.np
-    J, V, D, W, B_0, B_n, V_n = construct_jacobian(prob, m, N, rk, t, y, y_tilde, z_tilde, p, alpha)
-    A, C, H, b = reduce_jacobian(ny, nz, npar, m, N, W, D, J, V, f_a, f_b)
+    n_int = N - 1
+    chunk = n_int if chunk is None else max(1, int(chunk))
+    h = t[1:] - t[:-1]
+    A = np.empty((n_int * ny, ny))
+    C = np.empty((n_int * ny, ny))
+    H = np.empty((n_int * ny, npar))
+    b = np.empty((n_int, ny))
+
+    def blocks(i0, i1):
+        return interval_jacobian(prob, m, rk, h[i0:i1], y_tilde[i0 * m:i1 * m], z_tilde[i0 * m:i1 * m], p, alpha)
+
+    for i0 in range(0, n_int, chunk):
+        i1 = min(n_int, i0 + chunk)
+        J, V, D, W = blocks(i0, i1)
+        Ac, Cc, Hc, bc = reduce_jacobian(ny, nz, npar, m, i1 - i0 + 1, W, D, J, V, f_a[i0:i1], f_b[i0:i1])
+        A[i0 * ny:i1 * ny], C[i0 * ny:i1 * ny], H[i0 * ny:i1 * ny], b[i0:i1] = Ac, Cc, Hc, bc
+    B_0, B_n, V_n = boundary_jacobian(prob, N, y, p)
     dy, dp = solve_babd(ny, npar, N, A, C, H, b, B_0, B_n, V_n, r_bc, M=M)
-    _, dyd, dzt = recover_delta_k(ny, nz, m, N, dy, dp, f_a, J, V, W)
+    dyd = np.empty((n_int * m, ny))
+    dzt = np.empty((n_int * m, nz))
+    for i0 in range(0, n_int, chunk):
+        i1 = min(n_int, i0 + chunk)
+        J, V, D, W = blocks(i0, i1)
+        _, dyd[i0 * m:i1 * m], dzt[i0 * m:i1 * m] = recover_delta_k(ny, nz, m, i1 - i0 + 1, dy[i0:i1 + 1], dp,
+                                                                    f_a[i0:i1], J, V, W)
     return dy, dyd, dzt, dp
 
 
 def solve(prob, m, rk, seg, T0=None, Y0=None, Z0=None, P0=None, verbose=False, M=8, residual_type=1,
-          scale_by_time=True, residual2=False):
+          scale_by_time=True, residual2=False, chunk=None, trace=None):
     """The reference driver (CS:36-251): alpha continuation, damped Newton with
-    a halving line search, segment residual and remesh.  Returns SolveResult."""
+    a halving line search, segment residual and remesh.  Returns SolveResult.
+    chunk: see newton_step.  trace(event, **data), when given, is called with
+    ("direction", dy=, dp=) after every Newton direction (used to record the
+    first direction of large fixtures)."""
     ny, nz, npar = prob.ny, prob.nz, prob.np
     t_span = np.array(prob.T0 if T0 is None else T0, dtype=np.float64).copy()
     y0 = np.array(prob.Y0 if Y0 is None else Y0, dtype=np.float64)
@@ -473,7 +513,9 @@ def solve(prob, m, rk, seg, T0=None, Y0=None, Z0=None, P0=None, verbose=False, M
                 break
             res.jacobian_count += 1
             dy, dyd, dzt, dp = newton_step(prob, m, N, rk, t_span, y, y_dot, z_tilde, para, alpha,
-                                           f_a, f_b, r_bc, y_tilde, M=M)
+                                           f_a, f_b, r_bc, y_tilde, M=M, chunk=chunk)
+            if trace is not None:
+                trace("direction", dy=dy, dp=dp)
             a0 = 1.0
             for _ in range(max_linesearch):
                 yn = y + a0 * dy

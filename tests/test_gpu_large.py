@@ -251,3 +251,75 @@ def test_pendulum8_hybrid_layout_matches_oracle(cs):
     assert (s["N"], s["newton_steps"], s["residual_evals"]) == (ref.N, ref.jacobian_count, ref.residual_count)
     np.testing.assert_allclose(s["y"], ref.y, rtol=0, atol=1e-8)
     np.testing.assert_allclose(s["z"], ref.z, rtol=0, atol=1e-8)
+
+
+# ------------------------------------------ the stated sizes, against the oracle ---
+def _stated_size(cs, K, precision="fp64"):
+    pr = cs.workloads.pendulum_chain_problem(K)
+    cp = cs.CompiledProblem(pr, cs.workloads.PENDULUM_CHAINS[K]["m"], precision=precision)
+    bt = cs.Batch(cp, 1)
+    bt.set_guess([(np.asarray(pr.T0, float), np.asarray(pr.Y0, float), np.asarray(pr.Z0, float))],
+                 np.asarray(pr.P0, float).reshape(1, -1))
+    return pr, cp, bt
+
+
+def _rows(a, g):
+    """The fixture's node rows: every `stride`-th node and the last."""
+    n = a.shape[0]
+    return a[np.unique(np.r_[np.arange(0, n, int(g["stride"])), n - 1])]
+
+
+@pytest.mark.parametrize("K", [16, 32])
+def test_pendulum_chain_at_stated_size_matches_oracle(cs, K):
+    """Configs 2 and 4 at their stated sizes in FP64 (K = 16: Nodes 8193,
+    m = 5, tol 1e-6; K = 32: Nodes 16385, m = 4, tol 1e-8) against the
+    oracle's solve of the same instance from the same guess
+    (tests/golden/make_large_golden.py): the first Newton direction within
+    1e-8 of its scale, then the whole solve with the same Newton and residual
+    counts, remeshes and final mesh, y, z, p within 1e-8 of their scale."""
+    g = golden("large_pend%d" % K)
+    pr, cp, bt = _stated_size(cs, K)
+    N0 = len(pr.T0)
+    d = bt.stage_newton_direction(0.1)
+    sc = max(1.0, np.abs(g["dy0"]).max())
+    np.testing.assert_allclose(_rows(d["dy"][:N0], g), g["dy0"], rtol=0, atol=1e-8 * sc)
+    np.testing.assert_allclose(d["dp"][0], g["dp0"], rtol=0, atol=1e-8 * sc)
+    del bt
+    _, _, bt = _stated_size(cs, K)
+    bt.solve(cs.default_opts(pr))
+    s = bt.solution()[0]
+    assert s["success"] == bool(g["success"])
+    assert (s["newton_steps"], s["residual_evals"], s["N"], s["remeshes"]) == \
+           (int(g["jacobian_counts"]), int(g["residual_counts"]), int(g["N"]), len(g["nodes_after_remesh"]))
+    np.testing.assert_array_equal(s["t"], g["t"])
+    for k in ("y", "z"):
+        ref = g[k]
+        np.testing.assert_allclose(_rows(s[k], g), ref, rtol=0, atol=1e-8 * max(1.0, np.abs(ref).max()), err_msg=k)
+    np.testing.assert_allclose(s["p"], g["p"], rtol=0, atol=1e-8 * max(1.0, np.abs(g["p"]).max()))
+
+
+# the stated error bound of the reduced-precision (tensor-core) condensation
+# against the FP64 oracle, max-abs over y, z and p on the fixture's nodes
+REDUCED_BOUND = 1e-8
+
+
+@pytest.mark.parametrize("K,prec", [(16, "tf32"), (16, "bf16"), (32, "tf32"), (32, "bf16")])
+def test_pendulum_chain_reduced_precision_error_against_oracle(cs, K, prec):
+    """Configs 2 and 4 at their stated sizes with the TF32 / BF16 tensor-core
+    condensation (inexact Newton with the FP64 residual, line search and mesh
+    error): the solve reaches the tolerance on the oracle's final mesh and
+    its states, costates, controls and parameters are within REDUCED_BOUND
+    (max-abs) of the FP64 oracle's."""
+    g = golden("large_pend%d" % K)
+    pr, cp, bt = _stated_size(cs, K, prec)
+    bt.solve(cs.default_opts(pr))
+    s = bt.solution()[0]
+    assert s["success"] and bool(g["success"])
+    assert s["N"] == int(g["N"])
+    np.testing.assert_array_equal(s["t"], g["t"])
+    assert s["last_norm"] < float(g["tol"]) and s["max_residual"] <= 1.0
+    err = max(np.abs(_rows(s["y"], g) - g["y"]).max(), np.abs(_rows(s["z"], g) - g["z"]).max(),
+              np.abs(s["p"] - g["p"]).max())
+    print("K=%d %s: max-abs error against the FP64 oracle %.3g (Newton %d, oracle %d)"
+          % (K, prec, err, s["newton_steps"], int(g["jacobian_counts"])))
+    assert err < REDUCED_BOUND

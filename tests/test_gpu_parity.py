@@ -19,7 +19,8 @@ pytestmark = pytest.mark.gpu
 STAGES = [("vdp_n21_m4", "vdp"), ("vdp_n33_m5", "vdp"), ("dint_n33_m3", "dint_param"),
           ("pend2_n21_m5", "pend2"), ("econ_n17_m3", "eqcon")]
 E2E = [("vdp_cfg1", "vdp"), ("vdp_coarse", "vdp_coarse"), ("dint_param", "dint_param"), ("vdp_input", "vdp_input"),
-       ("pend2", "pend2"), ("vdp_ineq", "vdp_ineq"), ("vdp_svineq", "vdp_svineq"), ("vdp_m7", "vdp")]
+       ("pend2", "pend2"), ("vdp_ineq", "vdp_ineq"), ("vdp_svineq", "vdp_svineq"), ("vdp_m7", "vdp"),
+       ("eqcon", "eqcon")]
 
 
 @pytest.fixture(scope="module")
@@ -169,6 +170,33 @@ def test_batch_equals_independent_solves(cs):
         assert s["N"] == ref.N and s["newton_steps"] == ref.jacobian_count and s["residual_evals"] == ref.residual_count
         assert np.abs(s["y"] - ref.y).max() < 1e-8
         assert np.abs(s["z"] - ref.z).max() < 1e-8
+
+
+def test_plain_batch_sample_matches_oracle(cs):
+    """32 random instances of the batched plain-method workload (4096 Van der
+    Pol instances, seed 1: x0, T, r per instance, N ~ U{32..2048} intervals,
+    m in {3, 4, 5}), solved in one batch per m from the plain guess, against
+    the oracle on each instance alone: same outcome, Newton and residual
+    counts, remeshes and final mesh (bit for bit), y, z, p within 1e-8 of
+    their scale."""
+    from oracle_pool import solve_many
+    insts = cs.workloads.vdp_batch(4096, seed=1)
+    rng = np.random.default_rng(3)
+    pick = [insts[int(k)] for k in sorted(rng.choice(len(insts), 32, replace=False))]
+    assert {i.m for i in pick} == {3, 4, 5}
+    solver = cs.warmstart.BatchSolver(cs.warmstart.vdp_family())
+    sols = solver.solve(pick)
+    refs = solve_many([(i.m, i.theta) + tuple(i.guess()) for i in pick])
+    assert sum(r["success"] for r in refs) >= 28
+    for k, (s, ref) in enumerate(zip(sols, refs)):
+        label = "instance %d (m %d, %d intervals)" % (k, pick[k].m, pick[k].intervals)
+        assert s["success"] == ref["success"], label
+        assert (s["newton_steps"], s["residual_evals"], s["N"], s["remeshes"]) == \
+               (ref["newton_steps"], ref["residual_evals"], ref["N"], ref["remeshes"]), label
+        np.testing.assert_array_equal(s["t"], ref["t"], err_msg=label)
+        for key in ("y", "z", "p"):
+            sc = max(1.0, np.abs(ref[key]).max(initial=0.0))
+            np.testing.assert_allclose(s[key], ref[key], rtol=0, atol=1e-8 * sc, err_msg=label + " " + key)
 
 
 def test_failing_instances_match_oracle(cs):

@@ -9,18 +9,28 @@ from conftest import pkg
 pytestmark = pytest.mark.gpu
 
 
-def test_warm_start_gains_over_plain_guess():
+@pytest.fixture(scope="module")
+def vdp_net():
+    """A network trained on 1,536 solutions of the batched solver (Van der Pol
+    family, meshes of 32..160 intervals), shared by the tests below."""
     cs = pkg()
     ws = cs.warmstart
     fam = ws.vdp_family()
     solver = ws.BatchSolver(fam)
     train = cs.workloads.vdp_batch(1536, seed=1000, n_range=(32, 160))
-    held = cs.workloads.vdp_batch(256, seed=7, n_range=(32, 160))
     X, Y, _ = ws.training_set(fam, solver, train)
-    assert len(X) > 1200
     net = ws.Mlp(X.shape[1], Y.shape[1], width=256, depth=4, seed=0)
     net.fit_normalization(X, Y)
     net.train(X, Y, epochs=300, batch=256, lr=1e-3, seed=0)
+    return fam, solver, net, len(X)
+
+
+def test_warm_start_gains_over_plain_guess(vdp_net):
+    cs = pkg()
+    ws = cs.warmstart
+    fam, solver, net, n_train = vdp_net
+    held = cs.workloads.vdp_batch(256, seed=7, n_range=(32, 160))
+    assert n_train > 1200
     plain = solver.solve(held)
     final, fb, warm = ws.solve_warm(fam, solver, net, held)
     plain_ok = [s["success"] for s in plain]
@@ -171,3 +181,79 @@ def test_speculative_fallback_gives_the_sequential_results():
                    (b["success"], b.get("fallback", False), b["newton_steps"], b["residual_evals"], b["N"])
             np.testing.assert_array_equal(a["y"], b["y"])
             np.testing.assert_array_equal(a["t"], b["t"])
+
+
+def _held_out_sample(cs, per_m, seed):
+    """`per_m` random instances of each m from the benchmark's held-out batch
+    (8192 Van der Pol instances, seed 7, N ~ U{32..2048} intervals)."""
+    held = cs.workloads.vdp_batch(8192, seed=7)
+    rng = np.random.default_rng(seed)
+    pick = []
+    for m in (3, 4, 5):
+        idx = [k for k, inst in enumerate(held) if inst.m == m]
+        pick += sorted(int(k) for k in rng.choice(idx, per_m, replace=False))
+    return [held[k] for k in pick]
+
+
+def _split(st, k0, N):
+    """Instance rows of a packed state: (t, y, z) of the node slots."""
+    o = int(np.sum(N[:k0]))
+    n = int(N[k0])
+    return st["t"][o:o + n].copy(), st["y"][o:o + n].copy(), st["z"][o:o + n].copy()
+
+
+def _assert_same_solve(s, ref, label):
+    assert s["success"] == ref["success"], label
+    assert (s["newton_steps"], s["residual_evals"], s["N"], s["remeshes"]) == \
+           (ref["newton_steps"], ref["residual_evals"], ref["N"], ref["remeshes"]), label
+    np.testing.assert_array_equal(s["t"], ref["t"], err_msg=label)
+    for k in ("y", "z", "p"):
+        sc = max(1.0, np.abs(ref[k]).max(initial=0.0))
+        np.testing.assert_allclose(s[k], ref[k], rtol=0, atol=1e-8 * sc, err_msg="%s %s" % (label, k))
+
+
+def test_warm_started_bench_instances_match_oracle_from_the_same_guess(vdp_net):
+    """48 instances of the benchmark's own held-out batch (16 per m, meshes up
+    to 2048 intervals), warm-started as the benchmark does (device MLP,
+    device fill), against the oracle solving each from the same device-filled
+    guess: same outcome, Newton and residual counts, remeshes and final mesh
+    (bit for bit), y, z, p within 1e-8 of their scale.  Separately, where the
+    warm-started solve ends on the mesh of the oracle's solve from the plain
+    guess, the two solutions agree within the accuracy the tolerance gives
+    (both residuals below 1e-6): 1e-6 of the scale."""
+    from oracle_pool import solve_many
+    cs = pkg()
+    ws = cs.warmstart
+    fam, solver, net, _ = vdp_net
+    insts = _held_out_sample(cs, 16, seed=0)
+    runner = ws.WarmRunner(fam, solver, net, insts)
+    net.predict_device(runner.dX, len(runner.instances), runner.dY)
+    items, sols = [], []
+    for g in runner.groups:
+        bt = g["bt"]
+        bt.reset()
+        bt.warm_start(runner.dY.ptr + 4 * g["first"] * net.n_out, ws.N_NODES, net.n_out)
+        st = bt.state()
+        for b in range(g["n"]):
+            inst = runner.instances[g["first"] + b]
+            t, y, z = _split(st, b, st["N"])
+            items.append((inst.m, inst.theta, t, y, z, st["p"][b].copy()))
+        bt.solve(solver.opts)
+        sols += bt.solution()
+    plain_items = [(i.m, i.theta) + tuple(i.guess()) for i in runner.instances]
+    refs = solve_many(items + plain_items)
+    warm_ref, plain_ref = refs[:len(items)], refs[len(items):]
+    assert sum(s["success"] for s in sols) >= 40
+    assert max(s["N"] for s in sols) > 1500
+    same_mesh, worst = 0, 0.0
+    for k, (s, ref, pref) in enumerate(zip(sols, warm_ref, plain_ref)):
+        _assert_same_solve(s, ref, "instance %d (m %d)" % (k, runner.instances[k].m))
+        if s["success"] and pref["success"] and s["N"] == pref["N"] and np.array_equal(s["t"], pref["t"]):
+            same_mesh += 1
+            for key in ("y", "z", "p"):
+                sc = max(1.0, np.abs(pref[key]).max(initial=0.0))
+                d = np.abs(s[key] - pref[key]).max(initial=0.0) / sc
+                worst = max(worst, d)
+    print("warm vs plain-guess oracle: %d of %d on the same final mesh, max difference %.3g of scale"
+          % (same_mesh, len(sols), worst))
+    assert worst <= 1e-6

@@ -172,3 +172,23 @@ def test_oracle_end_to_end_with_residual2_matches_reference():
     np.testing.assert_array_equal(np.round(np.array(r.norms), 8), g["norms"])
     np.testing.assert_array_equal(r.t, g["t"])
     np.testing.assert_allclose(r.y, g["y"], atol=1e-8, rtol=0)
+
+
+@pytest.mark.parametrize("case,prob", STAGES[:3])
+def test_oracle_chunked_newton_step_is_the_same(case, prob):
+    """The memory-bounded Newton step (Jacobian, condensation and recovery
+    over ranges of intervals, used for the large fixtures) gives the same
+    numbers as the one-pass step, and both the reference's direction."""
+    cs = pkg()
+    g = golden("stage_" + case)
+    P = oracle_problem(prob)
+    m, N = int(g["m"]), int(g["N"])
+    rk = cs.tables.lobatto(m)
+    t, y, yd, zt, p, alpha = g["t"], g["y"], g["y_dot"], g["z_tilde"], g["p"], float(g["alpha"])
+    f_q, y_tilde, f_a, f_b, r_bc = O.compute_f_q(P, m, N, rk, t, y, yd, zt, p, alpha)
+    full = O.newton_step(P, m, N, rk, t, y, yd, zt, p, alpha, f_a, f_b, r_bc, y_tilde)
+    for chunk in (1, 3, 7):
+        part = O.newton_step(P, m, N, rk, t, y, yd, zt, p, alpha, f_a, f_b, r_bc, y_tilde, chunk=chunk)
+        for a, b in zip(full, part):
+            np.testing.assert_array_equal(a, b)
+    np.testing.assert_allclose(full[0], g["delta_y"], rtol=0, atol=1e-10 * max(1.0, np.abs(g["delta_y"]).max()))
