@@ -110,6 +110,8 @@ SIGNATURES = {
     "cs_device_alloc": (ctypes.c_void_p, [ctypes.c_size_t]),
     "cs_device_free": (None, [ctypes.c_void_p]),
     "cs_copy": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int]),
+    "cs_tc_update": (ctypes.c_int, [ctypes.c_int] * 4 + [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_int,
+                                                          ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]),
     "cs_babd_solve_noalloc": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int] + [ctypes.c_void_p] * 10 +
                               [ctypes.POINTER(ctypes.c_int), ctypes.c_void_p]),
 }

@@ -49,8 +49,10 @@ def _stale(target, deps):
 
 def build_library(force=False, verbose=False):
     hdr = _kernels_header()
-    sources = [os.path.join(CSRC, "cs_runtime.cu"), os.path.join(CSRC, "cs_babd.cu"), os.path.join(CSRC, "cs_mlp.cu")]
-    deps = sources + [os.path.join(CSRC, "cs_kernels.cuh"), os.path.join(ROOT, "include", "cs_gb300.h"), hdr]
+    sources = [os.path.join(CSRC, "cs_runtime.cu"), os.path.join(CSRC, "cs_babd.cu"), os.path.join(CSRC, "cs_mlp.cu"),
+               os.path.join(CSRC, "cs_tc.cu")]
+    deps = sources + [os.path.join(CSRC, "cs_kernels.cuh"), os.path.join(CSRC, "cs_umma.cuh"),
+                      os.path.join(ROOT, "include", "cs_gb300.h"), hdr]
     if not force and not _stale(LIB, deps):
         return LIB
     cmd = [NVCC, "-O3", "-std=c++17", "-lineinfo", *ARCH, "-shared", "-Xcompiler", "-fPIC",

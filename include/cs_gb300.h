@@ -241,6 +241,20 @@ int cs_babd_solve_noalloc(int ny, int np, int n, const double* A, const double* 
                           const double* b, const double* B0, const double* Bn, const double* Vn, const double* r,
                           double* dy, double* dp, int* singular, void* stream);
 
+/* The tensor-core block update C -= A B^T on one matrix in DEVICE memory:
+ * C (M x N, FP32, row stride ldc), A (M x K, row stride lda) and B (N x K, row
+ * stride ldb) in FP32, rounded to TF32 (precision 1, round to nearest, ties
+ * away) or BF16 (precision 2, round to nearest even) on the tensor cores
+ * (tcgen05.mma, FP32 accumulation in tensor memory).  1 <= M <= 256,
+ * 1 <= N <= 512, 1 <= K <= 64; ordered on `stream` and returns after it has
+ * finished.  It is the trailing update of the reduced-precision blocked LU
+ * that condenses large stage systems (the LU of
+ * collocation_solver_parallel_2d_shared.py:887-1001 and
+ * matrix_factorization_cuda.py:91-165, there in FP64 without tensor cores),
+ * exposed on its own so that the update can be checked and used alone. */
+int cs_tc_update(int precision, int M, int N, int K, const float* A, int lda, const float* B, int ldb, float* C,
+                 int ldc, void* stream);
+
 /* Current iterate to host: t, y (nodes), ydot, z~ (slots), z at nodes, p. */
 int cs_get_state(cs_batch* bt, double* t, double* y, double* ydot, double* zt, double* z_nodes, double* p);
 
