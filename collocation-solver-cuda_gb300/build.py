@@ -21,13 +21,14 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
 def _kernels_header():
-    """cs_kernels.cuh as a C string constant (the NVRTC program text)."""
+    """cs_umma.cuh + cs_kernels.cuh as a C string constant (the NVRTC program
+    text after the problem-specific prelude)."""
     os.makedirs(BUILD, exist_ok=True)
-    src = open(os.path.join(CSRC, "cs_kernels.cuh")).read()
+    src = open(os.path.join(CSRC, "cs_umma.cuh")).read() + "\n" + open(os.path.join(CSRC, "cs_kernels.cuh")).read()
     out = os.path.join(BUILD, "cs_kernels_src.h")
     delim = "CSKSRC"
     assert (")" + delim + '"') not in src
-    text = "// generated from cs_kernels.cuh by build.py\n"
+    text = "// generated from cs_umma.cuh and cs_kernels.cuh by build.py\n"
     # split into chunks: some compilers limit the length of one string literal
     chunks = [src[i:i + 16000] for i in range(0, len(src), 16000)]
     text += "static const char cs_kernels_source[] =\n"

@@ -1570,8 +1570,9 @@ extern "C" __global__ void k_babd_cta(CsBatch bt, int recover) {}
 //                 shared memory.  Same operations in the same order as the
 //                 unblocked elimination of cs_condense_group (pivot rule,
 //                 multipliers, the fma chain of every entry), so both give
-//                 the same bits.  CS_PREC 1 / 2: FP32 storage, trailing
-//                 updates on the tensor cores (TF32 / BF16).
+//                 the same bits.  CS_PREC 1 / 2 (TF32 / BF16):
+//                 cs_condense_tc, FP32 storage and the block updates on
+//                 the tensor cores with tcgen05.
 //   k_tree_level  one CTA per merge, compact-WY Householder in panels of
 //                 CS_HB reflectors (CS_PREC_TREE: on the tensor cores).
 //   k_top         one CTA per instance.
@@ -1709,82 +1710,6 @@ __device__ __forceinline__ unsigned long long cs_abskey(float v) {
 __device__ __forceinline__ bool cs_tiny(double v) { return cs_abskey(v) < 0x3ce4000000000000ull; }
 __device__ __forceinline__ bool cs_tiny(float v) { return fabsf(v) < 2.220446049250313e-15f; }
 
-// A22 -= L21 U12 on the tensor cores for the mixed-precision condensation:
-// warp items of 16 rows x 32 columns (four m16n8 tiles), FP32 accumulators
-// initialised from A22, operands -L21 (panel) and U12 rounded to TF32
-// (PREC 1, m16n8k8, two k-steps per 16-column panel) or BF16 (PREC 2,
-// m16n8k16).  Fragment layouts (g = lane / 4, t = lane % 4):
-//   C  c0 (g, 2t)  c1 (g, 2t+1)  c2 (g+8, 2t)  c3 (g+8, 2t+1)
-//   TF32 A a0 (g, t) a1 (g+8, t) a2 (g, t+4) a3 (g+8, t+4); B b0 (t, g) b1 (t+4, g)
-//   BF16 A pairs (g, 2t..) (g+8, 2t..) (g, 2t+8..) (g+8, 2t+8..); B pairs (2t.., g) (2t+8.., g)
-template <int PREC>
-__device__ void cs_trailing_mma(float* W, const float* P, const float* U, int r0, int c0, int nr, int ncol, int kb) {
-  const int tid = threadIdx.x, nt = blockDim.x;
-  const int lane = tid & 31, w = tid >> 5, nw = nt >> 5;
-  const int g = lane >> 2, t = lane & 3;
-  const int rt = (nr + 15) >> 4, ct = (ncol + 31) >> 5;
-  for (int item = w; item < rt * ct; item += nw) {
-    const int ri = item / ct, ci = item - ri * ct;
-    const int ra = ri * 16, cb = ci * 32;
-    float acc[4][4];
-#pragma unroll
-    for (int j = 0; j < 4; ++j)
-#pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        const int row = ra + g + ((q & 2) ? 8 : 0), col = cb + 8 * j + 2 * t + (q & 1);
-        acc[j][q] = (row < nr && col < ncol) ? W[(size_t)(r0 + row) * CS_LDG + c0 + col] : 0.f;
-      }
-    auto A = [&](int row, int l) -> float {
-      return (row < nr && l < kb) ? -P[(kb + row) * CS_PLD + l] : 0.f;
-    };
-    auto B = [&](int l, int col) -> float { return (l < kb && col < ncol) ? U[l * CS_LDG + col] : 0.f; };
-    if constexpr (PREC == 1) {
-#pragma unroll
-      for (int ks = 0; ks < CS_NB; ks += 8) {
-        const unsigned a0 = cs_tf32(A(ra + g, ks + t)), a1 = cs_tf32(A(ra + g + 8, ks + t));
-        const unsigned a2 = cs_tf32(A(ra + g, ks + t + 4)), a3 = cs_tf32(A(ra + g + 8, ks + t + 4));
-#pragma unroll
-        for (int j = 0; j < 4; ++j) {
-          const unsigned b0 = cs_tf32(B(ks + t, cb + 8 * j + g)), b1 = cs_tf32(B(ks + t + 4, cb + 8 * j + g));
-          asm volatile("mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-                       "{%0,%1,%2,%3};\n"
-                       : "+f"(acc[j][0]), "+f"(acc[j][1]), "+f"(acc[j][2]), "+f"(acc[j][3])
-                       : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
-        }
-      }
-    } else {
-#pragma unroll
-      for (int ks = 0; ks < CS_NB; ks += 16) {
-        const unsigned a0 = cs_bf2(A(ra + g, ks + 2 * t), A(ra + g, ks + 2 * t + 1));
-        const unsigned a1 = cs_bf2(A(ra + g + 8, ks + 2 * t), A(ra + g + 8, ks + 2 * t + 1));
-        const unsigned a2 = cs_bf2(A(ra + g, ks + 2 * t + 8), A(ra + g, ks + 2 * t + 9));
-        const unsigned a3 = cs_bf2(A(ra + g + 8, ks + 2 * t + 8), A(ra + g + 8, ks + 2 * t + 9));
-#pragma unroll
-        for (int j = 0; j < 4; ++j) {
-          const int col = cb + 8 * j + g;
-          const unsigned b0 = cs_bf2(B(ks + 2 * t, col), B(ks + 2 * t + 1, col));
-          const unsigned b1 = cs_bf2(B(ks + 2 * t + 8, col), B(ks + 2 * t + 9, col));
-          asm volatile("mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-                       "{%0,%1,%2,%3};\n"
-                       : "+f"(acc[j][0]), "+f"(acc[j][1]), "+f"(acc[j][2]), "+f"(acc[j][3])
-                       : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
-        }
-      }
-    }
-#pragma unroll
-    for (int j = 0; j < 4; ++j)
-#pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        const int row = ra + g + ((q & 2) ? 8 : 0), col = cb + 8 * j + 2 * t + (q & 1);
-        if (row < nr && col < ncol) W[(size_t)(r0 + row) * CS_LDG + c0 + col] = acc[j][q];
-      }
-  }
-}
-
-// FP64 instantiations never call the tensor-core update
-template <int PREC>
-__device__ __forceinline__ void cs_trailing_mma(double*, const double*, const double*, int, int, int, int, int) {}
-
 template <typename T, int PREC>
 __device__ void cs_condense_big(const CsBatch& bt, int slot, double* slab, double* sm) {
   constexpr int RB = CS_RB;
@@ -1853,46 +1778,11 @@ __device__ void cs_condense_big(const CsBatch& bt, int slot, double* slab, doubl
     }
   }
   __syncthreads();
-  // ---- reduced precision: FP32 copies of the stage Jacobians and X0, once
-  //      (conversions run on the FP64 pipe: none inside the fill's sums)
-  float* JGf = reinterpret_cast<float*>(X0 + (size_t)RB * CS_NRHS);  // [M][RB][NFG]
-  float* X0f = JGf + (size_t)CS_M * RB * CS_NFG;                      // [RB][NRHS]
-  float* hAf = X0f + (size_t)RB * CS_NRHS;                             // [M][M]
-  float* Bf = hAf + CS_M * CS_M;                                       // [M]
-  if constexpr (PREC != 0) {
-    for (int e = tid; e < CS_M * RB * CS_NFG; e += nt) JGf[e] = (float)JG[e];
-    for (int e = tid; e < RB * CS_NRHS; e += nt) X0f[e] = (float)X0[e];
-    for (int e = tid; e < CS_M * CS_M; e += nt) hAf[e] = (float)hA[e];
-    for (int e = tid; e < CS_M; e += nt) Bf[e] = (float)(h * CS_B[e]);
-    __syncthreads();
-  }
   // ---- the reduced system [W11 | R1 - W10 X0] (stages 1..M-1) into the slab
   for (int e = tid; e < CS_S1 * CS_NCOL1; e += nt) {
     const int row = e / CS_NCOL1, col = e - row * CS_NCOL1;
     const int j = 1 + row / RB, a = row - (j - 1) * RB;
     const double* J = JG + (size_t)(j * RB + a) * CS_NFG;
-    if constexpr (PREC != 0) {
-      const float* Jf = JGf + (size_t)(j * RB + a) * CS_NFG;
-      float vf;
-      if (col < CS_S1) {
-        const int k = 1 + col / RB, q = col - (k - 1) * RB;
-        if (q < CS_NY) {
-          vf = hAf[j * CS_M + k] * Jf[q];
-          if (k == j && q == a) vf -= 1.f;
-        } else {
-          vf = (k == j) ? Jf[q] : 0.f;
-        }
-      } else {
-        // the right-hand side of an inexact stage solve: FP32 suffices
-        const int c = col - CS_S1;
-        float w = 0.f;
-        for (int q = 0; q < CS_NY; ++q) w = fmaf(Jf[q], X0f[q * CS_NRHS + c], w);
-        const float r = (c < CS_NY) ? Jf[c] : ((c < CS_NY + CS_NPE) ? Jf[CS_NY + CS_NZ + (c - CS_NY)] : (float)fa[j * RB + a]);
-        vf = fmaf(-hAf[j * CS_M], w, r);
-      }
-      W[(size_t)row * CS_LDG + col] = (T)vf;
-      continue;
-    }
     double v;
     if (col < CS_S1) {
       const int k = 1 + col / RB, q = col - (k - 1) * RB;
@@ -1988,9 +1878,7 @@ __device__ void cs_condense_big(const CsBatch& bt, int slot, double* slab, doubl
     // trailing update A22 -= L21 U12: warp items of 16 rows x 32 columns,
     // lane owns one column (fills the lanes for any trailing width)
     const int r0 = k0 + kb, nr = CS_S1 - r0;
-    if constexpr (PREC != 0) {
-      if (nr > 0 && ncol > 0) cs_trailing_mma<PREC>(W, P, U, r0, c0, nr, ncol, kb);
-    } else if (nr > 0 && ncol > 0) {
+    if (nr > 0 && ncol > 0) {
       const int rt = (nr + 15) >> 4, ct = (ncol + 31) >> 5;
       const int lane = tid & 31, w = tid >> 5, nw = nt >> 5;
       for (int item = w; item < rt * ct; item += nw) {
@@ -2060,16 +1948,9 @@ __device__ void cs_condense_big(const CsBatch& bt, int slot, double* slab, doubl
   double* row = bt.rows0 + (size_t)slot * CS_ROWSZ;
   for (int e = tid; e < CS_NRHS * CS_NY; e += nt) {
     const int c = e / CS_NY, a = e - c * CS_NY;
-    double dx;
-    if constexpr (PREC != 0) {
-      float sf = Bf[0] * X0f[a * CS_NRHS + c];
-      for (int j = 1; j < CS_M; ++j) sf = fmaf(Bf[j], (float)W[(size_t)((j - 1) * RB + a) * CS_LDG + CS_S1 + c], sf);
-      dx = (double)sf;
-    } else {
-      double s = CS_B[0] * X0[a * CS_NRHS + c];
-      for (int j = 1; j < CS_M; ++j) s += CS_B[j] * (double)W[(size_t)((j - 1) * RB + a) * CS_LDG + CS_S1 + c];
-      dx = h * s;
-    }
+    double s = CS_B[0] * X0[a * CS_NRHS + c];
+    for (int j = 1; j < CS_M; ++j) s += CS_B[j] * (double)W[(size_t)((j - 1) * RB + a) * CS_LDG + CS_S1 + c];
+    const double dx = h * s;
     if (c < CS_NY) {
       row[c * CS_NY + a] = (a == c) ? dx - 1.0 : dx;
       row[(CS_NY + c) * CS_NY + a] = (a == c ? 1.0 : 0.0);
@@ -2084,9 +1965,461 @@ __device__ void cs_condense_big(const CsBatch& bt, int slot, double* slab, doubl
   __syncthreads();
 }
 
+#if CS_PREC != 0
+// ------------------------------------------------------------------------
+// Reduced-precision condensation on the tensor cores (CS_PREC 1: TF32,
+// 2: BF16).  FP32 storage of the stage system in the slab (column-major: a
+// thread of the tensor-memory epilogue owns a row, so a warp's accesses to
+// one column are one line), FP32 panel factorisation (partial pivoting, the
+// pivot rule of the FP64 path), and the three block updates of width >= 16
+// on tcgen05 (cs_umma.cuh: operands in shared memory, FP32 accumulators in
+// tensor memory):
+//   fill        R1 - W10 X0: (hA[j][0] J_y rows) x X0_y, K = ny in chunks of 64
+//   LU          A22 -= L21 U12 after every panel of CS_NBT = 32 columns
+//   back subst. X_above -= U_above,block X_block for blocks of CS_NB = 16 rows
+// The stage Jacobians, the stage-0 block solve and the residual stay FP64;
+// the result is an inexact Newton Jacobian (the FP64 residual, line search
+// and mesh error drive the solve to the FP64 tolerance).
+#define CS_NBT 32
+#define CS_PLDT (CS_NBT + 1)
+#define CS_LDR (((CS_S1 + 3) / 4) * 4)                   // leading dimension of the column-major slab matrix
+#define CS_TCE ((CS_PREC == 1) ? 4 : 8)                 // FP32 values per 16-byte operand segment
+#define CS_TCKC (CS_NBT / CS_TCE)                        // LU update: core matrices along K (K = CS_NBT)
+#define CS_TCKB (CS_NB / CS_TCE)                         // back substitution (K = CS_NB)
+#define CS_TCKF (64 / CS_TCE)                            // fill (K chunks of 64)
+#define CS_TCMP ((CS_S1 > CS_NBT) ? ((CS_S1 - CS_NBT + 127) / 128) * 128 : 128)  // L21 operand rows
+#define CS_TCMB (((CS_S1 + 127) / 128) * 128)            // U_above operand rows
+#define CS_TCNR (((CS_NRHS + 15) / 16) * 16)             // right-hand-side operand rows
+#define CS_TCNB 256                                      // U12 operand rows (a chunk of columns, one per thread)
+#define CS_TC_R128(x) ((((x) + 127) / 128) * 128)
+#define CS_TC_OPS_LU ((CS_TCMP + CS_TCNB) * CS_TCKC * 16)
+#define CS_TC_OPS_BS ((CS_TCMB + CS_TCNR) * CS_TCKB * 16)
+#define CS_TC_OPS CS_TC_R128((CS_TC_OPS_LU > CS_TC_OPS_BS) ? CS_TC_OPS_LU : CS_TC_OPS_BS)
+#define CS_TC_PANEL CS_TC_R128(CS_S1 * CS_PLDT * 4)
+#define CS_TC_FILL ((128 + CS_TCNR) * CS_TCKF * 16)      // fill operands: operand area + panel
+#define CS_TC_DBL (8 * (CS_M * CS_RB + CS_M * CS_M + CS_NY + 16))
+#define CS_TC_MISC (CS_TC_OPS + CS_TC_PANEL + CS_TC_DBL + CS_TC_R128(4 * CS_S1 + 4 * CS_NBT))
+#define CS_TC_SMB (CS_TC_MISC + 16)                      // + mbarrier, TMEM address, error flag
+#define CS_TC_SMD ((CS_TC_SMB + 7) / 8)
+#define CS_TC_WAIT 2000000000ll                          // MMA completion bound (cycles, about 1 s)
+#define CS_JLD (CS_NFG | 1)                              // row stride of the fill's staged Jacobian rows
+static_assert(CS_TC_FILL <= CS_TC_OPS + CS_TC_PANEL, "fill operands exceed the operand area and panel");
+static_assert(32 * CS_JLD * 4 <= CS_TC_PANEL, "the fill's staged Jacobian rows exceed the panel");
+static_assert((long long)CS_NCOL1 * CS_LDR <= 2ll * CS_S1 * CS_LDG, "column-major matrix exceeds the slab's matrix area");
+static_assert(CS_NBT % CS_TCE == 0 && CS_NB % CS_TCE == 0 && 64 % CS_TCE == 0, "operand K widths");
+
+// FP64 -> FP32 copy of n values, eight loads in flight per thread before
+// their stores (source and destination share the slab, so the compiler would
+// otherwise wait for each store before the next load)
+__device__ __forceinline__ void cs_copy_f32(const double* __restrict__ src, float* __restrict__ dst, int n) {
+  const int tid = threadIdx.x, nt = blockDim.x;
+  int e = tid;
+  for (; e + 7 * nt < n; e += 8 * nt) {
+    double v[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) v[u] = src[e + u * nt];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) dst[e + u * nt] = (float)v[u];
+  }
+  for (; e < n; e += nt) dst[e] = (float)src[e];
+}
+
+// shared memory (bytes): operands [CS_TC_OPS] | panel P [S1][PLDT] floats |
+// fa [M RB], hA [M M], fb [NY], red [16] doubles | inv [S1] floats, piv [NBT] |
+// mbarrier, TMEM address, error flag.  Returns false after a tensor-core
+// timeout (every thread; the operands and accumulator are then abandoned).
+template <int PREC>
+__device__ bool cs_condense_tc(const CsBatch& bt, int slot, double* slab, unsigned char* sm, unsigned tmem,
+                               unsigned mbar, unsigned& phase, int* flag) {
+  constexpr int RB = CS_RB;
+  constexpr int EPS = CS_TCE;
+  const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, w = tid >> 5, nw = nt >> 5;
+  float* W = reinterpret_cast<float*>(slab);                       // column-major [NCOL1][LDR]
+  double* JG = slab + (size_t)CS_S1 * CS_LDG;                      // [M][RB][NFG]
+  double* X0 = JG + (size_t)CS_M * RB * CS_NFG;                    // [RB][NRHS]
+  float* JGf = reinterpret_cast<float*>(X0 + (size_t)RB * CS_NRHS);  // FP32 copies
+  float* X0f = JGf + (size_t)CS_M * RB * CS_NFG;
+  float* hAf = X0f + (size_t)RB * CS_NRHS;
+  float* Bf = hAf + CS_M * CS_M;
+  unsigned char* ops = sm;
+  float* P = reinterpret_cast<float*>(sm + CS_TC_OPS);
+  double* fa = reinterpret_cast<double*>(sm + CS_TC_OPS + CS_TC_PANEL);
+  double* hA = fa + CS_M * RB;
+  double* fb = hA + CS_M * CS_M;
+  double* red = fb + CS_NY;
+  float* inv = reinterpret_cast<float*>(red + 16);
+  int* piv = reinterpret_cast<int*>(inv + CS_S1);
+  const int b = bt.inst_of[slot];
+  const double h = bt.t[slot + 1] - bt.t[slot];
+  const double* yi = bt.y + (size_t)slot * CS_NY;
+  const double* yd = bt.ydot + (size_t)slot * CS_M * CS_NY;
+  // ---- stage functions and Jacobians (FP64), thread j for stage j
+  for (int j = tid; j < CS_M; j += nt) cs_stage_big(bt, slot, b, j, h, JG, fa);
+  for (int e = tid; e < CS_M * CS_M; e += nt) hA[e] = h * CS_A[e];
+  for (int k = tid; k < CS_NY; k += nt) {
+    double s = 0.0;
+    for (int j = 0; j < CS_M; ++j) s += CS_B[j] * yd[j * CS_NY + k];
+    fb[k] = yi[CS_NY + k] - yi[k] - h * s;
+  }
+  __syncthreads();
+  // ---- stage 0: [-I h_z0; 0 g_z0] X0 = R0 (FP64), one thread per right-hand side
+  for (int c = tid; c < CS_NRHS; c += nt) {
+    const double* J0 = JG;
+#if CS_NZ > 0
+    double gz[CS_NZ][CS_NZ], xz[CS_NZ];
+    for (int a = 0; a < CS_NZ; ++a) {
+      for (int q = 0; q < CS_NZ; ++q) gz[a][q] = J0[(CS_NY + a) * CS_NFG + CS_NY + q];
+      xz[a] = cs_rhs(J0 + (CS_NY + a) * CS_NFG, fa, 0, CS_NY + a, c);
+    }
+    for (int kk = 0; kk < CS_NZ; ++kk) {
+      int pr = kk;
+      for (int r = kk + 1; r < CS_NZ; ++r)
+        if (cs_abskey(gz[r][kk]) > cs_abskey(gz[pr][kk])) pr = r;
+      if (pr != kk) {
+        for (int q = 0; q < CS_NZ; ++q) { const double t = gz[kk][q]; gz[kk][q] = gz[pr][q]; gz[pr][q] = t; }
+        const double t = xz[kk]; xz[kk] = xz[pr]; xz[pr] = t;
+      }
+      const double ip = 1.0 / gz[kk][kk];
+      for (int r = kk + 1; r < CS_NZ; ++r) {
+        const double l = gz[r][kk] * ip;
+        for (int q = kk + 1; q < CS_NZ; ++q) gz[r][q] = fma(-l, gz[kk][q], gz[r][q]);
+        xz[r] = fma(-l, xz[kk], xz[r]);
+      }
+    }
+    for (int r = CS_NZ - 1; r >= 0; --r) {
+      double v = xz[r];
+      for (int q = r + 1; q < CS_NZ; ++q) v = fma(-gz[r][q], xz[q], v);
+      xz[r] = v / gz[r][r];
+    }
+    for (int a = 0; a < CS_NZ; ++a) X0[(CS_NY + a) * CS_NRHS + c] = xz[a];
+#endif
+    for (int a = 0; a < CS_NY; ++a) {
+      double v = -cs_rhs(J0 + a * CS_NFG, fa, 0, a, c);
+#if CS_NZ > 0
+      for (int q = 0; q < CS_NZ; ++q) v = fma(J0[a * CS_NFG + CS_NY + q], xz[q], v);
+#endif
+      X0[a * CS_NRHS + c] = v;
+    }
+  }
+  __syncthreads();
+  // ---- FP32 copies of the stage Jacobians and X0, once
+  cs_copy_f32(JG, JGf, CS_M * RB * CS_NFG);
+  cs_copy_f32(X0, X0f, RB * CS_NRHS);
+  for (int e = tid; e < CS_M * CS_M; e += nt) hAf[e] = (float)hA[e];
+  for (int e = tid; e < CS_M; e += nt) Bf[e] = (float)(h * CS_B[e]);
+  __syncthreads();
+  // ---- the reduced system [W11 | R1] (stages 1..M-1), 32 rows at a time:
+  //      their Jacobian rows staged in shared memory (the panel's space),
+  //      then a warp per column, a lane per row (column-major stores are
+  //      one line per warp)
+  for (int rb0 = 0; rb0 < CS_S1; rb0 += 32) {
+    const int nrow = min(32, CS_S1 - rb0);
+    for (int r = w; r < nrow; r += nw) {
+      const int row = rb0 + r;
+      const int j = 1 + row / RB, a = row - (j - 1) * RB;
+      const float* Jf = JGf + (size_t)(j * RB + a) * CS_NFG;
+      for (int q = lane; q < CS_NFG; q += 32) P[r * CS_JLD + q] = Jf[q];
+    }
+    __syncthreads();
+    const int row = rb0 + lane;
+    const bool rok = lane < nrow;
+    const int j = rok ? 1 + row / RB : 1, a = rok ? row - (j - 1) * RB : 0;
+    const float* Js = P + lane * CS_JLD;
+    for (int col = w; col < CS_NCOL1; col += nw) {
+      float v;
+      if (col < CS_S1) {
+        const int k = 1 + col / RB, q = col - (k - 1) * RB;
+        if (q < CS_NY) {
+          v = hAf[j * CS_M + k] * Js[q];
+          if (k == j && q == a) v -= 1.f;
+        } else {
+          v = (k == j) ? Js[q] : 0.f;
+        }
+      } else {
+        const int c = col - CS_S1;
+        v = (c < CS_NY) ? Js[c] : ((c < CS_NY + CS_NPE) ? Js[CS_NY + CS_NZ + (c - CS_NY)] : (float)fa[j * RB + a]);
+      }
+      if (rok) W[(size_t)col * CS_LDR + row] = v;
+    }
+    __syncthreads();
+  }
+  // ---- R1 -= W10 X0 on the tensor cores: A rows hA[j][0] J_y(j, a), B rows the
+  //      right-hand sides of X0's y part, K = ny in chunks of 64
+  {
+    unsigned char* FA = ops;
+    unsigned char* FB = ops + 128 * CS_TCKF * 16;
+    for (int k0 = 0; k0 < CS_NY; k0 += 64) {
+      const int kw = min(64, CS_NY - k0);
+      __syncthreads();  // R1 written; earlier MMAs done with the operand area
+      for (int e = tid; e < CS_TCNR * CS_TCKF; e += nt) {
+        const int c = e / CS_TCKF, sg = e - c * CS_TCKF;
+        float x[EPS];
+#pragma unroll
+        for (int ee = 0; ee < EPS; ++ee) {
+          const int q = sg * EPS + ee;
+          x[ee] = (c < CS_NRHS && q < kw) ? X0f[(size_t)(k0 + q) * CS_NRHS + c] : 0.f;
+        }
+        cs_tc_put<PREC>(FB, c, sg, CS_TCKF, x);
+      }
+      for (int t0 = 0; t0 < CS_S1; t0 += 128) {
+        const int mr = min(128, CS_S1 - t0);
+        for (int e = tid; e < 128 * CS_TCKF; e += nt) {
+          const int r = e / CS_TCKF, sg = e - r * CS_TCKF;
+          float x[EPS];
+          if (r < mr) {
+            const int row = t0 + r;
+            const int j = 1 + row / RB, a = row - (j - 1) * RB;
+            const float* Jf = JGf + (size_t)(j * RB + a) * CS_NFG + k0;
+            const float s0 = hAf[j * CS_M];
+#pragma unroll
+            for (int ee = 0; ee < EPS; ++ee) {
+              const int q = sg * EPS + ee;
+              x[ee] = (q < kw) ? s0 * Jf[q] : 0.f;
+            }
+          } else {
+#pragma unroll
+            for (int ee = 0; ee < EPS; ++ee) x[ee] = 0.f;
+          }
+          cs_tc_put<PREC>(FA, r, sg, CS_TCKF, x);
+        }
+        cs_fence_async_smem();
+        __syncthreads();
+        if (!cs_tc_block_update<PREC>(W + (size_t)CS_S1 * CS_LDR + t0, 1, CS_LDR, mr, CS_NRHS, FA, FB, CS_TCKF,
+                                      CS_TCKF / 2, tmem, mbar, phase, CS_TC_WAIT, flag))
+          return false;
+      }
+    }
+  }
+  __syncthreads();
+  // ---- blocked LU with partial pivoting, panels of CS_NBT columns
+  int singular = 0;
+  unsigned char* A_s = ops;
+  unsigned char* B_s = ops + CS_TCMP * CS_TCKC * 16;
+#pragma unroll 1
+  for (int k0 = 0; k0 < CS_S1; k0 += CS_NBT) {
+    const int kb = min(CS_NBT, CS_S1 - k0);
+    const int pr = CS_S1 - k0;  // panel rows
+    for (int c = w; c < kb; c += nw)
+      for (int r = lane; r < pr; r += 32) P[r * CS_PLDT + c] = W[(size_t)(k0 + c) * CS_LDR + k0 + r];
+    __syncthreads();
+#pragma unroll 1
+    for (int kk = 0; kk < kb; ++kk) {
+      unsigned long long best = 0ull;
+      int brow = CS_S1;  // larger than any row: loses every tie
+      for (int r = kk + tid; r < pr; r += nt) {
+        const unsigned long long v = cs_abskey(P[r * CS_PLDT + kk]);
+        if (v > best || brow == CS_S1) { best = v; brow = r; }
+      }
+      cs_cta_argmax(best, brow, red);
+      if (tid == 0) piv[kk] = brow;
+      if (brow != kk)
+        for (int c = tid; c < kb; c += nt) {
+          const float tmp = P[kk * CS_PLDT + c];
+          P[kk * CS_PLDT + c] = P[brow * CS_PLDT + c];
+          P[brow * CS_PLDT + c] = tmp;
+        }
+      __syncthreads();
+      const float pv = P[kk * CS_PLDT + kk];
+      const bool tiny = cs_tiny(pv);
+      singular |= tiny;
+      const float ip = 1.f / pv;
+      if (tid == 0) inv[k0 + kk] = ip;
+      const float mul = tiny ? 0.f : ip;
+      // multipliers and the rank-1 update of the panel, a thread per row
+      for (int r = kk + 1 + tid; r < pr; r += nt) {
+        float* Pr = P + r * CS_PLDT;
+        const float l = Pr[kk] * mul;
+        Pr[kk] = l;
+        for (int c = kk + 1; c < kb; ++c) Pr[c] = fmaf(-l, P[kk * CS_PLDT + c], Pr[c]);
+      }
+      __syncthreads();
+    }
+    // U11 (and L11) rows back to the slab
+    for (int c = w; c < kb; c += nw)
+      for (int r = lane; r < kb; r += 32) W[(size_t)(k0 + c) * CS_LDR + k0 + r] = P[r * CS_PLDT + c];
+    const int c0 = k0 + kb, ncol = CS_NCOL1 - c0, r0 = k0 + kb, nr = CS_S1 - r0;
+    // A operand: L21, rows padded with zeros to a multiple of 128, K to CS_NBT
+    if (nr > 0)
+      for (int e = tid; e < ((nr + 127) & ~127) * CS_TCKC; e += nt) {
+        const int r = e / CS_TCKC, sg = e - r * CS_TCKC;
+        float x[EPS];
+#pragma unroll
+        for (int ee = 0; ee < EPS; ++ee) {
+          const int c = sg * EPS + ee;
+          x[ee] = (r < nr && c < kb) ? P[(kb + r) * CS_PLDT + c] : 0.f;
+        }
+        cs_tc_put<PREC>(A_s, r, sg, CS_TCKC, x);
+      }
+    // columns right of the panel, a column per thread at a time: the row
+    // swaps in order, U12 = L11^-1 A12 in registers, U12 into the slab and
+    // into the B operand, then A22 -= L21 U12 on the tensor cores
+    for (int n0 = 0; n0 < ncol; n0 += nt) {
+      const int nch = min(nt, ncol - n0);  // nt <= CS_TCNB (cs_big_ok)
+      if (tid < nch) {
+        float* colp = W + (size_t)(c0 + n0 + tid) * CS_LDR;
+        for (int kk = 0; kk < kb; ++kk) {
+          const int p2 = piv[kk];
+          if (p2 != kk) {
+            const float t0 = colp[k0 + kk];
+            colp[k0 + kk] = colp[k0 + p2];
+            colp[k0 + p2] = t0;
+          }
+        }
+        float u[CS_NBT];
+#pragma unroll
+        for (int i = 0; i < CS_NBT; ++i) u[i] = (i < kb) ? colp[k0 + i] : 0.f;
+#pragma unroll
+        for (int i = 1; i < CS_NBT; ++i) {
+          if (i < kb) {
+            float v = u[i];
+#pragma unroll
+            for (int l = 0; l < i; ++l) v = fmaf(-P[i * CS_PLDT + l], u[l], v);
+            u[i] = v;
+          }
+        }
+#pragma unroll
+        for (int i = 0; i < CS_NBT; ++i)
+          if (i < kb) colp[k0 + i] = u[i];
+        if (nr > 0) {
+#pragma unroll
+          for (int sg = 0; sg < CS_TCKC; ++sg) cs_tc_put<PREC>(B_s, tid, sg, CS_TCKC, u + sg * EPS);
+        }
+      } else if (nr > 0 && tid < ((nch + 15) & ~15)) {
+        float z[EPS];
+#pragma unroll
+        for (int ee = 0; ee < EPS; ++ee) z[ee] = 0.f;
+#pragma unroll
+        for (int sg = 0; sg < CS_TCKC; ++sg) cs_tc_put<PREC>(B_s, tid, sg, CS_TCKC, z);
+      }
+      if (nr > 0) {
+        cs_fence_async_smem();
+        __syncthreads();
+        if (!cs_tc_block_update<PREC>(W + (size_t)(c0 + n0) * CS_LDR + r0, 1, CS_LDR, nr, nch, A_s, B_s, CS_TCKC,
+                                      CS_TCKC / 2, tmem, mbar, phase, CS_TC_WAIT, flag))
+          return false;
+      }
+    }
+    __syncthreads();
+  }
+  // ---- back substitution, blocks of CS_NB rows from the bottom: the block's
+  //      triangular solve by one thread per right-hand side, then the rows
+  //      above on the tensor cores
+#pragma unroll 1
+  for (int k0 = ((CS_S1 - 1) / CS_NB) * CS_NB; k0 >= 0; k0 -= CS_NB) {
+    const int kb = min(CS_NB, CS_S1 - k0);
+    // U column block [0, k0+kb) x [k0, k0+kb) into the panel buffer
+    for (int c = w; c < kb; c += nw)
+      for (int r = lane; r < k0 + kb; r += 32) P[r * CS_PLDT + c] = W[(size_t)(k0 + c) * CS_LDR + r];
+    __syncthreads();
+    unsigned char* UA = ops;
+    unsigned char* XB = ops + CS_TCMB * CS_TCKB * 16;
+    for (int c = tid; c < CS_TCNR; c += nt) {
+      float x[CS_NB];
+#pragma unroll
+      for (int i = 0; i < CS_NB; ++i) x[i] = 0.f;
+      if (c < CS_NRHS) {
+        float* colp = W + (size_t)(CS_S1 + c) * CS_LDR;
+#pragma unroll
+        for (int i = 0; i < CS_NB; ++i)
+          if (i < kb) x[i] = colp[k0 + i];
+#pragma unroll
+        for (int i = CS_NB - 1; i >= 0; --i) {
+          if (i < kb) {
+            const float xi = x[i] * inv[k0 + i];
+            x[i] = xi;
+#pragma unroll
+            for (int q = 0; q < i; ++q) x[q] = fmaf(-P[(k0 + q) * CS_PLDT + i], xi, x[q]);
+          }
+        }
+#pragma unroll
+        for (int i = 0; i < CS_NB; ++i)
+          if (i < kb) colp[k0 + i] = x[i];
+      }
+      if (k0 > 0) {
+#pragma unroll
+        for (int sg = 0; sg < CS_TCKB; ++sg) cs_tc_put<PREC>(XB, c, sg, CS_TCKB, x + sg * EPS);
+      }
+    }
+    if (k0 > 0) {
+      for (int e = tid; e < ((k0 + 127) & ~127) * CS_TCKB; e += nt) {
+        const int r = e / CS_TCKB, sg = e - r * CS_TCKB;
+        float x[EPS];
+#pragma unroll
+        for (int ee = 0; ee < EPS; ++ee) {
+          const int c = sg * EPS + ee;
+          x[ee] = (r < k0 && c < kb) ? P[r * CS_PLDT + c] : 0.f;
+        }
+        cs_tc_put<PREC>(UA, r, sg, CS_TCKB, x);
+      }
+      cs_fence_async_smem();
+      __syncthreads();
+      if (!cs_tc_block_update<PREC>(W + (size_t)CS_S1 * CS_LDR, 1, CS_LDR, k0, CS_NRHS, UA, XB, CS_TCKB, CS_TCKB / 2,
+                                    tmem, mbar, phase, CS_TC_WAIT, flag))
+        return false;
+    }
+    __syncthreads();
+  }
+  // ---- X (column-major [NRHS][S]: stage-0 rows from X0, the others from W)
+  double* X = bt.X + (size_t)slot * CS_NRHS * CS_S;
+  for (int c = w; c < CS_NRHS; c += nw) {
+    // a column's loads before its stores (X is another array: no aliasing,
+    // which the compiler cannot see)
+    constexpr int NQ = (CS_S + 31) / 32;
+    double xv[NQ];
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) {
+      const int r = lane + 32 * q;
+      xv[q] = (r >= CS_S) ? 0.0 : ((r < RB) ? X0[r * CS_NRHS + c] : (double)W[(size_t)(CS_S1 + c) * CS_LDR + (r - RB)]);
+    }
+#pragma unroll
+    for (int q = 0; q < NQ; ++q)
+      if (lane + 32 * q < CS_S) X[(size_t)c * CS_S + lane + 32 * q] = xv[q];
+  }
+  // ---- condensed block row: D X = h sum_j b_j X[(j, a)]
+  double* row = bt.rows0 + (size_t)slot * CS_ROWSZ;
+  for (int c = w; c < CS_NRHS; c += nw)
+    for (int a = lane; a < CS_NY; a += 32) {
+      float sf = Bf[0] * X0f[a * CS_NRHS + c];
+      for (int j = 1; j < CS_M; ++j) sf = fmaf(Bf[j], W[(size_t)(CS_S1 + c) * CS_LDR + (j - 1) * RB + a], sf);
+      const double dx = (double)sf;
+      if (c < CS_NY) {
+        row[c * CS_NY + a] = (a == c) ? dx - 1.0 : dx;
+        row[(CS_NY + c) * CS_NY + a] = (a == c ? 1.0 : 0.0);
+      } else if (c < CS_NY + CS_NPE) {
+        row[(2 * CS_NY + (c - CS_NY)) * CS_NY + a] = dx;
+      } else {
+        row[(2 * CS_NY + CS_NPE) * CS_NY + a] = -fb[a] - dx;
+      }
+    }
+  singular = __syncthreads_or(singular);
+  if (singular && tid == 0) atomicAdd(&bt.inst[b].singular, 1);
+  __syncthreads();
+  return true;
+}
+#endif  // CS_PREC != 0
+
 extern "C" __global__ void __launch_bounds__(256, 2) k_condense(CsBatch bt) {
-  extern __shared__ double smem[];
+  extern __shared__ __align__(128) double smem[];
+#if CS_PREC == 0
   if (!cs_big_ok(bt, CS_WS_COND, CS_SM_COND)) return;
+#else
+  if (!cs_big_ok(bt, CS_WS_COND, CS_TC_SMD)) return;
+  // the CTA's tensor-memory accumulator and MMA barrier, for all its intervals
+  unsigned char* smb = reinterpret_cast<unsigned char*>(smem);
+  unsigned long long* mb = reinterpret_cast<unsigned long long*>(smb + CS_TC_MISC);
+  unsigned* tslot = reinterpret_cast<unsigned*>(mb + 1);
+  int* flag = reinterpret_cast<int*>(tslot + 1);
+  if (threadIdx.x == 0) {
+    cs_mbar_init(cs_sa(mb), 1);
+    *flag = 0;
+  }
+  if (threadIdx.x < 32) cs_tmem_alloc(cs_sa(tslot), CS_TC_COLS);
+  cs_tc_before_sync();
+  __syncthreads();
+  cs_tc_after_sync();
+  const unsigned tmem = *tslot;
+  unsigned phase = 0;
+#endif
   double* slab = bt.wsp + (size_t)blockIdx.x * bt.wsp_stride;
   const int njac = bt.nlist[1];
   const long long total = bt.jac_pre[njac];
@@ -2097,9 +2430,20 @@ extern "C" __global__ void __launch_bounds__(256, 2) k_condense(CsBatch bt) {
 #if CS_PREC == 0
     cs_condense_big<double, 0>(bt, slot, slab, smem);
 #else
-    cs_condense_big<float, CS_PREC>(bt, slot, slab, smem);
+    if (!cs_condense_tc<CS_PREC>(bt, slot, slab, smb, tmem, cs_sa(mb), phase, flag)) break;
 #endif
   }
+#if CS_PREC != 0
+  // release the accumulator; a tensor-core timeout is reported like a
+  // configuration error (the host then fails the call)
+  cs_tc_before_sync();
+  __syncthreads();
+  if (threadIdx.x == 0 && *flag) atomicAdd(&bt.counters[7], 1ull);
+  if (threadIdx.x < 32) {
+    cs_tc_after_sync();
+    cs_tmem_free(tmem, CS_TC_COLS);
+  }
+#endif
 }
 
 #endif  // CS_BIG_COND
@@ -2537,9 +2881,10 @@ extern "C" __global__ void __launch_bounds__(256) k_tree_level(CsBatch bt, int l
 }
 
 // Top of the tree, one CTA per instance (as cs_top_warp; Dr goes to the slab).
-extern "C" __global__ void __launch_bounds__(256) k_top(CsBatch bt) {
-  extern __shared__ double smem[];
-  if (!cs_big_ok(bt, CS_WS_TOP, CS_SM_TOP)) return;
+// dyk, dpk (refinement, else null): the system is solved for a correction of
+// the direction (dyk, dpk), so the boundary rows' right-hand side is their
+// residual -r - Dr [dy_0; dy_n; dp] (FP64).
+__device__ void cs_top_big(const CsBatch& bt, double* smem, const double* dyk, const double* dpk) {
   double* slab = bt.wsp + (size_t)blockIdx.x * bt.wsp_stride;
   double* top = CS_T_SMEM ? smem : slab;
   double* Dr = CS_T_SMEM ? slab : slab + CS_TSZ;
@@ -2570,6 +2915,16 @@ extern "C" __global__ void __launch_bounds__(256) k_top(CsBatch bt) {
       top[(size_t)c * CS_TLD + r] = v;
     }
     for (int r = tid; r < CS_NY; r += nt) top[(size_t)CS_NT * CS_TLD + r] = row[(2 * CS_NY + CS_NPE) * CS_NY + r];
+    if (dyk != nullptr) {
+      for (int q = tid; q < CS_NY + CS_NP; q += nt) {
+        const double* dr = Dr + (size_t)q * (2 * CS_NY + CS_NP);
+        double v = top[(size_t)CS_NT * CS_TLD + CS_NY + q];
+        for (int c = 0; c < CS_NY; ++c) v = fma(-dr[c], dyk[(size_t)off * CS_NY + c], v);
+        for (int c = 0; c < CS_NY; ++c) v = fma(-dr[CS_NY + c], dyk[(size_t)(off + N - 1) * CS_NY + c], v);
+        for (int c = 0; c < CS_NP; ++c) v = fma(-dr[2 * CS_NY + c], dpk[(size_t)b * CS_NP + c], v);
+        top[(size_t)CS_NT * CS_TLD + CS_NY + q] = v;
+      }
+    }
     __syncthreads();
 #pragma unroll 1
     for (int kk = 0; kk < CS_NT; ++kk) cs_householder_cta(top, CS_TLD, CS_NT, CS_NT + 1, kk, red);
@@ -2606,6 +2961,79 @@ extern "C" __global__ void __launch_bounds__(256) k_top(CsBatch bt) {
     __syncthreads();
   }
 }
+
+extern "C" __global__ void __launch_bounds__(256) k_top(CsBatch bt) {
+  extern __shared__ double smem[];
+  if (!cs_big_ok(bt, CS_WS_TOP, CS_SM_TOP)) return;
+  cs_top_big(bt, smem, nullptr, nullptr);
+}
+
+#if CS_PREC_TREE != 0
+// FP64 iterative refinement of the Newton direction when the tree merges run
+// on the tensor cores: the condensed system M d = b is solved by the
+// low-precision tree (relative error ~1e-2), so each sweep forms the FP64
+// residual of the saved condensed blocks [A C H b] at the current (dy, dp),
+// solves M c = residual with the same tree, top and back substitution, and
+// adds c.  A sweep multiplies the direction's error by about the tree's own.
+//
+// k_refine_residual: for every interval of an instance on the Newton list,
+// rows0 = [A C H rho] with rho = b - A dy_i - C dy_{i+1} - H dp (FP64, from
+// `keep`, the condensation's output); (dy, dp) saved in (dyk, dpk).
+extern "C" __global__ void k_refine_residual(CsBatch bt, const double* __restrict__ keep, double* dyk, double* dpk) {
+  const int wpc = blockDim.x >> 5, w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int njac = bt.nlist[1];
+  const long long total = bt.jac_pre[njac];
+  for (long long it = (long long)blockIdx.x * wpc + w; it < total; it += (long long)gridDim.x * wpc) {
+    const int k = cs_find(bt.jac_pre, njac, it);
+    const int b = bt.jac[k];
+    const int i = (int)(it - bt.jac_pre[k]);
+    const int slot = bt.off[b] + i;
+    const double* src = keep + (size_t)slot * CS_ROWSZ;
+    double* dst = bt.rows0 + (size_t)slot * CS_ROWSZ;
+    const double* yl = bt.dy + (size_t)slot * CS_NY;
+    const double* yr = yl + CS_NY;
+    const double* dpv = bt.dp + (size_t)b * CS_NP;
+    for (int q = lane; q < (2 * CS_NY + CS_NPE) * CS_NY; q += 32) dst[q] = src[q];
+    for (int a = lane; a < CS_NY; a += 32) {
+      double v = src[(size_t)(2 * CS_NY + CS_NPE) * CS_NY + a];
+      for (int c = 0; c < CS_NY; ++c) v = fma(-src[(size_t)c * CS_NY + a], yl[c], v);
+      for (int c = 0; c < CS_NY; ++c) v = fma(-src[(size_t)(CS_NY + c) * CS_NY + a], yr[c], v);
+      for (int c = 0; c < CS_NPE; ++c) v = fma(-src[(size_t)(2 * CS_NY + c) * CS_NY + a], dpv[c], v);
+      dst[(size_t)(2 * CS_NY + CS_NPE) * CS_NY + a] = v;
+      dyk[(size_t)slot * CS_NY + a] = yl[a];
+      if (i == bt.N[b] - 2) dyk[(size_t)(slot + 1) * CS_NY + a] = yr[a];
+    }
+    if (i == 0)
+      for (int c = lane; c < CS_NP; c += 32) dpk[(size_t)b * CS_NP + c] = dpv[c];
+  }
+}
+
+// the boundary rows of the correction solve (cs_top_big with dyk, dpk)
+extern "C" __global__ void __launch_bounds__(256) k_top_refine(CsBatch bt, const double* dyk, const double* dpk) {
+  extern __shared__ double smem[];
+  if (!cs_big_ok(bt, CS_WS_TOP, CS_SM_TOP)) return;
+  cs_top_big(bt, smem, dyk, dpk);
+}
+
+// (dy, dp) = saved direction + correction
+extern "C" __global__ void k_refine_add(CsBatch bt, const double* dyk, const double* dpk) {
+  const int wpc = blockDim.x >> 5, w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int njac = bt.nlist[1];
+  const long long total = bt.jac_pre[njac];
+  for (long long it = (long long)blockIdx.x * wpc + w; it < total; it += (long long)gridDim.x * wpc) {
+    const int k = cs_find(bt.jac_pre, njac, it);
+    const int b = bt.jac[k];
+    const int i = (int)(it - bt.jac_pre[k]);
+    const int slot = bt.off[b] + i;
+    for (int a = lane; a < CS_NY; a += 32) {
+      bt.dy[(size_t)slot * CS_NY + a] += dyk[(size_t)slot * CS_NY + a];
+      if (i == bt.N[b] - 2) bt.dy[(size_t)(slot + 1) * CS_NY + a] += dyk[(size_t)(slot + 1) * CS_NY + a];
+    }
+    if (i == 0)
+      for (int c = lane; c < CS_NP; c += 32) bt.dp[(size_t)b * CS_NP + c] += dpk[(size_t)b * CS_NP + c];
+  }
+}
+#endif  // CS_PREC_TREE != 0
 #endif  // CS_BIG_TREE
 #endif  // CS_BIG
 

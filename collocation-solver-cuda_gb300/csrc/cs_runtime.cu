@@ -263,6 +263,9 @@ struct cs_module {
   CUfunction f_form_initial, f_residual, f_decide, f_accept, f_condense, f_segres, f_mesh_decide,
       f_remesh_count, f_remesh_write, f_repack, f_znodes, f_lists, f_tree_level, f_top, f_backsub_level, f_recover,
       f_babd_cta, f_upper;
+  // FP64 refinement of the direction when the tree merges run on the tensor
+  // cores (prec_tree != 0)
+  CUfunction f_refine_res = nullptr, f_top_refine = nullptr, f_refine_add = nullptr;
   size_t babd_cta_smem;
   // k_upper (upper tree levels, top and their back substitution, CTA per
   // instance): 0 when the block rows are too large for lane merges
@@ -438,6 +441,24 @@ extern "C" int cs_module_load(const cs_module_desc* d, cs_module** out) {
     if (M->big_tree) M->slab = std::max(M->slab, std::max(q_smem ? 0ll : qsz, (t_smem ? 0ll : tsz) + drsz));
     if (M->big_cond) {
       M->condense_smem = (size_t)sm_cond * 8;
+      if (M->prec) {
+        // tensor-core condensation (CS_NBT .. CS_TC_SMB in cs_kernels.cuh)
+        const long long nbt = 32, eps = (M->prec == 1) ? 4 : 8, kc = nbt / eps, kb = nb / eps, kf = 64 / eps;
+        const long long mp = (s1 > nbt) ? ((s1 - nbt + 127) / 128) * 128 : 128, mb = ((s1 + 127) / 128) * 128;
+        const long long nr = ((M->nrhs + 15) / 16) * 16;
+        auto r128 = [](long long x) { return ((x + 127) / 128) * 128; };
+        const long long ops = r128(std::max((mp + 256) * kc * 16, (mb + nr) * kb * 16));
+        const long long panel = r128((long long)s1 * (nbt + 1) * 4);
+        const long long dbl = 8 * ((long long)d->m * rb + d->m * d->m + d->ny + 16);
+        const long long misc = ops + panel + dbl + r128(4 * (long long)s1 + 4 * nbt);
+        if ((128 + nr) * kf * 16 > ops + panel) {
+          delete M;
+          return set_err(CS_ERR_INVALID, "cs_module_load: tensor-core fill operands do not fit");
+        }
+        // at least 80 KB: at most two CTAs per SM, so that their tensor-memory
+        // accumulators (256 columns each) always fit the SM's 512
+        M->condense_smem = std::max<size_t>((size_t)(((misc + 16) + 7) / 8) * 8, 80 * 1024);
+      }
       if (M->condense_smem > (size_t)smem_optin) {
         delete M;
         return set_err(CS_ERR_INVALID, "cs_module_load: stage system of size " + std::to_string(M->s) + " too large");
@@ -539,18 +560,42 @@ extern "C" int cs_module_load(const cs_module_desc* d, cs_module** out) {
     for (int k = 0; k < 3; ++k)
       if (g_drv.moduleGetFunction(&M->f_cond_l[k], M->mod, names[k]) != CUDA_SUCCESS) M->f_cond_l[k] = nullptr;
   }
+  if (M->big_tree && M->prec_tree) {
+    struct {
+      CUfunction* f;
+      const char* name;
+    } rf[] = {{&M->f_refine_res, "k_refine_residual"}, {&M->f_top_refine, "k_top_refine"},
+              {&M->f_refine_add, "k_refine_add"}};
+    for (auto& e : rf) {
+      if (g_drv.moduleGetFunction(e.f, M->mod, e.name) != CUDA_SUCCESS) {
+        g_drv.moduleUnload(M->mod);
+        delete M;
+        return set_err(CS_ERR_CUDA, std::string("missing kernel ") + e.name);
+      }
+    }
+  }
   if (M->condense_smem > 48 * 1024)
     CS_CU(g_drv.funcSetAttribute(M->f_condense, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, (int)M->condense_smem));
   if (M->tree_smem > 48 * 1024)
     CS_CU(g_drv.funcSetAttribute(M->f_tree_level, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, (int)M->tree_smem));
-  if (M->top_smem > 48 * 1024)
+  if (M->top_smem > 48 * 1024) {
     CS_CU(g_drv.funcSetAttribute(M->f_top, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, (int)M->top_smem));
+    if (M->f_top_refine)
+      CS_CU(g_drv.funcSetAttribute(M->f_top_refine, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, (int)M->top_smem));
+  }
   if (M->big) {
     // persistent grids from the kernels' occupancy (registers and shared memory)
     M->big_ctas = 0;
     if (M->big_cond) {
       int pc = 0;
       CS_CU(g_drv.occupancy(&pc, M->f_condense, M->condense_block, M->condense_smem));
+      if (M->prec) {
+        // tensor-core condensation: two CTAs per SM whenever their shared
+        // memory fits (registers are bounded for two by the kernel; the
+        // occupancy query reports one for this kernel)
+        const int by_smem = (int)((size_t)smem_sm / (M->condense_smem + 1024));
+        pc = std::max(pc, std::min(2, by_smem));
+      }
       M->condense_grid = M->sms * std::max(1, pc);
       M->big_ctas = std::max(M->big_ctas, M->condense_grid);
     }
@@ -615,6 +660,7 @@ extern "C" void cs_opts_default(cs_opts* o) {
   o->residual_type = 1;
   o->scale_by_time = 1;
   o->residual2 = 0;
+  o->refine = 2;
 }
 
 
@@ -638,6 +684,9 @@ struct cs_batch {
   DBuf t[2], y[2], ydot[2], zt[2], znode[2];
   int cur = 0;
   DBuf inst_of, dy, dydot, dzt, X, rows0, rows1, tree, res;
+  // refinement (tensor-core tree): the condensed blocks as condensed, the
+  // direction a correction is added to
+  DBuf rows_keep, dy_keep, dp_keep;
   DBuf wsp;  // large stage systems: slab per CTA
   std::vector<int> hN, hoff;
   cs_opts opts;
@@ -652,6 +701,7 @@ struct cs_batch {
   int graph_nlvl[2] = {-1, -1};
   int graph_tune[2] = {-1, -1};
   int graph_lo[2] = {-1, -1};  // first k_upper level the graph was captured with
+  int graph_refine[2] = {-1, -1};  // refinement sweeps captured
   CsBatchDev graph_view[2];
   CsConsts graph_consts[2];
   // device copy of the last initial guess (cs_batch_reset)
@@ -709,6 +759,10 @@ static int alloc_slots(cs_batch* bt, long long cap, bool keep_current) {
   CS_TRY(dalloc(bt->rows1, c * M->rowsz * d));
   CS_TRY(dalloc(bt->tree, c * M->treesz * d));
   CS_TRY(dalloc(bt->res, c * d));
+  if (M->prec_tree) {
+    CS_TRY(dalloc(bt->rows_keep, c * M->rowsz * d));
+    CS_TRY(dalloc(bt->dy_keep, c * M->ny * d));
+  }
   bt->cap = (long long)c;
   return CS_OK;
 }
@@ -844,7 +898,9 @@ static int check_config(cs_batch* bt) {
   unsigned long long c7 = 0;
   CS_CUDA(cudaMemcpyAsync(&c7, (unsigned long long*)bt->dcounters.p + 7, sizeof(c7), cudaMemcpyDeviceToHost, bt->stream));
   CS_CUDA(cudaStreamSynchronize(bt->stream));
-  if (c7 != 0) return set_err(CS_ERR_STATE, "large-system kernel launched without its shared memory or slab");
+  if (c7 != 0)
+    return set_err(CS_ERR_STATE,
+                   "large-system kernel launched without its shared memory or slab, or a tensor-core MMA timed out");
   return CS_OK;
 }
 
@@ -897,6 +953,10 @@ static int run_direction(cs_batch* bt, CsBatchDev& v, int nlvl) {
     return launch_k(bt, M->f_recover, (unsigned)(M->sms * 8), 128, 0, ar, 1);
   }
   const unsigned g = (unsigned)(M->sms * 8);
+  const bool refine = M->prec_tree && bt->opts.refine > 0 && M->f_refine_res;
+  if (refine)  // the condensed blocks, for the residuals of the refinement
+    CS_CUDA(cudaMemcpyAsync(bt->rows_keep.p, bt->rows0.p, (size_t)bt->T * M->rowsz * sizeof(double),
+                            cudaMemcpyDeviceToDevice, bt->stream));
   // levels from l_lo up (at most 8 merges per instance there) and the top
   // system in one launch, CTA per instance
   const int l_lo = upper_levels(bt, nlvl);
@@ -917,6 +977,28 @@ static int run_direction(cs_batch* bt, CsBatchDev& v, int nlvl) {
   for (int l = l_lo - 1; l >= 0; --l) {
     void* a[] = {&v, &l};
     CS_TRY(launch_k(bt, M->f_backsub_level, g, 128, 0, a, 1));
+  }
+  if (refine) {
+    // FP64 iterative refinement: residual of the condensed system at the
+    // direction, the correction from the same (low-precision) tree, added
+    double* keep = (double*)bt->rows_keep.p;
+    double* dyk = (double*)bt->dy_keep.p;
+    double* dpk = (double*)bt->dp_keep.p;
+    for (int sw = 0; sw < bt->opts.refine; ++sw) {
+      void* ar[] = {&v, &keep, &dyk, &dpk};
+      CS_TRY(launch_k(bt, M->f_refine_res, g, 128, 0, ar, 1));
+      for (int l = 0; l < l_lo; ++l) {
+        void* a[] = {&v, &l};
+        CS_TRY(launch_k(bt, M->f_tree_level, (unsigned)M->tree_grid, 256, M->tree_smem, a, 1));
+      }
+      void* at[] = {&v, &dyk, &dpk};
+      CS_TRY(launch_k(bt, M->f_top_refine, (unsigned)std::min(M->big_ctas, bt->B), 256, M->top_smem, at, 1));
+      for (int l = l_lo - 1; l >= 0; --l) {
+        void* a[] = {&v, &l};
+        CS_TRY(launch_k(bt, M->f_backsub_level, g, 128, 0, a, 1));
+      }
+      CS_TRY(launch_k(bt, M->f_refine_add, g, 128, 0, at, 1));
+    }
   }
   void* a[] = {&v};
   return launch_k(bt, M->f_recover, g, 128, 0, a, 1);
@@ -973,6 +1055,7 @@ extern "C" int cs_batch_create(cs_module* M, int batch, long long node_capacity,
   if ((rc = dalloc(bt->dN, batch * sizeof(int))) || (rc = dalloc(bt->doff, batch * sizeof(int))) ||
       (rc = dalloc(bt->doff2, batch * sizeof(int))) || (rc = dalloc(bt->dp, batch * std::max(M->np, 1) * d)) ||
       (rc = dalloc(bt->ddp, batch * std::max(M->np, 1) * d)) ||
+      (M->prec_tree && (rc = dalloc(bt->dp_keep, batch * std::max(M->np, 1) * d))) ||
       (rc = dalloc(bt->dth, batch * std::max(M->nth, 1) * d)) || (rc = dalloc(bt->dinst, batch * sizeof(CsInst))) ||
       (rc = dalloc(bt->dcounters, 64)) || (rc = dalloc(bt->l_act, batch * sizeof(int))) ||
       (rc = dalloc(bt->dtrials, (size_t)batch * CS_LSW * sizeof(unsigned long long))) ||
@@ -1003,7 +1086,8 @@ extern "C" void cs_batch_free(cs_batch* bt) {
   DBuf* all[] = {&bt->dN, &bt->doff, &bt->doff2, &bt->dp, &bt->dth, &bt->ddp, &bt->dinst, &bt->dcounters, &bt->dtrials,
                  &bt->inst_of, &bt->dy, &bt->dydot, &bt->dzt, &bt->X, &bt->rows0, &bt->rows1, &bt->tree, &bt->res,
                  &bt->iN, &bt->ioff, &bt->it, &bt->iy, &bt->iz, &bt->ip, &bt->l_act, &bt->l_jac, &bt->l_acc,
-                 &bt->l_actp, &bt->l_jacp, &bt->l_accp, &bt->l_lvlp, &bt->l_n, &bt->wsp};
+                 &bt->l_actp, &bt->l_jacp, &bt->l_accp, &bt->l_lvlp, &bt->l_n, &bt->wsp,
+                 &bt->rows_keep, &bt->dy_keep, &bt->dp_keep};
   for (DBuf* b : all) dfree(*b);
   for (int k = 0; k < 2; ++k)
     if (bt->graph[k]) cudaGraphExecDestroy(bt->graph[k]);
@@ -1172,6 +1256,7 @@ static int get_graph(cs_batch* bt, const CsConsts& c, int nlvl, int reps) {
   const int k = use_cta_path(bt) ? 1 : 0;
   const int lo = upper_levels(bt, nlvl);
   if (bt->graph[k] && bt->graph_nlvl[k] == nlvl && bt->graph_tune[k] == bt->M->tune_ver && bt->graph_lo[k] == lo &&
+      bt->graph_refine[k] == bt->opts.refine &&
       memcmp(&bt->graph_view[k], &v, sizeof(v)) == 0 && memcmp(&bt->graph_consts[k], &c, sizeof(c)) == 0)
     return CS_OK;
   if (bt->graph[k]) {
@@ -1199,6 +1284,7 @@ static int get_graph(cs_batch* bt, const CsConsts& c, int nlvl, int reps) {
   bt->graph_nlvl[k] = nlvl;
   bt->graph_tune[k] = bt->M->tune_ver;
   bt->graph_lo[k] = lo;
+  bt->graph_refine[k] = bt->opts.refine;
   return CS_OK;
 }
 

@@ -62,7 +62,8 @@ __global__ void __launch_bounds__(256) k_tc_update(int M, int N, int K, const fl
   cs_tc_after_sync();
   const unsigned tmem = *slot;
   unsigned phase = 0;
-  const bool ok = cs_tc_block_update<PREC>(C, ldc, M, N, A_s, B_s, kc, nks, tmem, cs_sa(mbar), phase, kWaitCycles, flag);
+  const bool ok =
+      cs_tc_block_update<PREC>(C, ldc, 1, M, N, A_s, B_s, kc, nks, tmem, cs_sa(mbar), phase, kWaitCycles, flag);
   cs_tc_before_sync();
   __syncthreads();
   if (tid < 32) {

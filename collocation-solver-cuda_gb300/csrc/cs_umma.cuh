@@ -176,13 +176,16 @@ struct CsTcElems {
 
 // C[0:M, 0:N] -= A B^T, all threads of the CTA (blockDim.x a multiple of
 // 128); A_s, B_s staged as described above with kc core matrices along K and
-// nks k-steps; C row r at C + r * ldc (global or shared memory).  tmem: the
+// nks k-steps; element (r, c) of C at C[r * rs + c * cs] (global or shared
+// memory).  A thread updates one row of C (its TMEM lane), so with C
+// column-major (rs = 1, cs = its leading dimension) a warp's accesses to one
+// column are one contiguous 128-byte line.  tmem: the
 // CTA's CS_TC_COLS accumulator columns; mbar / phase: the CTA's barrier and
 // its next phase.  Returns false (on every thread) if an MMA group did not
 // complete within `limit` cycles; the caller reports it and must not reuse
 // the operands or the accumulator.
 template <int PREC>
-__device__ bool cs_tc_block_update(float* C, long long ldc, int M, int N, const unsigned char* A_s,
+__device__ bool cs_tc_block_update(float* C, long long rs, long long cs, int M, int N, const unsigned char* A_s,
                              const unsigned char* B_s, int kc, int nks, unsigned tmem, unsigned mbar, unsigned& phase,
                              long long limit, int* flag_smem) {
   const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5, nw = blockDim.x >> 5;
@@ -222,11 +225,16 @@ __device__ bool cs_tc_block_update(float* C, long long ldc, int M, int N, const 
         float v[16];
         cs_tmem_ld16(tmem + ((unsigned)(quad * 32) << 16) + (unsigned)(gi * 16), v);
         if (row < M) {
-          float* cr = C + (long long)row * ldc + n0 + gi * 16;
+          // all 16 loads before the stores (they cannot alias each other, which
+          // the compiler does not know): one memory latency per 16 columns
+          float* cr = C + (long long)row * rs + (long long)(n0 + gi * 16) * cs;
           const int nv = min(16, nch - gi * 16);
+          float c[16];
+#pragma unroll
+          for (int j = 0; j < 16; ++j) c[j] = (j < nv) ? cr[j * cs] : 0.f;
 #pragma unroll
           for (int j = 0; j < 16; ++j)
-            if (j < nv) cr[j] -= v[j];
+            if (j < nv) cr[j * cs] = c[j] - v[j];
         }
       }
       cs_tc_before_sync();

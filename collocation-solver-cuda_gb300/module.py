@@ -47,6 +47,7 @@ def kernel_program_text(problem, m, big=False, smem_max=232448):
     out += arr("CS_A", t["A"]) + arr("CS_B", t["b"]) + arr("CS_C", t["c"]) + arr("CS_GW", t["gw"])
     out += arr("CS_GL", t["gL"]) + arr("CS_GI", t["gI"]) + arr("CS_L0", t["L0"]) + arr("CS_L1", t["L1"])
     out += cuda_problem_source(pc)
+    out += open(os.path.join(HERE, "csrc", "cs_umma.cuh")).read() + "\n"
     out += open(os.path.join(HERE, "csrc", "cs_kernels.cuh")).read()
     return out
 

@@ -103,6 +103,11 @@ typedef struct cs_opts {
                             (default), 2 weighted squares, 0 weighted maximum */
   int scale_by_time;     /* multiply the running estimate by h (default 1) */
   int residual2;         /* 1: the residual2 estimate instead (CS:1895-2013) */
+  int refine;            /* tree merges on the tensor cores (precision 3, 4): sweeps of
+                            FP64 iterative refinement of every Newton direction (the
+                            residual of the condensed system in FP64, a correction from
+                            the same tree); default 2, 0 off.  No reference counterpart
+                            (the reference solves in FP64 only) */
 } cs_opts;
 
 void cs_opts_default(cs_opts* o);

@@ -217,21 +217,26 @@ def test_reduced_precision_solve_reaches_fp64_oracle_solution(cs, prec):
         assert np.abs(s[k] - rk).max() < 1e-6, (k, np.abs(s[k] - rk).max())
 
 
-def test_tensor_core_tree_option_converges_on_small_chain(cs):
-    """The opt-in TF32 tree merges (precision "tf32-tree"): a more inexact
-    direction (measured ~1e-2 relative), so more Newton steps, but the FP64
-    residual still drives the solve to the tolerance: K = 16 from a coarse
-    9-node guess lands within 1e-5 of the FP64 oracle (measured 5e-7)."""
+@pytest.mark.parametrize("refine", [0, 2])
+def test_tensor_core_tree_option_converges_on_small_chain(cs, refine):
+    """The opt-in TF32 tree merges (precision "tf32-tree"): without
+    refinement a more inexact direction (measured ~1e-2 relative), so more
+    Newton steps, but the FP64 residual still drives the solve to the
+    tolerance; with the default two FP64 refinement sweeps, the oracle's
+    Newton count.  K = 16 from a coarse 9-node guess, within 1e-5 of the FP64
+    oracle (measured 5e-7 unrefined)."""
     pr = _pendulum(cs, 16, 9)
     cp = cs.CompiledProblem(pr, 5, precision="tf32-tree")
     bt = cs.Batch(cp, 1)
     bt.set_guess([(np.asarray(pr.T0, float), np.asarray(pr.Y0, float), np.asarray(pr.Z0, float))],
                  np.asarray(pr.P0, float).reshape(1, -1))
-    bt.solve(cs.default_opts(pr))
+    bt.solve(cs.default_opts(pr, refine=refine))
     s = bt.solution()[0]
     ref = O.solve(OracleProblem(pr), 5, cs.tables.lobatto(5), cs.tables.segment_tables(5))
     assert s["success"] and s["N"] == ref.N
     assert np.abs(s["y"] - ref.y).max() < 1e-5
+    if refine:
+        assert s["newton_steps"] == ref.jacobian_count
 
 
 def test_pendulum8_hybrid_layout_matches_oracle(cs):
@@ -322,4 +327,27 @@ def test_pendulum_chain_reduced_precision_error_against_oracle(cs, K, prec):
               np.abs(s["p"] - g["p"]).max())
     print("K=%d %s: max-abs error against the FP64 oracle %.3g (Newton %d, oracle %d)"
           % (K, prec, err, s["newton_steps"], int(g["jacobian_counts"])))
+    assert err < REDUCED_BOUND
+
+
+@pytest.mark.parametrize("K,prec", [(16, "tf32-tree"), (16, "bf16-tree"), (32, "tf32-tree"), (32, "bf16-tree")])
+def test_tensor_core_tree_with_refinement_keeps_the_fp64_newton_count(cs, K, prec):
+    """The tree merges on the tensor cores as well (an inexact BABD solve,
+    ~1e-2 relative), with FP64 iterative refinement of every direction (two
+    sweeps, the default: the residual of the condensed system in FP64, a
+    correction from the same tree): the stated-size solve takes the FP64
+    oracle's Newton and residual counts and lands within REDUCED_BOUND of its
+    solution."""
+    g = golden("large_pend%d" % K)
+    pr, cp, bt = _stated_size(cs, K, prec)
+    opts = cs.default_opts(pr)
+    assert opts.refine == 2
+    bt.solve(opts)
+    s = bt.solution()[0]
+    assert s["success"]
+    assert (s["newton_steps"], s["residual_evals"], s["N"]) == \
+           (int(g["jacobian_counts"]), int(g["residual_counts"]), int(g["N"]))
+    err = max(np.abs(_rows(s["y"], g) - g["y"]).max(), np.abs(_rows(s["z"], g) - g["z"]).max(),
+              np.abs(s["p"] - g["p"]).max())
+    print("K=%d %s, 2 refinement sweeps: max-abs error against the FP64 oracle %.3g" % (K, prec, err))
     assert err < REDUCED_BOUND
