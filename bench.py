@@ -914,6 +914,8 @@ def main():
     ap.add_argument("--profile-case", action="store_true",
                     help="small case for ncu: 512 instances, one full-batch condensation per m group, one solve; "
                          "with --workload pendulum: one Newton direction of the large instance")
+    ap.add_argument("--profile-instances", type=int, default=512,
+                    help="instances of the plain profile case (the batched Van der Pol distribution, seed 1)")
     args = ap.parse_args()
     BABD_PATH[0] = args.babd_path
     if args.profile_case and args.workload == "pendulum":
@@ -956,7 +958,7 @@ def main():
     if args.profile_case:
         cs = _pkg()
         cs.build.build_library()
-        W = Workload(cs, cs.workloads.vdp_batch(512, seed=SEED))
+        W = Workload(cs, cs.workloads.vdp_batch(args.profile_instances, seed=SEED))
         for g in W.groups:
             g["bt"].reset()
             ms = g["bt"].time_condense(reps=1)

@@ -14,4 +14,4 @@ is no CPU fallback.
 """
 from . import tables, ocp, codegen, io, _lib, module, solver, build, workloads, warmstart  # noqa: F401
 from .ocp import Problem  # noqa: F401
-from .module import Batch, CompiledProblem, default_opts  # noqa: F401
+from .module import Batch, CompiledProblem, GeneratedProblem, default_opts  # noqa: F401

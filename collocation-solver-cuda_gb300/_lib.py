@@ -80,6 +80,7 @@ SIGNATURES = {
     "cs_last_error": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_size_t]),
     "cs_time_condense": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _dp]),
     "cs_measure_fp64_peak": (ctypes.c_int, [_dp]),
+    "cs_measure_dmma_peak": (ctypes.c_int, [_dp]),
     "cs_profiler_start": (ctypes.c_int, []),
     "cs_batch_set_opts": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
     "cs_autotune_condense": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(TuneResult)]),

@@ -869,7 +869,10 @@ __device__ __forceinline__ void cs_condense_entry(const CsBatch& bt) {
 
 extern "C" __global__ void k_condense(CsBatch bt) { cs_condense_entry<CS_CGL>(bt); }
 #if CS_S1 <= 48
-// the tuner's candidates: 8, 16 or 32 lanes per interval
+// the tuner's candidates: 4, 8, 16 or 32 lanes per interval (fewer lanes:
+// more intervals share each warp instruction of the elimination, whose
+// short loops leave fewer lanes idle)
+extern "C" __global__ void k_condense_l4(CsBatch bt) { cs_condense_entry<4>(bt); }
 extern "C" __global__ void k_condense_l8(CsBatch bt) { cs_condense_entry<8>(bt); }
 extern "C" __global__ void k_condense_l16(CsBatch bt) { cs_condense_entry<16>(bt); }
 extern "C" __global__ void k_condense_l32(CsBatch bt) { cs_condense_entry<32>(bt); }

@@ -220,6 +220,26 @@ __global__ void k_dfma_peak(double* out, int iters) {
   if (s == 12345.678) out[0] = s;
 }
 
+// FP64 tensor-core (DMMA, mma.sync m8n8k4) throughput: four independent
+// accumulator tiles per warp
+__global__ void k_dmma_peak(double* out, int iters) {
+  const double a = threadIdx.x * 1e-3, b = 0.999;
+  double c[4][2];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) c[q][0] = c[q][1] = q;
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+      asm volatile("mma.sync.aligned.m8n8k4.row.col.f64.f64.f64.f64 {%0,%1}, {%2}, {%3}, {%0,%1};"
+                   : "+d"(c[q][0]), "+d"(c[q][1])
+                   : "d"(a), "d"(b));
+  }
+  double s = 0.0;
+#pragma unroll
+  for (int q = 0; q < 4; ++q) s += c[q][0] + c[q][1];
+  if (s == 12345.678) out[0] = s;
+}
+
 // y, z at the nodes of every instance from its trajectory vector (linear in
 // normalised time on n_nodes equispaced nodes), and p from its tail
 __global__ void k_warm_fill(int B, int ny, int nz, int np, int n_nodes, const float* traj, int stride, const int* N,
@@ -290,7 +310,7 @@ struct cs_module {
   int big_ctas = 0;    // CTAs with a slab (the largest grid of the slab kernels)
   int tree_grid = 0;   // k_tree_level grid (large systems)
   // condensation shape tuner
-  CUfunction f_cond_l[3] = {nullptr, nullptr, nullptr};  // 8, 16, 32 lanes per interval
+  CUfunction f_cond_l[4] = {nullptr, nullptr, nullptr, nullptr};  // 4, 8, 16, 32 lanes per interval
   size_t grp_bytes = 0;  // shared memory of one interval group (shared-memory kernel)
   int smem_optin = 0;
   int tune_ver = 0;      // bumped when the tuner changes the shape (graphs re-captured)
@@ -556,8 +576,8 @@ extern "C" int cs_module_load(const cs_module_desc* d, cs_module** out) {
     }
   }
   {
-    const char* names[3] = {"k_condense_l8", "k_condense_l16", "k_condense_l32"};
-    for (int k = 0; k < 3; ++k)
+    const char* names[4] = {"k_condense_l4", "k_condense_l8", "k_condense_l16", "k_condense_l32"};
+    for (int k = 0; k < 4; ++k)
       if (g_drv.moduleGetFunction(&M->f_cond_l[k], M->mod, names[k]) != CUDA_SUCCESS) M->f_cond_l[k] = nullptr;
   }
   if (M->big_tree && M->prec_tree) {
@@ -1663,6 +1683,34 @@ extern "C" int cs_measure_fp64_peak(double* tflops) {
   return CS_OK;
 }
 
+extern "C" int cs_measure_dmma_peak(double* tflops) {
+  if (!tflops) return set_err(CS_ERR_INVALID, "cs_measure_dmma_peak: null");
+  CS_TRY(ensure_context());
+  int dev = 0, sms = 0;
+  CS_CUDA(cudaGetDevice(&dev));
+  CS_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  double* out = nullptr;
+  CS_CUDA(cudaMalloc(&out, sizeof(double)));
+  const int iters = 2048, block = 256, grid = sms * 8;
+  k_dmma_peak<<<grid, block>>>(out, 32);
+  cudaEvent_t e0, e1;
+  CS_CUDA(cudaEventCreate(&e0));
+  CS_CUDA(cudaEventCreate(&e1));
+  CS_CUDA(cudaEventRecord(e0));
+  k_dmma_peak<<<grid, block>>>(out, iters);
+  CS_CUDA(cudaEventRecord(e1));
+  CS_CUDA(cudaEventSynchronize(e1));
+  float t = 0.f;
+  CS_CUDA(cudaEventElapsedTime(&t, e0, e1));
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(out);
+  // 2 * 8 * 8 * 4 flops per warp-wide m8n8k4, four per iteration
+  const double flops = 512.0 * 4.0 * iters * (double)grid * (block / 32);
+  *tflops = flops / (t * 1e-3) / 1e12;
+  return CS_OK;
+}
+
 extern "C" int cs_batch_reset(cs_batch* bt) {
   if (!bt || !bt->have_guess || bt->iT == 0) return set_err(CS_ERR_STATE, "cs_batch_reset: no initial guess to restore");
   cs_module* M = bt->M;
@@ -1817,8 +1865,8 @@ extern "C" int cs_autotune_condense(cs_batch* bt, int reps, cs_tune_result* out)
   std::vector<Cand> cands;
   cands.push_back({M->f_condense, M->big_cond ? 0 : M->cgw, M->condense_block, M->condense_grid, M->condense_smem});
   if (!M->big_cond) {
-    const int lanes[3] = {8, 16, 32};
-    for (int k = 0; k < 3; ++k) {
+    const int lanes[4] = {4, 8, 16, 32};
+    for (int k = 0; k < 4; ++k) {
       if (!M->f_cond_l[k]) continue;
       const int gpw = 32 / lanes[k];
       for (int w = 1; w <= 8; w *= 2) {

@@ -69,12 +69,13 @@ class CompiledProblem:
         lib = _lib.load()
         self.problem = problem
         self.m = m
-        pc = ProblemCode(problem.sym)
+        generated = isinstance(problem, GeneratedProblem)
+        pc = problem.code if generated else ProblemCode(problem.sym)
         self.pc = pc
         self.ny, self.nz, self.np, self.np_eff, self.nth = pc.ny, pc.nz, pc.np, pc.np_eff, pc.nth
         self.s = m * (pc.ny + pc.nz)
         self.rowsz = pc.ny * (2 * pc.ny + pc.np_eff + 1)
-        self._src = cuda_problem_source(pc).encode()
+        self._src = (problem.cuda_source if generated else cuda_problem_source(pc)).encode()
         self._t = _tables(m)
         self._cache = (cache_dir or "").encode()
         d = _lib.ModuleDesc()
@@ -102,6 +103,45 @@ class CompiledProblem:
                 self.handle = None
         except Exception:  # noqa: BLE001
             pass
+
+
+class GeneratedProblem:
+    """A problem given by its generated CUDA problem functions (the text
+    codegen.cuda_problem_source emits) with its sizes, constants and solver
+    settings, without the OCP front end and sympy: for machines that only
+    solve problems prepared elsewhere (from_problem makes one from a
+    front-end Problem; the fields can be stored and loaded as plain arrays)."""
+
+    def __init__(self, cuda_source, ny, nz, np_, np_eff, nth, theta=(), tolerance=1e-6,
+                 maximum_newton_iterations=200, maximum_mesh_refinements=10, maximum_nodes=2000, size_inequality=0,
+                 size_sv_inequality=0, name="generated"):
+        import types
+        self.cuda_source = str(cuda_source)
+        self.code = types.SimpleNamespace(ny=int(ny), nz=int(nz), np=int(np_), np_eff=int(np_eff), nth=int(nth))
+        self.size_y, self.size_z, self.size_p = int(ny), int(nz), int(np_)
+        self.theta = np.asarray(theta, dtype=np.float64).reshape(-1)
+        self.tolerance = float(tolerance)
+        self.maximum_newton_iterations = int(maximum_newton_iterations)
+        self.maximum_mesh_refinements = int(maximum_mesh_refinements)
+        self.maximum_nodes = int(maximum_nodes)
+        self.size_inequality = int(size_inequality)
+        self.size_sv_inequality = int(size_sv_inequality)
+        self.name = name
+
+    @classmethod
+    def from_problem(cls, pr, name="generated"):
+        pc = ProblemCode(pr.sym)
+        return cls(cuda_problem_source(pc), pc.ny, pc.nz, pc.np, pc.np_eff, pc.nth, pr.theta, pr.tolerance,
+                   pr.maximum_newton_iterations, pr.maximum_mesh_refinements, pr.maximum_nodes, pr.size_inequality,
+                   pr.size_sv_inequality, name=name)
+
+    @classmethod
+    def from_arrays(cls, d):
+        """From a mapping of plain values (e.g. an npz file's arrays)."""
+        return cls(str(d["cuda_source"]), int(d["ny"]), int(d["nz"]), int(d["np"]), int(d["np_eff"]), int(d["nth"]),
+                   d["theta"], float(d["tolerance"]), int(d["maximum_newton_iterations"]),
+                   int(d["maximum_mesh_refinements"]), int(d["maximum_nodes"]), int(d["size_inequality"]),
+                   int(d["size_sv_inequality"]), name=str(d.get("name", "generated")))
 
 
 def default_opts(problem=None, **kw):
@@ -403,4 +443,12 @@ def measure_fp64_peak():
     lib = _lib.load()
     v = ctypes.c_double()
     _lib.check(lib.cs_measure_fp64_peak(ctypes.byref(v)), "cs_measure_fp64_peak")
+    return v.value
+
+
+def measure_dmma_peak():
+    """FP64 tensor-core (DMMA) throughput in TFLOP/s (register-resident loop)."""
+    lib = _lib.load()
+    v = ctypes.c_double()
+    _lib.check(lib.cs_measure_dmma_peak(ctypes.byref(v)), "cs_measure_dmma_peak")
     return v.value

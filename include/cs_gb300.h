@@ -339,7 +339,7 @@ int cs_last_error(char* buf, size_t len);
 int cs_time_condense(cs_batch* bt, int reps, double* ms);
 
 /* Launch-shape tuner of the condensation (the per-(m, ny) tile shape):
- * times every candidate on the batch's current intervals -- 8, 16 or 32
+ * times every candidate on the batch's current intervals -- 4, 8, 16 or 32
  * lanes per interval x 1..8 warps per CTA for shared-memory stage systems,
  * 128 or 256 threads per CTA for the large-system kernel -- and makes the
  * fastest the module's shape for all its batches.  No reference
@@ -358,6 +358,11 @@ int cs_autotune_condense(cs_batch* bt, int reps, cs_tune_result* out);
  * (TFLOP/s, counting an FMA as 2 flops); the denominator of FP64 roofline
  * fractions. */
 int cs_measure_fp64_peak(double* tflops);
+
+/* FP64 throughput of the tensor cores (mma.sync m8n8k4 f64, "DMMA") in
+ * TFLOP/s from a register-resident loop over the whole GPU, to compare with
+ * cs_measure_fp64_peak (DFMA on the FP64 pipe).  No reference counterpart. */
+int cs_measure_dmma_peak(double* tflops);
 
 /* Start / stop the profiler's collection range (cudaProfilerStart/Stop), so
  * a profiler launched with collection off from the start captures exactly
