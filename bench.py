@@ -914,6 +914,8 @@ def main():
     ap.add_argument("--profile-case", action="store_true",
                     help="small case for ncu: 512 instances, one full-batch condensation per m group, one solve; "
                          "with --workload pendulum: one Newton direction of the large instance")
+    ap.add_argument("--profile-nodes", type=int, default=0,
+                    help="pendulum profile case: nodes of the instance's mesh (0: the stated size)")
     ap.add_argument("--profile-instances", type=int, default=512,
                     help="instances of the plain profile case (the batched Van der Pol distribution, seed 1)")
     args = ap.parse_args()
@@ -923,7 +925,7 @@ def main():
         cs = _pkg()
         cs.build.build_library()
         lib = cs._lib.load()
-        pr = pendulum_problem(cs, args.pendulum)
+        pr = cs.workloads.pendulum_chain_problem(args.pendulum, nodes=args.profile_nodes or None)
         cp = cs.CompiledProblem(pr, _pendulum_configs()[args.pendulum]["m"], precision=args.precision)
         bt = cs.Batch(cp, 1)
         bt.set_guess([(np.asarray(pr.T0, float), np.asarray(pr.Y0, float), np.asarray(pr.Z0, float))],
