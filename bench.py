@@ -326,10 +326,11 @@ class Workload:
         return succ, newton, N
 
 
-# DRAM bytes per condensed interval measured by ncu on the m = 3 case
-# (dram__bytes_read.sum + dram__bytes_write.sum = 130.7 MB over 179,417
-# intervals, profiles/k_condense_vdp_batch512_m3.md)
-TRAFFIC_PER_INTERVAL_NCU = 728.5
+# DRAM bytes per condensed interval measured by ncu per m, one launch over
+# about a million intervals of each m-group (working set far above L2:
+# dram__bytes_read.sum + dram__bytes_write.sum ÷ intervals,
+# profiles/k_condense_vdp_batch3072_mix.md)
+TRAFFIC_PER_INTERVAL_NCU = {3: 1000.4, 4: 1240.4, 5: 1474.0}
 
 
 def flops_per_interval(m, ny=4, nz=1, npe=0):
@@ -402,7 +403,7 @@ def _sum_over_ranks(dist, x):
 def _roofline(groups, fp64_peak):
     """Condensation of every interval of each group, timed alone with CUDA
     events on the batch's stream (one launch per group)."""
-    flops = cbytes = cms = 0.0
+    flops = cbytes = cms = traffic = 0.0
     n_all = 0
     for m, bt in groups:
         bt.reset()
@@ -413,13 +414,16 @@ def _roofline(groups, fp64_peak):
         cbytes += n_int * bytes_per_interval(m, cp.ny, cp.nz, cp.np_eff)
         cms += ms
         n_all += n_int
+        # measured for the Van der Pol family only (ny = 4)
+        traffic += (TRAFFIC_PER_INTERVAL_NCU.get(m, float("nan")) if cp.ny == 4 else float("nan")) * n_int
     achieved = flops / (cms * 1e-3) / 1e12
     return {"bound": "fp64", "kernel": "k_condense", "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
             "frac": achieved / fp64_peak if fp64_peak else None,
-            "traffic": TRAFFIC_PER_INTERVAL_NCU * n_all / len(groups),
-            "traffic_note": "DRAM bytes per launch: the ncu capture of the m=3 case "
-                            "(profiles/k_condense_vdp_batch512_m3.md, 728.5 B per interval) scaled by the intervals "
-                            "of one launch; algorithmic bytes per interval are in flops_note",
+            "traffic": (traffic / len(groups)) if traffic == traffic else None,
+            "traffic_note": "DRAM bytes per launch (average over the m-groups): bytes per interval measured by ncu "
+                            "for each m on a launch of ~1M intervals (profiles/k_condense_vdp_batch3072_mix.md: "
+                            "1000 / 1240 / 1474 B for m = 3 / 4 / 5, 92-94 % of the algorithmic bytes) times the "
+                            "intervals of this launch; algorithmic bytes per interval are in flops_note",
             "peak_source": "DFMA microbenchmark (cs_measure_fp64_peak) in this run; FP64 is absent from "
                            "MEASURED_PEAKS.json",
             "flops_per_launch": flops / len(groups), "ms_per_launch": cms / len(groups),
