@@ -722,6 +722,15 @@ struct cs_batch {
   int graph_tune[2] = {-1, -1};
   int graph_lo[2] = {-1, -1};  // first k_upper level the graph was captured with
   int graph_refine[2] = {-1, -1};  // refinement sweeps captured
+  // Grids of the per-super-step launches are capped to the work of the
+  // instances still in Newton once few are (the tail of a batch): slots of
+  // those instances and their count, 0 = no cap.  Instances only leave the
+  // Newton phase until the next mesh phase, so a cap set at a check holds for
+  // the rest of the phase.  Every capped kernel is grid-stride: the grid
+  // changes the time, not the results.
+  long long work_cap = 0;
+  int inst_cap = 0;
+  long long graph_cap[2] = {-1, -1};
   CsBatchDev graph_view[2];
   CsConsts graph_consts[2];
   // device copy of the last initial guess (cs_batch_reset)
@@ -898,6 +907,19 @@ static int launch(cs_batch* bt, CUfunction f, unsigned grid, unsigned block, siz
 
 static unsigned cdiv(long long a, long long b) { return (unsigned)((a + b - 1) / b); }
 
+// grid g of a grid-stride launch that does `per_cta` items of `items` per CTA
+// at most, where items scale with the capped work (bt->work_cap slots)
+static unsigned capped(const cs_batch* bt, unsigned g, long long items_per_slot, long long per_cta) {
+  if (bt->work_cap <= 0) return g;
+  const long long need = (bt->work_cap * items_per_slot + per_cta - 1) / per_cta;
+  return (unsigned)std::max<long long>(1, std::min<long long>((long long)g, need));
+}
+// grid of a launch with one CTA per instance in Newton
+static unsigned capped_inst(const cs_batch* bt, unsigned g) {
+  if (bt->work_cap <= 0) return g;
+  return (unsigned)std::max(1, std::min((int)g, bt->inst_cap));
+}
+
 static int run_slots(cs_batch* bt, CUfunction f, CsBatchDev& v) {
   void* args[] = {&v};
   return launch(bt, f, cdiv(bt->T, 256), 256, 0, args);
@@ -908,7 +930,10 @@ static int run_insts(cs_batch* bt, CUfunction f, void** args) { return launch(bt
 static int run_condense(cs_batch* bt, CsBatchDev& v) {
   cs_module* M = bt->M;
   void* args[] = {&v};
-  return launch_k(bt, M->f_condense, (unsigned)M->condense_grid, M->condense_block, M->condense_smem, args, 0);
+  // intervals per CTA: groups of cgw lanes (shared-memory kernel), one (large systems)
+  const long long per_cta = M->big_cond ? 1 : std::max(1, M->condense_block / std::max(1, M->cgw));
+  return launch_k(bt, M->f_condense, capped(bt, (unsigned)M->condense_grid, 1, per_cta), M->condense_block,
+                  M->condense_smem, args, 0);
 }
 
 // large-system kernels count a launch that gave them too little shared
@@ -980,23 +1005,28 @@ static int run_direction(cs_batch* bt, CsBatchDev& v, int nlvl) {
   // levels from l_lo up (at most 8 merges per instance there) and the top
   // system in one launch, CTA per instance
   const int l_lo = upper_levels(bt, nlvl);
+  // merges of a level <= slots; per CTA: one (large), at least 4 (warps / lanes)
+  const unsigned gtree = M->big_tree ? capped(bt, (unsigned)M->tree_grid, 1, 1)
+                                     : capped(bt, (unsigned)M->tree_small_grid, 1, 4);
+  const unsigned gback = capped(bt, g, 1, 4);
   for (int l = 0; l < l_lo; ++l) {
     void* a[] = {&v, &l};
-    if (M->big_tree) CS_TRY(launch_k(bt, M->f_tree_level, (unsigned)M->tree_grid, 256, M->tree_smem, a, 1));
-    else CS_TRY(launch_k(bt, M->f_tree_level, (unsigned)M->tree_small_grid, 128, M->tree_smem, a, 1));
+    if (M->big_tree) CS_TRY(launch_k(bt, M->f_tree_level, gtree, 256, M->tree_smem, a, 1));
+    else CS_TRY(launch_k(bt, M->f_tree_level, gtree, 128, M->tree_smem, a, 1));
   }
   if (M->upper_smem && bt->opts.babd_path != 2) {
     int lo = l_lo;
     void* a[] = {&v, &lo};
-    CS_TRY(launch_k(bt, M->f_upper, (unsigned)std::min(M->upper_grid, bt->B), 128, M->upper_smem, a, 1));
+    CS_TRY(launch_k(bt, M->f_upper, capped_inst(bt, (unsigned)std::min(M->upper_grid, bt->B)), 128, M->upper_smem, a, 1));
   } else {
     void* a[] = {&v};
-    if (M->big_tree) CS_TRY(launch_k(bt, M->f_top, (unsigned)std::min(M->big_ctas, bt->B), 256, M->top_smem, a, 1));
-    else CS_TRY(launch_k(bt, M->f_top, (unsigned)(M->sms * 4), 32 * M->top_wpc, M->top_smem, a, 1));
+    if (M->big_tree)
+      CS_TRY(launch_k(bt, M->f_top, capped_inst(bt, (unsigned)std::min(M->big_ctas, bt->B)), 256, M->top_smem, a, 1));
+    else CS_TRY(launch_k(bt, M->f_top, capped_inst(bt, (unsigned)(M->sms * 4)), 32 * M->top_wpc, M->top_smem, a, 1));
   }
   for (int l = l_lo - 1; l >= 0; --l) {
     void* a[] = {&v, &l};
-    CS_TRY(launch_k(bt, M->f_backsub_level, g, 128, 0, a, 1));
+    CS_TRY(launch_k(bt, M->f_backsub_level, gback, 128, 0, a, 1));
   }
   if (refine) {
     // FP64 iterative refinement: residual of the condensed system at the
@@ -1006,22 +1036,23 @@ static int run_direction(cs_batch* bt, CsBatchDev& v, int nlvl) {
     double* dpk = (double*)bt->dp_keep.p;
     for (int sw = 0; sw < bt->opts.refine; ++sw) {
       void* ar[] = {&v, &keep, &dyk, &dpk};
-      CS_TRY(launch_k(bt, M->f_refine_res, g, 128, 0, ar, 1));
+      CS_TRY(launch_k(bt, M->f_refine_res, capped(bt, g, 1, 4), 128, 0, ar, 1));
       for (int l = 0; l < l_lo; ++l) {
         void* a[] = {&v, &l};
-        CS_TRY(launch_k(bt, M->f_tree_level, (unsigned)M->tree_grid, 256, M->tree_smem, a, 1));
+        CS_TRY(launch_k(bt, M->f_tree_level, gtree, 256, M->tree_smem, a, 1));
       }
       void* at[] = {&v, &dyk, &dpk};
-      CS_TRY(launch_k(bt, M->f_top_refine, (unsigned)std::min(M->big_ctas, bt->B), 256, M->top_smem, at, 1));
+      CS_TRY(launch_k(bt, M->f_top_refine, capped_inst(bt, (unsigned)std::min(M->big_ctas, bt->B)), 256,
+                      M->top_smem, at, 1));
       for (int l = l_lo - 1; l >= 0; --l) {
         void* a[] = {&v, &l};
-        CS_TRY(launch_k(bt, M->f_backsub_level, g, 128, 0, a, 1));
+        CS_TRY(launch_k(bt, M->f_backsub_level, gback, 128, 0, a, 1));
       }
-      CS_TRY(launch_k(bt, M->f_refine_add, g, 128, 0, at, 1));
+      CS_TRY(launch_k(bt, M->f_refine_add, capped(bt, g, 1, 4), 128, 0, at, 1));
     }
   }
   void* a[] = {&v};
-  return launch_k(bt, M->f_recover, g, 128, 0, a, 1);
+  return launch_k(bt, M->f_recover, capped(bt, g, 1, 4), 128, 0, a, 1);
 }
 
 static int fill_inst_of(cs_batch* bt) {
@@ -1254,7 +1285,8 @@ static int super_step(cs_batch* bt, const CsConsts& c, int nlvl) {
   const unsigned g = (unsigned)(M->sms * 8);
   {
     void* args[] = {&v};
-    CS_TRY(launch_k(bt, M->f_residual, (unsigned)M->res_grid, 256, 0, args, 2));
+    // (interval, trial) items: up to CS_LSW trials per interval
+    CS_TRY(launch_k(bt, M->f_residual, capped(bt, (unsigned)M->res_grid, CS_LSW, 256), 256, 0, args, 2));
   }
   bt->super_steps += 1;
   CsConsts cc = c;
@@ -1263,7 +1295,7 @@ static int super_step(cs_batch* bt, const CsConsts& c, int nlvl) {
   CS_TRY(run_lists(bt, v, 1, use_cta_path(bt) ? 0 : nlvl));
   {
     void* args[] = {&v};
-    CS_TRY(launch(bt, M->f_accept, g, 256, 0, args));
+    CS_TRY(launch(bt, M->f_accept, capped(bt, g, 1, 256), 256, 0, args));
   }
   CS_TRY(run_condense(bt, v));
   return run_direction(bt, v, nlvl);
@@ -1276,7 +1308,7 @@ static int get_graph(cs_batch* bt, const CsConsts& c, int nlvl, int reps) {
   const int k = use_cta_path(bt) ? 1 : 0;
   const int lo = upper_levels(bt, nlvl);
   if (bt->graph[k] && bt->graph_nlvl[k] == nlvl && bt->graph_tune[k] == bt->M->tune_ver && bt->graph_lo[k] == lo &&
-      bt->graph_refine[k] == bt->opts.refine &&
+      bt->graph_refine[k] == bt->opts.refine && bt->graph_cap[k] == bt->work_cap &&
       memcmp(&bt->graph_view[k], &v, sizeof(v)) == 0 && memcmp(&bt->graph_consts[k], &c, sizeof(c)) == 0)
     return CS_OK;
   if (bt->graph[k]) {
@@ -1305,6 +1337,7 @@ static int get_graph(cs_batch* bt, const CsConsts& c, int nlvl, int reps) {
   bt->graph_tune[k] = bt->M->tune_ver;
   bt->graph_lo[k] = lo;
   bt->graph_refine[k] = bt->opts.refine;
+  bt->graph_cap[k] = bt->work_cap;
   return CS_OK;
 }
 
@@ -1376,6 +1409,26 @@ extern "C" int cs_solve(cs_batch* bt, const cs_opts* opts) {
   const long long max_super = 10000000;
   long long steps = 0;
   const int per_launch_steps = 1;
+  // grid caps for the tail (see cs_batch::work_cap): set when at most this
+  // many instances are in Newton, tightened each time their number halves
+  const int cap_at = std::max(64, bt->B / 32);
+  auto set_cap = [&](const std::vector<CsInst>& st) {
+    long long slots = 0;
+    int n = 0;
+    for (int b = 0; b < bt->B; ++b)
+      if (st[b].status == ST_FRESH || st[b].status == ST_LS) {
+        slots += bt->hN[b];
+        ++n;
+      }
+    if (n > 0 && n <= cap_at) {
+      bt->work_cap = slots;
+      bt->inst_cap = n;
+    } else {
+      bt->work_cap = 0;
+      bt->inst_cap = 0;
+    }
+  };
+  set_cap(hi);
   for (int outer = 0; outer < 1000000 && rc == CS_OK; ++outer) {
     // ---- Newton phase: device state machine, work lists, graph replays
     const int nlvl = tree_levels(bt);
@@ -1407,6 +1460,10 @@ extern "C" int cs_solve(cs_batch* bt, const cs_opts* opts) {
       if (steps > max_super) {
         rc = set_err(CS_ERR_STATE, "Newton phase did not terminate");
         break;
+      }
+      if (use_graph && bt->h_n[0] <= cap_at && (bt->inst_cap == 0 || 2 * bt->h_n[0] <= bt->inst_cap)) {
+        if ((rc = read_inst(bt, hi)) != CS_OK) break;
+        set_cap(hi);
       }
     }
     if (rc != CS_OK) break;
@@ -1445,7 +1502,10 @@ extern "C" int cs_solve(cs_batch* bt, const cs_opts* opts) {
       any_newton = true;
     }
     if (!any_newton) break;
+    set_cap(hi);
   }
+  bt->work_cap = 0;
+  bt->inst_cap = 0;
   if (rc == CS_OK) rc = check_config(bt);
   if (rc == CS_OK) CS_CUDA(cudaStreamSynchronize(bt->stream));
   return rc;
