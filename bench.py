@@ -521,14 +521,15 @@ def run_warm(args, cs, rank, world, local_rank, cpu, cfg):
     # ---- evaluation batch, resident in HBM
     _log("trained in %.1f s (loss %.3g)" % (t_train, loss))
     held = _family_batch(cs, args.family, args.batch, 7 + 100 * rank)
-    runner = ws.WarmRunner(fam, solver, net, held)
+    runner = ws.WarmRunner(fam, solver, net, held, spares=args.spares >= 0)
+    spare_at = max(args.spares, 0.0)
     # launch-shape tuner (set-up, untimed): condensation shape per m on the batch
     tune = [dict(m=g["m"], **g["bt"].autotune(reps=3)) for g in runner.groups]
     _log("tuned condensation shapes: %s" % tune)
     ws_gb = sum(g["bt"].sizes()[1] for g in runner.groups) * 8 * 300 / 1e9
     cfg["l2"] = cfg["l2"] % ("%.1f" % ws_gb)
     for _ in range(args.warmup):
-        runner.run(warm=True, speculate=args.speculate)
+        runner.run(warm=True, speculate=args.speculate, spare_at=spare_at)
     for g in runner.groups:
         g["bt"].profile_reset(timing=False)
     _log("warm-up done; timed warm-started steps")
@@ -536,7 +537,7 @@ def run_warm(args, cs, rank, world, local_rank, cpu, cfg):
     with ClockSampler(_gpu_index(local_rank)) as clk:
         t0 = time.perf_counter()
         for _ in range(args.steps):
-            solved, n_fb, sols = runner.run(warm=True, speculate=args.speculate)
+            solved, n_fb, sols = runner.run(warm=True, speculate=args.speculate, spare_at=spare_at)
         dt = time.perf_counter() - t0
     dt = _max_over_ranks(dist, dt)
     runner_times = dict(runner.times)
@@ -570,7 +571,7 @@ def run_warm(args, cs, rank, world, local_rank, cpu, cfg):
     hosts = []
     for g in runner.groups:
         insts = runner.instances[g["first"]:g["first"] + g["n"]]
-        N, t, y, z, p, th = ws.pack_family(fam, insts)
+        N, t, y, z, p, th = ws.pack_family(fam, insts * (2 if runner.spares else 1))
         hh = {}
         for k, a in (("N", N), ("t", t), ("y", y), ("z", z), ("p", p), ("th", th)):
             pa = cs.module.PinnedArray(a.shape, a.dtype)
@@ -578,7 +579,7 @@ def run_warm(args, cs, rank, world, local_rank, cpu, cfg):
             hh[k] = pa
         cap = int(N.sum() * 4)
         out = {k: cs.module.PinnedArray(shape) for k, shape in (("t", (cap,)), ("y", (cap, fam.ny)),
-                                                                 ("z", (cap, fam.nz)), ("p", (g["n"], fam.np)))}
+                                                                 ("z", (cap, fam.nz)), ("p", (g["bt"].B, fam.np)))}
         hosts.append((hh, out))
     h2d = Xh.array.nbytes + sum(sum(a.array.nbytes for a in hh.values()) for hh, _ in hosts)
     d2h = 0
@@ -587,6 +588,9 @@ def run_warm(args, cs, rank, world, local_rank, cpu, cfg):
         # guesses from pinned host memory, warm start, solve, solutions back to
         # pinned host memory, the failed instances again from the plain guess
         bt = g["bt"]
+        n = g["n"]
+        if runner.spares:
+            bt.set_spares(n, int(spare_at * n))
         bt.set_guess_packed(hh["N"].array, hh["t"].array, hh["y"].array, hh["z"].array, hh["p"].array,
                             hh["th"].array)
         bt.warm_start(runner.dY.ptr + 4 * g["first"] * net.n_out, ws.N_NODES, net.n_out)
@@ -598,10 +602,15 @@ def run_warm(args, cs, rank, world, local_rank, cpu, cfg):
         cs._lib.check(bt._lib.cs_get_solution(bt.handle, cs._lib.dptr(out["t"].array), cs._lib.dptr(out["y"].array),
                                               cs._lib.dptr(out["z"].array), cs._lib.dptr(out["p"].array), st),
                       "cs_get_solution")
-        failed = [runner.instances[g["first"] + b] for b in range(bt.B) if st[b].status != 3]
-        n_ok = bt.B - len(failed)
-        if failed:
-            n_ok += sum(int(s["success"]) for s in solver.solve(failed))
+        status = np.ctypeslib.as_array(st)["status"]
+        if runner.spares:
+            # a failed instance takes its spare's solution (started in the same solve)
+            n_ok = int(np.count_nonzero((status[:n] == 3) | (status[n:] == 3)))
+        else:
+            failed = [runner.instances[g["first"] + b] for b in range(n) if status[b] != 3]
+            n_ok = n - len(failed)
+            if failed:
+                n_ok += sum(int(s["success"]) for s in solver.solve(failed))
         res[g["m"]] = (n_ok, 8 * T * (1 + fam.ny + fam.nz) + 8 * bt.B * fam.np + bt.B * 64)
 
     _barrier(dist)
@@ -926,8 +935,11 @@ def main():
     ap.add_argument("--epochs", type=int, default=150)
     ap.add_argument("--single-sample", type=int, default=64)
     ap.add_argument("--speculate", type=float, default=0.0,
-                    help="warm: start the plain-guess solves of the instances still iterating once at most this "
-                         "fraction of an m-group is (0: fallbacks only after the warm solve)")
+                    help="warm, without spares: start the plain-guess solves of the instances still iterating on "
+                         "a second thread once at most this fraction of an m-group is (0: after the warm solve)")
+    ap.add_argument("--spares", type=float, default=0.02,
+                    help="warm: the plain-guess copies of the instances ride in the warm batch and start once at "
+                         "most this fraction of an m-group is in Newton (negative: separate fallback solves)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--babd-path", type=int, default=0, help="0 automatic, 1 one CTA per instance, 2 per level")
     ap.add_argument("--layout", type=int, default=0,
@@ -969,12 +981,12 @@ def main():
         net = ws.Mlp(X.shape[1], Y.shape[1], width=256, depth=4, seed=0)
         net.fit_normalization(X, Y)
         net.train(X, Y, epochs=60, batch=1024, lr=1e-3, seed=0)
-        runner = ws.WarmRunner(fam, solver, net, _family_batch(cs, args.family, 2048, 7))
+        runner = ws.WarmRunner(fam, solver, net, _family_batch(cs, args.family, 2048, 7), spares=args.spares >= 0)
         # the m-groups one after another on this thread (profilers serialise
         # kernels anyway, and a single host thread keeps the capture simple)
-        runner.run(warm=True, threads=False, speculate=0)
+        runner.run(warm=True, threads=False, spare_at=max(args.spares, 0.0))
         cs._lib.check(lib.cs_profiler_start(), "cs_profiler_start")
-        solved, n_fb, _ = runner.run(warm=True, threads=False, speculate=0)
+        solved, n_fb, _ = runner.run(warm=True, threads=False, spare_at=max(args.spares, 0.0))
         cs._lib.check(lib.cs_profiler_stop(), "cs_profiler_stop")
         print("profile case ok: solved %d of 2048, %d fallbacks" % (solved, n_fb))
         return
@@ -1033,10 +1045,17 @@ def main():
     else:
         cfg = None
     if cfg is not None:
-        cfg["fallback"] = ("every instance that fails from its warm guess is solved again from the plain guess; "
-                           "those still iterating once at most %g of an m-group is are started early on a second "
-                           "thread (same results, shorter wall time)" % args.speculate
-                           if args.speculate > 0 else "after the warm solve of each m-group")
+        if args.spares >= 0:
+            cfg["fallback"] = ("every instance that fails from its warm guess is solved again from the plain guess, "
+                               "inside the same batch: each m-group batch holds every instance twice (warm and "
+                               "plain copy); the plain copies of the instances still iterating or failed start "
+                               "once at most %g of the group is in Newton, those whose warm copy succeeded stop "
+                               "(same results as solving the failed ones afterwards)" % args.spares)
+        else:
+            cfg["fallback"] = ("every instance that fails from its warm guess is solved again from the plain guess; "
+                               "those still iterating once at most %g of an m-group is are started early on a "
+                               "second thread (same results, shorter wall time)" % args.speculate
+                               if args.speculate > 0 else "after the warm solve of each m-group")
     else:
         instances = cs.workloads.vdp_batch(args.batch, seed=SEED + rank)
         cfg = {"workload": "plain batched solve: Van der Pol batch, %d instances (x0~U[-2,2]^2, T~U[2,8], "

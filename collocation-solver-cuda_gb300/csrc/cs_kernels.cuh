@@ -56,6 +56,10 @@
 #define ST_DONE 3
 #define ST_FAIL 4
 #define ST_REMESH 5
+// spares (host-managed pairing): parked with their initial guess, or stopped;
+// no kernel of the state machine takes either
+#define ST_PARKED 6
+#define ST_CANCELLED 7
 
 #define FAIL_NONE 0
 #define FAIL_ITER 1

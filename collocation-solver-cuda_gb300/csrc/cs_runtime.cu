@@ -143,8 +143,16 @@ struct CsBatchDev {
 
 static const int CS_MAXLVL = 32;
 
-enum { ST_FRESH = 0, ST_LS = 1, ST_SEG = 2, ST_DONE = 3, ST_FAIL = 4, ST_REMESH = 5 };
+enum { ST_FRESH = 0, ST_LS = 1, ST_SEG = 2, ST_DONE = 3, ST_FAIL = 4, ST_REMESH = 5, ST_PARKED = 6, ST_CANCELLED = 7 };
 enum { FAIL_NONE = 0, FAIL_ITER = 1, FAIL_NODES = 2, FAIL_MESH = 3 };
+
+// the record of an instance starting Newton at continuation parameter alpha0
+__host__ __device__ inline void init_inst(CsInst& s, double alpha0) {
+  memset(&s, 0, sizeof(s));
+  s.status = ST_FRESH;
+  s.alpha = alpha0;
+  s.alpha_ls = 1.0;
+}
 
 uint64_t fnv1a(const std::string& s, uint64_t h = 1469598103934665603ull) {
   for (unsigned char c : s) {
@@ -267,6 +275,28 @@ __global__ void k_warm_fill(int B, int ny, int nz, int np, int n_nodes, const fl
   if (threadIdx.x == 0) {
     const float* vp = v + (size_t)n_nodes * (ny + nz);
     for (int c = 0; c < np; ++c) p[(size_t)b * np + c] = (double)vp[c];
+  }
+}
+
+// One thread per primary k (spare n + k): start the parked spare of a primary
+// still in Newton or failed, stop the running spare of a primary that
+// succeeded.  counts[0] / counts[1]: spares started / stopped.
+__global__ void k_spares(int n, CsInst* inst, double alpha0, int* counts) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const int ps = inst[k].status;
+  CsInst& q = inst[n + k];
+  const int ss = q.status;
+  if (ss == ST_PARKED && (ps == ST_FRESH || ps == ST_LS || ps == ST_FAIL)) {
+    CsInst f;
+    init_inst(f, alpha0);
+    q = f;
+    atomicAdd(&counts[0], 1);
+  } else if (ps == ST_DONE && (ss == ST_FRESH || ss == ST_LS || ss == ST_SEG)) {
+    q.status = ST_CANCELLED;
+    q.need_jac = 0;
+    q.accepted = 0;
+    atomicAdd(&counts[1], 1);
   }
 }
 
@@ -712,7 +742,7 @@ struct cs_batch {
   cs_opts opts;
   // work lists
   DBuf l_act, l_jac, l_acc, l_actp, l_jacp, l_accp, l_lvlp, l_n;
-  int* h_n = nullptr;  // pinned copy of nlist
+  int* h_n = nullptr;  // pinned copy of nlist (8 ints: the lists' counts, then k_spares' counts)
   cs_progress_fn progress = nullptr;
   void* progress_user = nullptr;
   // captured super-step, one graph per Newton-direction path (0 per level,
@@ -731,6 +761,10 @@ struct cs_batch {
   long long work_cap = 0;
   int inst_cap = 0;
   long long graph_cap[2] = {-1, -1};
+  // spares (cs_batch_set_spares): instance n_primary + k backs up instance k;
+  // started once at most spare_trigger instances are in Newton (< 0: never)
+  int n_primary = 0;
+  int spare_trigger = -1;
   CsBatchDev graph_view[2];
   CsConsts graph_consts[2];
   // device copy of the last initial guess (cs_batch_reset)
@@ -1115,7 +1149,7 @@ extern "C" int cs_batch_create(cs_module* M, int batch, long long node_capacity,
       (rc = dalloc(bt->l_jacp, (batch + 1) * sizeof(long long))) ||
       (rc = dalloc(bt->l_accp, (batch + 1) * sizeof(long long))) ||
       (rc = dalloc(bt->l_lvlp, (size_t)CS_MAXLVL * (batch + 1) * sizeof(long long))) ||
-      (rc = dalloc(bt->l_n, 4 * sizeof(int))) ||
+      (rc = dalloc(bt->l_n, 8 * sizeof(int))) ||
       (rc = alloc_slots(bt, std::max<long long>(node_capacity, 2 * batch), false)) ||
       (M->big && (rc = dalloc(bt->wsp, (size_t)M->big_ctas * M->slab * d)))) {
     cs_batch_free(bt);
@@ -1154,11 +1188,12 @@ extern "C" void cs_batch_free(cs_batch* bt) {
   delete bt;
 }
 
-static void init_inst(CsInst& s, double alpha0) {
-  memset(&s, 0, sizeof(s));
-  s.status = ST_FRESH;
-  s.alpha = alpha0;
-  s.alpha_ls = 1.0;
+
+// every instance fresh, the spares parked
+static void init_insts(const cs_batch* bt, std::vector<CsInst>& hi) {
+  for (auto& s : hi) init_inst(s, bt->opts.alpha0);
+  if (bt->n_primary > 0)
+    for (int b = bt->n_primary; b < bt->B; ++b) hi[b].status = ST_PARKED;
 }
 
 extern "C" int cs_batch_set_guess(cs_batch* bt, const int* N, const double* t, const double* y, const double* z,
@@ -1206,7 +1241,7 @@ extern "C" int cs_batch_set_guess(cs_batch* bt, const int* N, const double* t, c
   bt->ihoff = bt->hoff;
   bt->iT = (int)T;
   std::vector<CsInst> hi(bt->B);
-  for (auto& s : hi) init_inst(s, bt->opts.alpha0);
+  init_insts(bt, hi);
   CS_CUDA(cudaMemcpyAsync(bt->dinst.p, hi.data(), hi.size() * sizeof(CsInst), cudaMemcpyHostToDevice, st));
   CS_TRY(fill_inst_of(bt));
   CsBatchDev v = devview(bt);
@@ -1259,7 +1294,7 @@ extern "C" int cs_batch_set_state(cs_batch* bt, const int* N, const double* t, c
   if (M->np > 0) CS_CUDA(cudaMemcpyAsync(bt->dp.p, p, (size_t)bt->B * M->np * d, cudaMemcpyHostToDevice, st));
   if (M->nth > 0) CS_CUDA(cudaMemcpyAsync(bt->dth.p, theta, (size_t)bt->B * M->nth * d, cudaMemcpyHostToDevice, st));
   std::vector<CsInst> hi(bt->B);
-  for (auto& s : hi) init_inst(s, bt->opts.alpha0);
+  init_insts(bt, hi);
   CS_CUDA(cudaMemcpyAsync(bt->dinst.p, hi.data(), hi.size() * sizeof(CsInst), cudaMemcpyHostToDevice, st));
   CS_TRY(fill_inst_of(bt));
   CS_CUDA(cudaStreamSynchronize(st));
@@ -1404,7 +1439,7 @@ extern "C" int cs_solve(cs_batch* bt, const cs_opts* opts) {
     s.alpha = o.alpha0;
   }
   CS_TRY(write_inst(bt, hi));
-  if (!bt->h_n) CS_CUDA(cudaMallocHost(&bt->h_n, 4 * sizeof(int)));
+  if (!bt->h_n) CS_CUDA(cudaMallocHost(&bt->h_n, 8 * sizeof(int)));
   int rc = CS_OK;
   const long long max_super = 10000000;
   long long steps = 0;
@@ -1429,6 +1464,41 @@ extern "C" int cs_solve(cs_batch* bt, const cs_opts* opts) {
     }
   };
   set_cap(hi);
+  // spares (cs_batch_set_spares): from the check at which at most
+  // spare_trigger instances are in Newton on, every check starts and stops
+  // spares (k_spares).  Started spares need the residual list rebuilt and,
+  // if they outgrow the grid caps, larger caps.  A stopped spare needs
+  // nothing: every kernel skips it, and the next super-step's lists drop it.
+  // A spare starts at most once, so the solve still ends.
+  const bool spares = bt->n_primary > 0 && bt->spare_trigger >= 0;
+  bool spares_on = false;
+  auto spare_pass = [&](bool reread) -> int {
+    int* dcount = (int*)bt->l_n.p + 4;
+    CS_CUDA(cudaMemsetAsync(dcount, 0, 2 * sizeof(int), bt->stream));
+    k_spares<<<cdiv(bt->n_primary, 128), 128, 0, bt->stream>>>(bt->n_primary, (CsInst*)bt->dinst.p, o.alpha0,
+                                                               dcount);
+    CS_CUDA(cudaGetLastError());
+    bt->launches += 1;
+    CS_CUDA(cudaMemcpyAsync(bt->h_n + 4, dcount, 2 * sizeof(int), cudaMemcpyDeviceToHost, bt->stream));
+    CS_CUDA(cudaStreamSynchronize(bt->stream));
+    if (bt->h_n[4] > 0) {
+      CsBatchDev vl = devview(bt);
+      CS_TRY(run_lists(bt, vl, 0, 0));
+      CS_CUDA(cudaMemcpyAsync(bt->h_n, bt->l_n.p, sizeof(int), cudaMemcpyDeviceToHost, bt->stream));
+      CS_TRY(read_inst(bt, hi));
+      long long slots = 0;
+      int n = 0;
+      for (int b = 0; b < bt->B; ++b)
+        if (hi[b].status == ST_FRESH || hi[b].status == ST_LS) {
+          slots += bt->hN[b];
+          ++n;
+        }
+      if (bt->work_cap > 0 && (slots > bt->work_cap || n > bt->inst_cap)) set_cap(hi);
+    } else if (bt->h_n[5] > 0 && reread) {
+      CS_TRY(read_inst(bt, hi));
+    }
+    return CS_OK;
+  };
   for (int outer = 0; outer < 1000000 && rc == CS_OK; ++outer) {
     // ---- Newton phase: device state machine, work lists, graph replays
     const int nlvl = tree_levels(bt);
@@ -1456,6 +1526,10 @@ extern "C" int cs_solve(cs_batch* bt, const cs_opts* opts) {
         break;
       }
       if (bt->progress) bt->progress(bt->progress_user, bt->h_n[0], steps);
+      if (spares && (spares_on || bt->h_n[0] <= bt->spare_trigger)) {
+        spares_on = true;
+        if ((rc = spare_pass(false)) != CS_OK) break;
+      }
       if (bt->h_n[0] == 0) break;
       if (steps > max_super) {
         rc = set_err(CS_ERR_STATE, "Newton phase did not terminate");
@@ -1501,6 +1575,14 @@ extern "C" int cs_solve(cs_batch* bt, const cs_opts* opts) {
       if ((rc = write_inst(bt, hi)) != CS_OK) break;
       any_newton = true;
     }
+    // spares of the primaries that failed or succeeded in this mesh phase;
+    // at the end of the solve, of every failed primary
+    if (spares && (spares_on || !any_newton)) {
+      spares_on = true;
+      if ((rc = spare_pass(true)) != CS_OK) break;
+      if (bt->h_n[4] > 0)
+        for (auto& s : hi) any_newton |= (s.status == ST_FRESH || s.status == ST_LS);
+    }
     if (!any_newton) break;
     set_cap(hi);
   }
@@ -1509,6 +1591,25 @@ extern "C" int cs_solve(cs_batch* bt, const cs_opts* opts) {
   if (rc == CS_OK) rc = check_config(bt);
   if (rc == CS_OK) CS_CUDA(cudaStreamSynchronize(bt->stream));
   return rc;
+}
+
+extern "C" int cs_batch_set_spares(cs_batch* bt, int n_primary, int trigger) {
+  if (!bt) return set_err(CS_ERR_INVALID, "cs_batch_set_spares: null batch");
+  if (n_primary < 0 || (n_primary > 0 && 2LL * n_primary != bt->B))
+    return set_err(CS_ERR_INVALID, "cs_batch_set_spares: the batch must hold 2 * n_primary instances");
+  const bool paired = n_primary != bt->n_primary;
+  bt->n_primary = n_primary;
+  bt->spare_trigger = trigger;
+  if (n_primary == 0 || !paired || !bt->have_guess) return CS_OK;
+  // park the spares that have not started since their guess was set
+  std::vector<CsInst> hi;
+  CS_TRY(read_inst(bt, hi));
+  for (int b = n_primary; b < bt->B; ++b)
+    if (hi[b].status == ST_FRESH && hi[b].residual_count == 0 && hi[b].jac_count == 0 && hi[b].remesh_count == 0)
+      hi[b].status = ST_PARKED;
+  CS_TRY(write_inst(bt, hi));
+  CS_CUDA(cudaStreamSynchronize(bt->stream));
+  return CS_OK;
 }
 
 extern "C" int cs_batch_set_progress(cs_batch* bt, cs_progress_fn fn, void* user) {
@@ -1789,7 +1890,7 @@ extern "C" int cs_batch_reset(cs_batch* bt) {
   if (M->nz > 0) CS_CUDA(cudaMemcpyAsync(bt->znode[0].p, bt->iz.p, T * M->nz * d, cudaMemcpyDeviceToDevice, st));
   if (M->np > 0) CS_CUDA(cudaMemcpyAsync(bt->dp.p, bt->ip.p, (size_t)bt->B * M->np * d, cudaMemcpyDeviceToDevice, st));
   std::vector<CsInst> hi(bt->B);
-  for (auto& s : hi) init_inst(s, bt->opts.alpha0);
+  init_insts(bt, hi);
   CS_CUDA(cudaMemcpyAsync(bt->dinst.p, hi.data(), hi.size() * sizeof(CsInst), cudaMemcpyHostToDevice, st));
   CS_TRY(fill_inst_of(bt));
   CsBatchDev v = devview(bt);
@@ -1805,12 +1906,15 @@ extern "C" int cs_batch_warm_start(cs_batch* bt, int n_nodes, const float* traj,
   cs_module* M = bt->M;
   if (stride < n_nodes * (M->ny + M->nz) + M->np) return set_err(CS_ERR_INVALID, "cs_batch_warm_start: stride too small");
   const int s = bt->cur;
-  k_warm_fill<<<bt->B, 128, 0, bt->stream>>>(bt->B, M->ny, M->nz, M->np, n_nodes, traj, stride, (const int*)bt->dN.p,
-                                             (const int*)bt->doff.p, (const double*)bt->t[s].p, (double*)bt->y[s].p,
-                                             (double*)bt->znode[s].p, (double*)bt->dp.p);
+  // with spares only the primaries take the trajectories; the spares keep
+  // their records (parked) and guesses
+  const int nf = bt->n_primary > 0 ? bt->n_primary : bt->B;
+  k_warm_fill<<<nf, 128, 0, bt->stream>>>(nf, M->ny, M->nz, M->np, n_nodes, traj, stride, (const int*)bt->dN.p,
+                                          (const int*)bt->doff.p, (const double*)bt->t[s].p, (double*)bt->y[s].p,
+                                          (double*)bt->znode[s].p, (double*)bt->dp.p);
   CS_CUDA(cudaGetLastError());
   bt->launches += 1;
-  std::vector<CsInst> hi(bt->B);
+  std::vector<CsInst> hi(nf);
   for (auto& q : hi) init_inst(q, bt->opts.alpha0);
   CS_CUDA(cudaMemcpyAsync(bt->dinst.p, hi.data(), hi.size() * sizeof(CsInst), cudaMemcpyHostToDevice, bt->stream));
   CsBatchDev v = devview(bt);

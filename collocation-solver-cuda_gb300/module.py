@@ -264,10 +264,11 @@ class Batch:
 
     def statuses(self):
         """Per-instance status codes (0 fresh, 1 line search, 2 segment
-        residual, 3 done, 4 failed, 5 remesh) without copying the solution."""
+        residual, 3 done, 4 failed, 5 remesh, 6 parked spare, 7 stopped
+        spare) without copying the solution."""
         st = (_lib.Stats * self.B)()
         _lib.check(self._lib.cs_get_solution(self.handle, None, None, None, None, st), "cs_get_solution")
-        return np.array([s.status for s in st], dtype=np.int32)
+        return np.ctypeslib.as_array(st)["status"].astype(np.int32)
 
     # ---- data out
     def sizes(self):
@@ -288,12 +289,14 @@ class Batch:
                    "cs_get_solution")
         return N, t, y, z[:, :cp.nz], p[:, :cp.np], st
 
-    def solution(self):
-        N, t, y, z, p, st = self.solution_packed()
+    def solution(self, indices=None, packed=None):
+        """Per-instance solution dicts, of every instance or of `indices`
+        (from `packed`, a solution_packed() result, if given)."""
+        N, t, y, z, p, st = self.solution_packed() if packed is None else packed
+        off = np.concatenate(([0], np.cumsum(N, dtype=np.int64)))
         out = []
-        o = 0
-        for b in range(self.B):
-            n = int(N[b])
+        for b in (range(self.B) if indices is None else indices):
+            o, n = int(off[b]), int(N[b])
             s = st[b]
             out.append(dict(N=n, t=t[o:o + n], y=y[o:o + n], z=z[o:o + n], p=p[b],
                             status=int(s.status), success=int(s.status) == 3, newton_steps=int(s.newton_steps),
@@ -301,7 +304,6 @@ class Batch:
                             remeshes=int(s.remeshes), continuation_steps=int(s.continuation_steps),
                             alpha=float(s.alpha), max_residual=float(s.max_residual), last_norm=float(s.last_norm),
                             singular=int(s.singular), fail_reason=int(s.fail_reason)))
-            o += n
         return out
 
     def state(self):
@@ -365,6 +367,17 @@ class Batch:
         ptr = traj_dev.ptr if isinstance(traj_dev, DeviceArray) else traj_dev
         _lib.check(self._lib.cs_batch_warm_start(self.handle, int(n_nodes), ctypes.c_void_p(ptr), int(stride)),
                    "cs_batch_warm_start")
+
+    def set_spares(self, n_primary, trigger):
+        """Pair instance k < n_primary (the primary) with instance
+        n_primary + k (its spare: the same instance from another guess) on a
+        batch of 2 n_primary instances.  Spares stay parked until at most
+        `trigger` instances are in Newton (never if trigger < 0); from then on
+        the spare of every primary still iterating or failed runs in the same
+        super-steps, and every failed primary's spare has run when solve()
+        returns.  warm_start() then fills only the primaries.  n_primary = 0
+        removes the pairing."""
+        _lib.check(self._lib.cs_batch_set_spares(self.handle, int(n_primary), int(trigger)), "cs_batch_set_spares")
 
     def autotune(self, reps=3):
         """Time the condensation's launch shapes on this batch's intervals and

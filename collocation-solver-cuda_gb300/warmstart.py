@@ -273,11 +273,17 @@ class WarmRunner:
     """Device-resident warm-started batch solve of a fixed list of instances:
     features and plain guesses live in HBM; each run resets the batches,
     predicts the trajectories, fills the guesses on the device, solves, and
-    solves the failed instances again from the plain guess."""
+    solves the failed instances again from the plain guess.
 
-    def __init__(self, family, solver, mlp, instances):
+    spares: each m-group's batch also holds every instance a second time
+    from the plain guess, paired with its warm-started copy (Batch.set_spares):
+    the fallback solves then run inside the warm solve's own super-steps
+    instead of after it."""
+
+    def __init__(self, family, solver, mlp, instances, spares=False):
         from .module import DeviceArray
         self.family, self.solver, self.mlp = family, solver, mlp
+        self.spares = bool(spares)
         order = sorted(range(len(instances)), key=lambda k: instances[k].m)
         self.instances = [instances[k] for k in order]
         self.order = order
@@ -296,14 +302,25 @@ class WarmRunner:
                 meshes.append((t, y0, z0))
                 ps.append(p0)
                 ths.append(family.theta(self.instances[k]))
-            bt = Batch(solver.cp(m), len(idx))
-            bt.set_guess(meshes, np.array(ps).reshape(len(idx), -1), np.array(ths).reshape(len(idx), -1))
-            self.groups.append(dict(m=m, first=start, n=len(idx), bt=bt))
+            n = len(idx)
+            copies = 2 if self.spares else 1
+            bt = Batch(solver.cp(m), copies * n)
+            bt.set_guess(meshes * copies, np.array(ps * copies).reshape(copies * n, -1),
+                         np.array(ths * copies).reshape(copies * n, -1))
+            if self.spares:
+                bt.set_spares(n, -1)
+            self.groups.append(dict(m=m, first=start, n=n, bt=bt))
             start += len(idx)
 
-    def run(self, warm=True, fallback=True, threads=True, speculate=0.0):
+    def run(self, warm=True, fallback=True, threads=True, speculate=0.0, spare_at=0.02):
         """One solve of every instance; returns (solved, fallback count, stats).
         self.times holds the seconds of the phases of the last run.
+
+        spare_at (runners built with spares): the spares start once no more
+        than this fraction of a group is in the Newton iteration.  Every
+        instance's result is independent of its batch-mates and of when its
+        spare started, so the outcome is the one of falling back after the
+        warm solve.
 
         speculate: once no more than this fraction of a group is still in the
         Newton iteration, the instances still iterating are solved from the
@@ -327,11 +344,13 @@ class WarmRunner:
 
         def one(g):
             bt = g["bt"]
+            if self.spares:
+                bt.set_spares(g["n"], max(0, int(spare_at * g["n"])) if warm and fallback else -1)
             bt.reset()
             if warm:
                 bt.warm_start(self.dY.ptr + 4 * g["first"] * self.mlp.n_out, N_NODES, self.mlp.n_out)
             spec = {}
-            if warm and fallback and speculate > 0:
+            if warm and fallback and speculate > 0 and not self.spares:
                 limit = max(1, int(speculate * g["n"]))
 
                 def side(ks):
@@ -359,6 +378,23 @@ class WarmRunner:
             finally:
                 bt.set_progress(None)
             g["t_solve"] = time.perf_counter() - t1
+            if self.spares:
+                n = g["n"]
+                packed = bt.solution_packed()
+                st = np.ctypeslib.as_array(packed[5])["status"]
+                failed = [int(k) for k in np.flatnonzero(st[:n] != 3)] if warm and fallback else []
+                for k in failed:
+                    if st[n + k] not in (3, 4):
+                        raise RuntimeError("spare of failed instance %d did not run (status %d)" % (k, st[n + k]))
+                sols = bt.solution(list(range(n)) + [n + k for k in failed], packed=packed)
+                g["sols"] = sols[:n]
+                for j, k in enumerate(failed):
+                    g["sols"][k] = dict(sols[n + j], fallback=True)
+                g["fallback"] = failed
+                g["speculated"] = int(np.count_nonzero(st[n:] != 6))
+                g["t_spec"] = None
+                g["t_done"] = time.perf_counter() - t1
+                return
             g["sols"] = bt.solution()
             if "thread" in spec:
                 spec["thread"].join()

@@ -38,6 +38,11 @@ extern "C" {
 /* per-instance status after cs_solve (matches the device state machine) */
 #define CS_STATUS_DONE 3
 #define CS_STATUS_FAIL 4
+/* spare instance not started (holds its initial guess), and spare stopped
+ * because its primary succeeded (its state is then undefined); see
+ * cs_batch_set_spares */
+#define CS_STATUS_PARKED 6
+#define CS_STATUS_CANCELLED 7
 
 typedef struct cs_module cs_module;
 typedef struct cs_batch cs_batch;
@@ -324,6 +329,27 @@ int cs_mlp_predict_device(cs_mlp* mlp, const float* dX, int n, float* dY, void* 
  * (OCP2ABVP.py:402-447) as the Newton initial guess; no reference
  * counterpart. */
 int cs_batch_warm_start(cs_batch* bt, int n_nodes, const float* traj, int stride);
+
+/* Fallback inside the batch.  With n_primary > 0 the batch (B = 2 n_primary
+ * instances) pairs instance k < n_primary, the primary, with instance
+ * n_primary + k, its spare: the same problem instance from another initial
+ * guess (normally the plain one, with the primary warm-started).  Spares are
+ * parked (CS_STATUS_PARKED, untouched by every kernel) by cs_batch_set_guess,
+ * cs_batch_set_state and cs_batch_reset, and by this call when it changes the
+ * pairing (the spares not started since their guess was set); and
+ * cs_batch_warm_start fills only the primaries (traj holds n_primary rows).
+ * During cs_solve, once at most `trigger` instances are in the Newton
+ * iteration, the spare of every primary still iterating or failed starts from
+ * its initial guess in the same super-steps as the rest of the batch, and a
+ * spare whose primary has succeeded is stopped (CS_STATUS_CANCELLED); before
+ * cs_solve returns, the spare of every failed primary has run.  A started
+ * spare's result is the one of solving it alone from its initial guess, so a
+ * primary that fails takes its spare's solution: the outcome of solving the
+ * failed instances again afterwards, in one pass.  trigger < 0 keeps the
+ * spares parked; n_primary = 0 removes the pairing (instances parked stay so
+ * until the next set_guess / reset).  No reference counterpart (the reference
+ * solves one initial guess per call, CS:36-251). */
+int cs_batch_set_spares(cs_batch* bt, int n_primary, int trigger);
 
 /* Device memory for callers of the device-pointer entry points. */
 void* cs_device_alloc(size_t bytes);

@@ -155,8 +155,9 @@ def test_guess_and_solution_files_round_trip(tmp_path):
 
 def test_speculative_fallback_gives_the_sequential_results():
     """Starting the plain-guess solves early (for every instance still
-    iterating, at the first check or once 3 % of a group is) changes no
-    instance's result against falling back after the warm solve."""
+    iterating, at the first check or once 3 % of a group is), on a second
+    thread or as spares inside the warm batch, changes no instance's result
+    against falling back after the warm solve."""
     cs = pkg()
     ws = cs.warmstart
     fam = ws.vdp_family()
@@ -171,16 +172,34 @@ def test_speculative_fallback_gives_the_sequential_results():
     runner = ws.WarmRunner(fam, solver, net, insts)
     base = runner.run(warm=True, speculate=0)
     assert base[1] > 0
-    for frac in (1.0, 0.03):
-        got = runner.run(warm=True, speculate=frac)
+    def same(got):
         assert got[:2] == base[:2]
-        if frac == 1.0:
-            assert sum(n for _, n, _ in runner.times["speculated"]) >= base[1]
         for a, b in zip(got[2], base[2]):
             assert (a["success"], a.get("fallback", False), a["newton_steps"], a["residual_evals"], a["N"]) == \
                    (b["success"], b.get("fallback", False), b["newton_steps"], b["residual_evals"], b["N"])
             np.testing.assert_array_equal(a["y"], b["y"])
             np.testing.assert_array_equal(a["t"], b["t"])
+
+    for frac in (1.0, 0.03):
+        got = runner.run(warm=True, speculate=frac)
+        if frac == 1.0:
+            assert sum(n for _, n, _ in runner.times["speculated"]) >= base[1]
+        same(got)
+    # the plain copies inside the warm batch (spares): started at the first
+    # check, once 3 % of a group is in Newton, or once none is
+    paired = ws.WarmRunner(fam, solver, net, insts, spares=True)
+    for at in (1.0, 0.03, 0.0):
+        got = paired.run(warm=True, spare_at=at)
+        started = sum(n for _, n, _ in paired.times["speculated"])
+        assert started >= base[1]
+        same(got)
+    # without the warm start the spares stay parked: the plain batched solve
+    plain = runner.run(warm=False)
+    got = paired.run(warm=False)
+    assert got[:2] == plain[:2] and sum(n for _, n, _ in paired.times["speculated"]) == 0
+    for a, b in zip(got[2], plain[2]):
+        assert (a["newton_steps"], a["N"]) == (b["newton_steps"], b["N"])
+        np.testing.assert_array_equal(a["y"], b["y"])
 
 
 def _held_out_sample(cs, per_m, seed):
