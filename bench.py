@@ -937,9 +937,11 @@ def main():
     ap.add_argument("--speculate", type=float, default=0.0,
                     help="warm, without spares: start the plain-guess solves of the instances still iterating on "
                          "a second thread once at most this fraction of an m-group is (0: after the warm solve)")
-    ap.add_argument("--spares", type=float, default=0.02,
+    ap.add_argument("--spares", type=float, default=-1.0,
                     help="warm: the plain-guess copies of the instances ride in the warm batch and start once at "
-                         "most this fraction of an m-group is in Newton (negative: separate fallback solves)")
+                         "most this fraction of an m-group is in Newton, e.g. 0.005 (negative, the default: "
+                         "separate fallback solves, 1-2 %% faster on the 8192-instance batch, where the GPU is busy "
+                         "to the end of the step; the spares are ~10 %% faster on 2048)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--babd-path", type=int, default=0, help="0 automatic, 1 one CTA per instance, 2 per level")
     ap.add_argument("--layout", type=int, default=0,
