@@ -8,8 +8,10 @@ A warm-started solve is accepted only when it meets the tolerance; any
 instance whose warm-started Newton iteration fails is solved again from the
 plain initial guess (fallback).
 """
+import collections
 import ctypes
 import sys
+import threading
 
 import numpy as np
 
@@ -193,13 +195,38 @@ def pack_family(family, instances):
 
 class BatchSolver:
     """Solves lists of instances of a family in one batch per m; compiled
-    problems are kept per m."""
+    problems are kept per m, and idle batches per (m, instance count), so a
+    repeated solve of as many instances (the fallbacks of a warm-started
+    batch) sets its guesses into device buffers it already has instead of
+    allocating and freeing them (cudaFree waits for the whole device)."""
+
+    _KEEP = 8  # idle batches kept, least recently used dropped first
 
     def __init__(self, family, opts=None, layout=0):
         self.family = family
         self.compiled = {}
         self.layout = layout
         self.opts = opts if opts is not None else default_opts(family.problem, max_nodes=20000)
+        self._idle = collections.OrderedDict()
+        self._lock = threading.Lock()
+
+    def _take(self, m, n):
+        with self._lock:
+            free = self._idle.get((m, n))
+            if free:
+                self._idle.move_to_end((m, n))
+                return free.pop()
+        return Batch(self.cp(m), n)
+
+    def _give(self, m, n, bt):
+        with self._lock:
+            self._idle.setdefault((m, n), []).append(bt)
+            self._idle.move_to_end((m, n))
+            while sum(len(v) for v in self._idle.values()) > self._KEEP:
+                k, v = next(iter(self._idle.items()))
+                v.pop(0)
+                if not v:
+                    del self._idle[k]
 
     def cp(self, m):
         if m not in self.compiled:
@@ -222,11 +249,12 @@ class BatchSolver:
                 meshes.append((t, y0, z0))
                 ps.append(p0)
                 ths.append(fam.theta(inst))
-            bt = Batch(self.cp(m), len(idx))
+            bt = self._take(m, len(idx))
             bt.set_guess(meshes, np.array(ps).reshape(len(idx), -1), np.array(ths).reshape(len(idx), -1))
             bt.solve(self.opts)
             for k, s in zip(idx, bt.solution()):
                 out[k] = s
+            self._give(m, len(idx), bt)
         return out
 
 
