@@ -603,15 +603,20 @@ def run_warm(args, cs, rank, world, local_rank, cpu, cfg):
                                               cs._lib.dptr(out["z"].array), cs._lib.dptr(out["p"].array), st),
                       "cs_get_solution")
         status = np.ctypeslib.as_array(st)["status"]
+        d2h_fb = h2d_fb = 0
         if runner.spares:
             # a failed instance takes its spare's solution (started in the same solve)
             n_ok = int(np.count_nonzero((status[:n] == 3) | (status[n:] == 3)))
         else:
+            # the failed instances again from the plain guess (host-built guesses
+            # in, solutions out: counted with the step's bytes)
             failed = [runner.instances[g["first"] + b] for b in range(n) if status[b] != 3]
             n_ok = n - len(failed)
-            if failed:
-                n_ok += sum(int(s["success"]) for s in solver.solve(failed))
-        res[g["m"]] = (n_ok, 8 * T * (1 + fam.ny + fam.nz) + 8 * bt.B * fam.np + bt.B * 64)
+            for i, s in zip(failed, solver.solve(failed) if failed else []):
+                n_ok += int(s["success"])
+                d2h_fb += s["t"].nbytes + s["y"].nbytes + s["z"].nbytes + s["p"].nbytes + 64
+                h2d_fb += sum(a.nbytes for a in fam.plain_guess(i)) + 8 * len(fam.theta(i))
+        res[g["m"]] = (n_ok, 8 * T * (1 + fam.ny + fam.nz) + 8 * bt.B * fam.np + bt.B * 64 + d2h_fb, h2d_fb)
 
     _barrier(dist)
     t0 = time.perf_counter()
@@ -628,9 +633,10 @@ def run_warm(args, cs, rank, world, local_rank, cpu, cfg):
             raise RuntimeError("end-to-end step: an m-group failed")
         n_e2e = sum(v[0] for v in res.values())
         d2h = sum(v[1] for v in res.values())
+        h2d_fb = sum(v[2] for v in res.values())
     dte = _max_over_ranks(dist, time.perf_counter() - t0)
-    e2e = {"value": _sum_over_ranks(dist, args.steps * n_e2e) / dte, "unit": "solves/s", "h2d_bytes_per_step": h2d,
-           "d2h_bytes_per_step": d2h}
+    e2e = {"value": _sum_over_ranks(dist, args.steps * n_e2e) / dte, "unit": "solves/s",
+           "h2d_bytes_per_step": h2d + h2d_fb, "d2h_bytes_per_step": d2h}
     roof = _roofline([(g["m"], g["bt"]) for g in runner.groups], fp64_peak)
     roof["peak_measurement"] = peak_clock
     if rank == 0:

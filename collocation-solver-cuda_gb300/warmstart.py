@@ -432,6 +432,9 @@ class WarmRunner:
             if "error" in spec:
                 raise spec["error"]
             if warm and fallback:
+                # (a second thread for these solves while this one downloads
+                # the batch's solutions was measured slower: 0.574 s per step
+                # against 0.553 s)
                 failed = [k for k, s in enumerate(g["sols"]) if not s["success"]]
                 have = dict(zip(spec.get("ks", []), spec.get("sols", [])))
                 rest = [k for k in failed if k not in have]
