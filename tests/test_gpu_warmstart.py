@@ -276,3 +276,58 @@ def test_warm_started_bench_instances_match_oracle_from_the_same_guess(vdp_net):
     print("warm vs plain-guess oracle: %d of %d on the same final mesh, max difference %.3g of scale"
           % (same_mesh, len(sols), worst))
     assert worst <= 1e-6
+
+
+def test_spares_parked_filled_and_started_at_the_end():
+    """The spare half of a paired batch (cs_batch_set_spares) is parked by the
+    guess, keeps its guess through the warm start, stays parked in a solve
+    with trigger < 0, and, with a trigger of 0 in a later solve, runs exactly
+    for the failed primaries (a short iteration limit makes failures): each
+    such spare equals the plain solve of its instance, bit for bit; the
+    spares of succeeded primaries stay parked."""
+    cs = pkg()
+    ws = cs.warmstart
+    fam = ws.vdp_family()
+    insts = [i for i in cs.workloads.vdp_batch(64, seed=29, n_range=(32, 96)) if i.m == 4]
+    n = len(insts)
+    opts = cs.default_opts(fam.problem, max_nodes=20000, max_iter=6)
+    solver = ws.BatchSolver(fam, opts)
+    net = ws.Mlp(4, fam.n_out, width=64, depth=3, seed=3)
+    X = np.array([fam.features(i) for i in insts], np.float32)
+    rng = np.random.default_rng(1)
+    net.fit_normalization(X, (1.5 * rng.standard_normal((n, fam.n_out))).astype(np.float32))
+    N, t, y, z, p, th = ws.pack_family(fam, insts + insts)
+    bt = cs.Batch(solver.cp(4), 2 * n)
+    with pytest.raises(cs._lib.CsError):
+        bt.set_spares(n + 1, 0)
+    bt.set_spares(n, -1)
+    bt.set_guess_packed(N, t, y, z, p, th)
+    st = bt.statuses()
+    assert (st[:n] == 0).all() and (st[n:] == 6).all()
+    dX = cs.module.DeviceArray(X.shape, np.float32)
+    dX.upload(X)
+    dY = cs.module.DeviceArray((n, net.n_out), np.float32)
+    net.predict_device(dX, n, dY)
+    bt.warm_start(dY, ws.N_NODES, net.n_out)
+    s0 = bt.state()
+    o = int(N[:n].sum())
+    np.testing.assert_array_equal(s0["y"][o:], y[o:])
+    assert not np.array_equal(s0["y"][:o], y[:o])
+    bt.solve(opts)
+    st = bt.statuses()
+    assert (st[n:] == 6).all() and set(st[:n].tolist()) <= {3, 4}
+    failed = [int(k) for k in np.flatnonzero(st[:n] == 4)]
+    done = [int(k) for k in np.flatnonzero(st[:n] == 3)]
+    assert failed
+    bt.set_spares(n, 0)
+    bt.solve(opts)
+    st = bt.statuses()
+    assert set(st[[n + k for k in failed]].tolist()) <= {3, 4}
+    assert (st[[n + k for k in done]] == 6).all()
+    sols = bt.solution([n + k for k in failed])
+    ref = solver.solve([insts[k] for k in failed])
+    for a, b in zip(sols, ref):
+        assert (a["status"], a["newton_steps"], a["residual_evals"], a["N"]) == \
+               (b["status"], b["newton_steps"], b["residual_evals"], b["N"])
+        np.testing.assert_array_equal(a["t"], b["t"])
+        np.testing.assert_array_equal(a["y"], b["y"])
