@@ -637,6 +637,9 @@ def run_warm(args, cs, rank, world, local_rank, cpu, cfg):
     dte = _max_over_ranks(dist, time.perf_counter() - t0)
     e2e = {"value": _sum_over_ranks(dist, args.steps * n_e2e) / dte, "unit": "solves/s",
            "h2d_bytes_per_step": h2d + h2d_fb, "d2h_bytes_per_step": d2h}
+    # ---- solution files of the whole batch: formatted on the GPU
+    #      (cs_format_solutions) against the host writer on a sample
+    files = _solution_files_rate(cs, runner)
     roof = _roofline([(g["m"], g["bt"]) for g in runner.groups], fp64_peak)
     roof["peak_measurement"] = peak_clock
     if rank == 0:
@@ -650,6 +653,7 @@ def run_warm(args, cs, rank, world, local_rank, cpu, cfg):
                 "plain_single_gpu": {"value": plain_single, "unit": "solves/s",
                                      "sample": "%d random instances of the batch, one Batch of 1 each" % len(sample)},
                 "speedup_vs_plain_single_gpu": value / plain_single if plain_single else None,
+                "solution_files": files,
                 "warm_start": {"solved": solved, "of": len(held), "fallbacks": n_fb, "phase_s": runner_times,
                                "fallback_rate": n_fb / len(held), "newton_steps_per_solve": float(newton_warm),
                                "train_solutions": int(len(X)), "train_data_s": t_data, "train_s": t_train,
@@ -922,6 +926,36 @@ def run_pendulum(args, cs, rank, world, local_rank):
         print(json.dumps(line))
     if dist is not None:
         dist.destroy_process_group()
+
+
+def _solution_files_rate(cs, runner, sample=32):
+    """Text of every instance's solution file (the reference's format) for the
+    solved batch: formatted on the GPU, and by the host writer for a sample of
+    instances, in bytes per second (untimed by the step)."""
+    t0 = time.perf_counter()
+    nbytes = 0
+    for g in runner.groups:
+        text, off = g["bt"].solution_text()
+        nbytes += len(text)
+    dt_dev = time.perf_counter() - t0
+    g = runner.groups[0]
+    sols = g["bt"].solution()[:sample]
+    cp = g["bt"].cp
+    t0 = time.perf_counter()
+    hb = 0
+    for s in sols:
+        parts = ["nt:\n{}\nt:\n".format(s["N"]), "".join(cs.io._fmt(v) + " " for v in s["t"]),
+                 "\nny:\n{}\ny:\n".format(cp.ny)]
+        parts += ["".join(cs.io._fmt(v) + " " for v in row) + "\n" for row in s["y"]]
+        parts.append("nz:\n{}\nz:\n".format(cp.nz))
+        parts += ["".join(cs.io._fmt(v) + " " for v in row) + "\n" for row in s["z"]]
+        parts.append("np:\n{}\np:\n".format(cp.np))
+        parts.append("".join(cs.io._fmt(v) + " " for v in s["p"]))
+        hb += len("".join(parts))
+    dt_host = time.perf_counter() - t0
+    return {"bytes": nbytes, "files": sum(g["bt"].B for g in runner.groups), "device_s": dt_dev,
+            "device_MB_per_s": nbytes / dt_dev / 1e6, "host_MB_per_s": hb / dt_host / 1e6,
+            "host_sample": "%d files of the m=%d group, Python writer (the reference's formatting)" % (len(sols), g["m"])}
 
 
 def main():

@@ -109,6 +109,8 @@ SIGNATURES = {
                                              ctypes.c_void_p]),
     "cs_batch_warm_start": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_int]),
     "cs_batch_set_spares": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]),
+    "cs_format_solutions": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_longlong, ctypes.c_void_p]),
+    "cs_format_double": (ctypes.c_int, [ctypes.c_double, ctypes.c_char_p]),
     "cs_device_alloc": (ctypes.c_void_p, [ctypes.c_size_t]),
     "cs_device_free": (None, [ctypes.c_void_p]),
     "cs_copy": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int]),

@@ -51,8 +51,9 @@ def _stale(target, deps):
 def build_library(force=False, verbose=False):
     hdr = _kernels_header()
     sources = [os.path.join(CSRC, "cs_runtime.cu"), os.path.join(CSRC, "cs_babd.cu"), os.path.join(CSRC, "cs_mlp.cu"),
-               os.path.join(CSRC, "cs_tc.cu")]
+               os.path.join(CSRC, "cs_tc.cu"), os.path.join(CSRC, "cs_text.cu")]
     deps = sources + [os.path.join(CSRC, "cs_kernels.cuh"), os.path.join(CSRC, "cs_umma.cuh"),
+                      os.path.join(CSRC, "cs_dtoa.h"), os.path.join(CSRC, "cs_text.h"),
                       os.path.join(ROOT, "include", "cs_gb300.h"), hdr]
     if not force and not _stale(LIB, deps):
         return LIB

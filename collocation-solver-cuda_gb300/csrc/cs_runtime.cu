@@ -27,6 +27,7 @@
 #include <unistd.h>
 #include <vector>
 
+#include "cs_text.h"
 #include "cs_gb300.h"
 #include "cs_kernels_src.h"  // generated: const char* cs_kernels_source
 
@@ -1629,6 +1630,30 @@ extern "C" int cs_batch_sizes(cs_batch* bt, int* N_out, long long* total_out) {
 static int compute_znodes(cs_batch* bt) {
   CsBatchDev v = devview(bt);
   return run_slots(bt, bt->M->f_znodes, v);
+}
+
+extern "C" int cs_format_solutions(cs_batch* bt, char* out, long long cap, long long* offsets) {
+  if (!bt || !bt->have_guess) return set_err(CS_ERR_STATE, "cs_format_solutions: nothing solved");
+  if (!offsets) return set_err(CS_ERR_INVALID, "cs_format_solutions: null offsets");
+  cs_module* M = bt->M;
+  // z at the nodes, as cs_get_solution gives it
+  if (M->nz > 0) CS_TRY(compute_znodes(bt));
+  const int s = bt->cur;
+  CsTextArgs a;
+  a.t = (const double*)bt->t[s].p;
+  a.y = (const double*)bt->y[s].p;
+  a.z = (const double*)bt->znode[s].p;
+  a.p = (const double*)bt->dp.p;
+  a.T = bt->T;
+  a.B = bt->B;
+  a.ny = M->ny;
+  a.nz = M->nz;
+  a.np = M->np;
+  a.dN = (const int*)bt->dN.p;
+  a.doff = (const int*)bt->doff.p;
+  a.stream = bt->stream;
+  bt->launches += 3;
+  return cs_text_files(a, out, cap, offsets);
 }
 
 extern "C" int cs_get_solution(cs_batch* bt, double* t, double* y, double* z, double* p, cs_stats* stats) {

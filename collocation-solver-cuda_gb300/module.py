@@ -306,6 +306,17 @@ class Batch:
                             singular=int(s.singular), fail_reason=int(s.fail_reason)))
         return out
 
+    def solution_text(self):
+        """Every instance's solution file (the reference's text format, the
+        numbers as "{}".format prints them), formatted on the GPU: the text of
+        all files and their byte offsets (file b is text[off[b]:off[b + 1]])."""
+        off = np.zeros(self.B + 1, dtype=np.int64)
+        _lib.check(self._lib.cs_format_solutions(self.handle, None, 0, off.ctypes.data), "cs_format_solutions")
+        buf = np.empty(max(int(off[-1]), 1), dtype=np.uint8)
+        _lib.check(self._lib.cs_format_solutions(self.handle, buf.ctypes.data, int(off[-1]), off.ctypes.data),
+                   "cs_format_solutions")
+        return buf[:int(off[-1])].tobytes(), off
+
     def state(self):
         cp = self.cp
         N, T = self.sizes()

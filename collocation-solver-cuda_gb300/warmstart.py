@@ -169,15 +169,26 @@ def write_guess_file(family, mlp, instance, path, n_nodes=None):
     return bvpdae_write_data(path, len(t), family.ny, family.nz, family.np, t, y, z, p)
 
 
-def write_solution_files(batch, path_fmt):
+def write_solution_files(batch, path_fmt, device=True):
     """Every instance's solution of a solved Batch as a BVPDAEReadWriteData
-    file: path_fmt % b names instance b's file.  Returns the list of writer
-    statuses."""
-    from .io import bvpdae_write_data
-    cp = batch.cp
+    file: path_fmt % b names instance b's file.  device: the text is
+    formatted on the GPU (Batch.solution_text, the same bytes), else by the
+    host writer value by value.  Returns the list of writer statuses (0 ok,
+    1 failure, as the reference's writer)."""
+    if not device:
+        from .io import bvpdae_write_data
+        cp = batch.cp
+        return [bvpdae_write_data(path_fmt % b, s["N"], cp.ny, cp.nz, cp.np, s["t"], s["y"], s["z"], s["p"])
+                for b, s in enumerate(batch.solution())]
+    text, off = batch.solution_text()
     out = []
-    for b, s in enumerate(batch.solution()):
-        out.append(bvpdae_write_data(path_fmt % b, s["N"], cp.ny, cp.nz, cp.np, s["t"], s["y"], s["z"], s["p"]))
+    for b in range(batch.B):
+        try:
+            with open(path_fmt % b, "wb") as f:
+                f.write(text[off[b]:off[b + 1]])
+            out.append(0)
+        except OSError:
+            out.append(1)
     return out
 
 

@@ -265,6 +265,20 @@ int cs_babd_solve_noalloc(int ny, int np, int n, const double* A, const double* 
 int cs_tc_update(int precision, int M, int N, int K, const float* A, int lda, const float* B, int ldb, float* C,
                  int ldc, void* stream);
 
+/* The solution file of every instance in the reference's text format
+ * (BVPDAEReadWriteData: labels, then t, y and z rows and p, every number as
+ * Python's "{}".format of the double prints it), formatted on the GPU from
+ * the values cs_get_solution returns.  offsets (B + 1 entries) are always
+ * filled: file b is out[offsets[b] .. offsets[b+1]).  out = NULL only sizes
+ * the files; a cap below offsets[B] fails with CS_ERR_INVALID.
+ * Replaces: the per-value Python writer (BVPDAEReadWriteData.py:337-364)
+ * called once per solution. */
+int cs_format_solutions(cs_batch* bt, char* out, long long cap, long long* offsets);
+
+/* One double as that text ("{}".format / repr: shortest round-trip digits),
+ * host code: out needs 25 bytes; returns the length (-1: out is NULL). */
+int cs_format_double(double v, char* out);
+
 /* Current iterate to host: t, y (nodes), ydot, z~ (slots), z at nodes, p. */
 int cs_get_state(cs_batch* bt, double* t, double* y, double* ydot, double* zt, double* z_nodes, double* p);
 
