@@ -309,13 +309,14 @@ class Batch:
     def solution_text(self):
         """Every instance's solution file (the reference's text format, the
         numbers as "{}".format prints them), formatted on the GPU: the text of
-        all files and their byte offsets (file b is text[off[b]:off[b + 1]])."""
+        all files (a memoryview of bytes, not copied again) and their byte
+        offsets (file b is text[off[b]:off[b + 1]])."""
         off = np.zeros(self.B + 1, dtype=np.int64)
         _lib.check(self._lib.cs_format_solutions(self.handle, None, 0, off.ctypes.data), "cs_format_solutions")
         buf = np.empty(max(int(off[-1]), 1), dtype=np.uint8)
         _lib.check(self._lib.cs_format_solutions(self.handle, buf.ctypes.data, int(off[-1]), off.ctypes.data),
                    "cs_format_solutions")
-        return buf[:int(off[-1])].tobytes(), off
+        return memoryview(buf)[:int(off[-1])], off
 
     def state(self):
         cp = self.cp
