@@ -516,7 +516,8 @@ def run_warm(args, cs, rank, world, local_rank, cpu, cfg):
     t0 = time.perf_counter()
     net = ws.Mlp(X.shape[1], Y.shape[1], width=256, depth=4, seed=0)
     net.fit_normalization(X, Y)
-    loss = net.train(X, Y, epochs=args.epochs, batch=1024, lr=1e-3, seed=0)
+    loss = net.train(X, Y, epochs=args.epochs, batch=1024, lr=args.lr, seed=0,
+                     lr_final=args.lr_final if args.lr_final >= 0 else None)
     t_train = time.perf_counter() - t0
     # ---- evaluation batch, resident in HBM
     _log("trained in %.1f s (loss %.3g)" % (t_train, loss))
@@ -657,7 +658,8 @@ def run_warm(args, cs, rank, world, local_rank, cpu, cfg):
                 "warm_start": {"solved": solved, "of": len(held), "fallbacks": n_fb, "phase_s": runner_times,
                                "fallback_rate": n_fb / len(held), "newton_steps_per_solve": float(newton_warm),
                                "train_solutions": int(len(X)), "train_data_s": t_data, "train_s": t_train,
-                               "train_loss": loss, "epochs": args.epochs},
+                               "train_loss": loss, "epochs": args.epochs, "lr": args.lr,
+                               "lr_schedule": ("cosine to %g of lr" % args.lr_final) if args.lr_final >= 0 else "constant"},
                 "autotune": tune}
         print(json.dumps(line))
     if dist is not None:
@@ -972,7 +974,10 @@ def main():
                     help="pendulum: precision of the large-system condensation")
     ap.add_argument("--batch", type=int, default=None, help="instances per step (warm: 8192, plain: 4096)")
     ap.add_argument("--train", type=int, default=65536, help="training solutions (warm)")
-    ap.add_argument("--epochs", type=int, default=150)
+    ap.add_argument("--epochs", type=int, default=600)
+    ap.add_argument("--lr", type=float, default=2e-3, help="warm: Adam learning rate of the MLP")
+    ap.add_argument("--lr-final", type=float, default=0.02,
+                    help="warm: cosine decay of the learning rate to this fraction of it (negative: constant)")
     ap.add_argument("--single-sample", type=int, default=64)
     ap.add_argument("--speculate", type=float, default=0.0,
                     help="warm, without spares: start the plain-guess solves of the instances still iterating on "

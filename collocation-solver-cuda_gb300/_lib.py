@@ -111,6 +111,7 @@ SIGNATURES = {
     "cs_batch_set_spares": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]),
     "cs_format_solutions": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_longlong, ctypes.c_void_p]),
     "cs_format_double": (ctypes.c_int, [ctypes.c_double, ctypes.c_char_p]),
+    "cs_mlp_set_schedule": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_float]),
     "cs_device_alloc": (ctypes.c_void_p, [ctypes.c_size_t]),
     "cs_device_free": (None, [ctypes.c_void_p]),
     "cs_copy": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int]),

@@ -220,6 +220,7 @@ struct cs_mlp {
   float* m2 = nullptr;
   float* norm = nullptr;  // xm, xs, ym, ys
   long long step = 0;
+  float lr_final = -1.f;  // cosine decay of the learning rate to lr_final * lr (< 0: constant)
   cudaStream_t st = nullptr;
   // activations for a batch of up to cap rows
   int cap = 0;
@@ -473,6 +474,10 @@ extern "C" int cs_mlp_train(cs_mlp* M, const float* X, const float* Y, int n, in
   std::mt19937_64 rng(seed);
   const float* nr = M->norm;
   double last = 0.0;
+  // learning rate of step q of this call: constant, or cosine from lr down to
+  // lr_final * lr over the call's steps
+  const long long total = (long long)epochs * (n / batch);
+  long long q = 0;
   for (int ep = 0; ep < epochs && rc == CS_OK; ++ep) {
     std::shuffle(perm.begin(), perm.end(), rng);
     MLP_CUDA(cudaMemcpyAsync(dperm, perm.data(), (size_t)n * sizeof(int), cudaMemcpyHostToDevice, M->st));
@@ -488,7 +493,13 @@ extern "C" int cs_mlp_train(cs_mlp* M, const float* X, const float* Y, int n, in
       M->step += 1;
       const float b1 = 0.9f, b2 = 0.999f;
       const float c1 = 1.f - std::pow(b1, (float)M->step), c2 = 1.f - std::pow(b2, (float)M->step);
-      k_adam<<<grid_for(M->nparam), 256, 0, M->st>>>(M->w, M->g, M->m1, M->m2, M->nparam, lr, b1, b2, 1e-8f, c1, c2);
+      float lq = lr;
+      if (M->lr_final >= 0.f && total > 1) {
+        const double f = M->lr_final + 0.5 * (1.0 - M->lr_final) * (1.0 + std::cos(3.14159265358979323846 * (double)q / (double)(total - 1)));
+        lq = (float)(lr * f);
+      }
+      ++q;
+      k_adam<<<grid_for(M->nparam), 256, 0, M->st>>>(M->w, M->g, M->m1, M->m2, M->nparam, lq, b1, b2, 1e-8f, c1, c2);
       ++nb;
     }
     if (rc == CS_OK && ep == epochs - 1) {
@@ -506,6 +517,12 @@ extern "C" int cs_mlp_train(cs_mlp* M, const float* X, const float* Y, int n, in
   cudaFree(dperm);
   if (final_loss) *final_loss = last;
   return rc;
+}
+
+extern "C" int cs_mlp_set_schedule(cs_mlp* M, float lr_final) {
+  if (!M || lr_final > 1.f) return cs_internal_set_error(CS_ERR_INVALID, "cs_mlp_set_schedule: bad argument");
+  M->lr_final = lr_final;
+  return CS_OK;
 }
 
 extern "C" int cs_mlp_predict_device(cs_mlp* M, const float* dX, int n, float* dY, void* stream) {

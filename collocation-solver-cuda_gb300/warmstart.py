@@ -79,7 +79,11 @@ class Mlp:
                                              _lib.fptr(g)), "cs_mlp_gradient")
         return loss.value, g
 
-    def train(self, X, Y, epochs=200, batch=512, lr=1e-3, seed=0):
+    def train(self, X, Y, epochs=200, batch=512, lr=1e-3, seed=0, lr_final=None):
+        """Adam on mini-batches; lr_final (a fraction of lr): the rate decays
+        along a half cosine to lr_final * lr over the run, else constant."""
+        _lib.check(self._lib.cs_mlp_set_schedule(self.handle, ctypes.c_float(-1.0 if lr_final is None else lr_final)),
+                   "cs_mlp_set_schedule")
         X = np.ascontiguousarray(X, dtype=np.float32)
         Y = np.ascontiguousarray(Y, dtype=np.float32)
         loss = ctypes.c_double()

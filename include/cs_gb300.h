@@ -327,6 +327,10 @@ int cs_mlp_set_params(cs_mlp* mlp, const float* host);
 int cs_mlp_gradient(cs_mlp* mlp, const float* X, const float* Y, int n, double* loss, float* grad);
 int cs_mlp_train(cs_mlp* mlp, const float* X, const float* Y, int n, int epochs, int batch, float lr,
                  unsigned long long seed, double* final_loss);
+/* learning-rate schedule of cs_mlp_train: lr_final >= 0 decays the rate of
+ * every call along a half cosine from lr to lr_final * lr over the call's
+ * steps; lr_final < 0 (the default) keeps it constant */
+int cs_mlp_set_schedule(cs_mlp* mlp, float lr_final);
 int cs_mlp_predict(cs_mlp* mlp, const float* X, int n, float* Y);
 
 /* forward pass on DEVICE arrays (n rows), ordered on `stream` (cudaStream_t

@@ -59,3 +59,22 @@ def test_predict_matches_oracle_and_training_lowers_loss():
     # way in FP32 than in float64: a few entries move by one bf16 step
     assert np.linalg.norm(P - ref) <= 2e-3 * np.linalg.norm(ref)
     assert np.abs(P - ref).max() <= 1e-2 * np.abs(ref).max()
+
+
+def test_cosine_schedule_plumbing():
+    """cs_mlp_set_schedule: a cosine from lr to 1.0 * lr is the constant rate
+    (same bits); a decay to 0 trains to different parameters, with a finite
+    loss no worse than 1.5x the constant rate's on this short run."""
+    cs = pkg()
+    X, Y = _data(2048, 4, 40, seed=2)
+    nets = []
+    for lr_final in (None, 1.0, 0.0):
+        net = cs.warmstart.Mlp(4, 40, width=64, depth=3, seed=5)
+        net.fit_normalization(X, Y)
+        net.train(X, Y, epochs=20, batch=256, lr=2e-3, seed=1, lr_final=lr_final)
+        nets.append(net)
+    np.testing.assert_array_equal(nets[0].params(), nets[1].params())
+    assert not np.array_equal(nets[0].params(), nets[2].params())
+    l0, _ = nets[0].gradient(X, Y)
+    l2, _ = nets[2].gradient(X, Y)
+    assert np.isfinite(l2) and l2 <= 1.5 * l0
