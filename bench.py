@@ -514,7 +514,7 @@ def run_warm(args, cs, rank, world, local_rank, cpu, cfg):
     t_data = time.perf_counter() - t0
     _log("training set: %d solutions in %.1f s; training" % (len(X), t_data))
     t0 = time.perf_counter()
-    net = ws.Mlp(X.shape[1], Y.shape[1], width=256, depth=4, seed=0)
+    net = ws.Mlp(X.shape[1], Y.shape[1], width=args.width, depth=4, seed=0)
     net.fit_normalization(X, Y)
     loss = net.train(X, Y, epochs=args.epochs, batch=1024, lr=args.lr, seed=0,
                      lr_final=args.lr_final if args.lr_final >= 0 else None)
@@ -975,6 +975,7 @@ def main():
     ap.add_argument("--batch", type=int, default=None, help="instances per step (warm: 8192, plain: 4096)")
     ap.add_argument("--train", type=int, default=65536, help="training solutions (warm)")
     ap.add_argument("--epochs", type=int, default=600)
+    ap.add_argument("--width", type=int, default=256, help="warm: hidden width of the MLP (4 layers)")
     ap.add_argument("--lr", type=float, default=2e-3, help="warm: Adam learning rate of the MLP")
     ap.add_argument("--lr-final", type=float, default=0.02,
                     help="warm: cosine decay of the learning rate to this fraction of it (negative: constant)")
@@ -1078,7 +1079,7 @@ def main():
                            "N~U{32..128} intervals, m=4, seed 7 + 100 rank), MLP trained on %d batched-solver "
                            "solutions (seed 1000)" % (args.batch, args.train),
                "batch_per_gpu": args.batch, "tol": 1e-6, "precision": "fp64 solver, bf16/fp32 network",
-               "warm_start": "MLP 4x256 GELU, 64 normalised-time nodes, fallback to the plain guess",
+               "warm_start": "MLP 4x%d GELU, 64 normalised-time nodes, fallback to the plain guess" % args.width,
                "l2": "working set %s GB per step, larger than L2 (129 MB)"}
     elif args.workload == "warm":
         instances = cs.workloads.vdp_batch(args.batch, seed=7 + 100 * rank)
@@ -1087,7 +1088,7 @@ def main():
                            "100 rank), MLP trained on %d batched-solver solutions (seed 1000, N~U{32..256})"
                            % (args.batch, args.train),
                "batch_per_gpu": args.batch, "tol": 1e-6, "precision": "fp64 solver, bf16/fp32 network",
-               "warm_start": "MLP 4x256 GELU, 64 normalised-time nodes, fallback to the plain guess",
+               "warm_start": "MLP 4x%d GELU, 64 normalised-time nodes, fallback to the plain guess" % args.width,
                "l2": "working set %s GB per step, larger than L2 (129 MB)"}
     else:
         cfg = None
