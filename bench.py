@@ -1047,7 +1047,9 @@ def main():
             ms = g["bt"].time_condense(reps=1)
             print("m=%d condense %.3f ms over %d intervals" % (g["m"], ms, g["bt"].sizes()[1] - g["bt"].B))
         W.step_resident()
-        print("profile case ok", W.results())
+        # the solution files of the solved batch, formatted on the device
+        nbytes = sum(len(g["bt"].solution_text()[0]) for g in W.groups)
+        print("profile case ok", W.results(), "solution text %d bytes" % nbytes)
         return
 
     rank = int(os.environ.get("RANK", "0"))
