@@ -298,11 +298,15 @@ class Workload:
         if errs:
             raise errs[0]
 
-    def step_resident(self):
+    def step_resident(self, threads=True):
         def f(g):
             g["bt"].reset()
             g["bt"].solve(self.opts)
-        self._run_groups(f)
+        if threads:
+            self._run_groups(f)
+        else:
+            for g in self.groups:
+                f(g)
 
     def step_e2e(self):
         def f(g):
@@ -1046,7 +1050,10 @@ def main():
             g["bt"].reset()
             ms = g["bt"].time_condense(reps=1)
             print("m=%d condense %.3f ms over %d intervals" % (g["m"], ms, g["bt"].sizes()[1] - g["bt"].B))
-        W.step_resident()
+        # the m-groups one after another on this thread: under ncu, solves
+        # of several groups on several host threads ended the process with
+        # error code 11 (the same run without ncu exits 0)
+        W.step_resident(threads=False)
         # the solution files of the solved batch, formatted on the device
         nbytes = sum(len(g["bt"].solution_text()[0]) for g in W.groups)
         print("profile case ok", W.results(), "solution text %d bytes" % nbytes)
