@@ -78,9 +78,11 @@ typedef struct cs_module_desc {
                                accumulation (an inexact Newton Jacobian: the
                                residual, line search, mesh error and BABD
                                solve stay FP64); 3 / 4: TF32 / BF16 also for
-                               the tree merges' block updates (slower to
-                               converge: see the design notes).  Nonzero
-                               implies the large-system condensation. */
+                               the tree merges' block updates (their rounding
+                               compounds over the tree's levels; cs_opts.refine
+                               sweeps of FP64 iterative refinement correct each
+                               Newton direction).  Nonzero implies the
+                               large-system condensation. */
 } cs_module_desc;
 
 /* Compile (or load from the cache) and load the module on the current device. */
