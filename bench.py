@@ -1032,7 +1032,8 @@ def main():
         X, Y, _ = ws.training_set(fam, solver, _family_batch(cs, args.family, 2048, 1000, train=True))
         net = ws.Mlp(X.shape[1], Y.shape[1], width=256, depth=4, seed=0)
         net.fit_normalization(X, Y)
-        net.train(X, Y, epochs=60, batch=1024, lr=1e-3, seed=0)
+        net.train(X, Y, epochs=args.epochs, batch=1024, lr=args.lr, seed=0,
+                  lr_final=args.lr_final if args.lr_final >= 0 else None)
         runner = ws.WarmRunner(fam, solver, net, _family_batch(cs, args.family, 2048, 7), spares=args.spares >= 0)
         # the m-groups one after another on this thread (profilers serialise
         # kernels anyway, and a single host thread keeps the capture simple)
