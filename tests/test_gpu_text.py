@@ -76,3 +76,9 @@ def test_device_files_equal_host_writer_on_bit_patterns():
     bt = cs.Batch(solver.cp(3), len(insts))
     bt.set_guess_packed(N, t, y, z, p, th)
     _check(cs, bt)
+    # a buffer one byte short is refused (the offsets are still filled)
+    off = np.zeros(bt.B + 1, dtype=np.int64)
+    assert bt._lib.cs_format_solutions(bt.handle, None, 0, off.ctypes.data) == 0
+    buf = np.zeros(int(off[-1]), dtype=np.uint8)
+    rc = bt._lib.cs_format_solutions(bt.handle, buf.ctypes.data, int(off[-1]) - 1, off.ctypes.data)
+    assert rc == 1 and "too small" in cs._lib.last_error()
