@@ -508,8 +508,8 @@ def run_warm(args, cs, rank, world, local_rank, cpu, cfg):
     ws = cs.warmstart
     fp64_peak, peak_clock = fp64_peak_with_clock(cs, _gpu_index(local_rank))
     fam = _family(cs, args.family)
-    solver = ws.BatchSolver(fam, cs.default_opts(fam.problem, max_nodes=20000, babd_path=args.babd_path),
-                            layout=args.layout)
+    solver = ws.BatchSolver(fam, cs.default_opts(fam.problem, max_nodes=20000, babd_path=args.babd_path,
+                                                  ls_grow=args.ls_grow), layout=args.layout)
     # ---- set-up: training data from the batched solver, then training
     t0 = time.perf_counter()
     train = _family_batch(cs, args.family, args.train, 1000 + 100 * rank, train=True)
@@ -992,6 +992,9 @@ def main():
                          "most this fraction of an m-group is in Newton, e.g. 0.005 (negative, the default: "
                          "separate fallback solves, 1-2 %% faster on the 8192-instance batch, where the GPU is busy "
                          "to the end of the step; the spares are ~10 %% faster on 2048)")
+    ap.add_argument("--ls-grow", type=int, default=2,
+                    help="line-search trials per super-step after a search that rejected k: ls_grow*k+2 "
+                         "(0: all 20); same results")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--babd-path", type=int, default=0, help="0 automatic, 1 one CTA per instance, 2 per level")
     ap.add_argument("--layout", type=int, default=0,

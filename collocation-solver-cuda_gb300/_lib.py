@@ -31,7 +31,8 @@ class Opts(ctypes.Structure):
                 ("max_nodes", ctypes.c_int), ("min_nodes", ctypes.c_int), ("max_linesearch", ctypes.c_int),
                 ("alpha0", ctypes.c_double), ("alpha_m", ctypes.c_double), ("beta", ctypes.c_double),
                 ("check_every", ctypes.c_int), ("babd_path", ctypes.c_int), ("residual_type", ctypes.c_int),
-                ("scale_by_time", ctypes.c_int), ("residual2", ctypes.c_int), ("refine", ctypes.c_int)]
+                ("scale_by_time", ctypes.c_int), ("residual2", ctypes.c_int), ("refine", ctypes.c_int),
+                ("ls_grow", ctypes.c_int)]
 
 
 class Stats(ctypes.Structure):

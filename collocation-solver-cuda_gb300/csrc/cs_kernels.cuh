@@ -84,6 +84,7 @@ struct CsInst {
 struct CsConsts {
   double tol, alpha_m, beta;
   int max_iter, max_mesh, max_nodes, min_nodes, max_ls;
+  int ls_grow;  // trials of a new line search after one that rejected some (cs_opts.ls_grow)
 };
 
 struct CsBatch {
@@ -425,7 +426,12 @@ extern "C" __global__ void k_decide(CsBatch bt, CsConsts c) {
     }
     // a new direction follows: an instance whose last line search rejected
     // trials evaluates several at once from the start
-    if (s.need_jac) s.ntrial = (s.ls_prev > 0) ? min(CS_LSW, c.max_ls) : 1;
+    // (ls_grow > 0: as many as ls_grow times the trials the last search
+    // rejected, plus two; the rest, if needed, in the next super-step)
+    if (s.need_jac) {
+      const int many = min(CS_LSW, c.max_ls);
+      s.ntrial = (s.ls_prev > 0) ? (c.ls_grow > 0 ? min(many, c.ls_grow * s.ls_prev + 2) : many) : 1;
+    }
     if (s.status == ST_FRESH || s.status == ST_LS || s.need_jac) atomicAdd(&bt.counters[0], 1ull);
     if (s.need_jac) {
       atomicAdd(&bt.counters[1], (unsigned long long)(bt.N[b] - 1));

@@ -100,6 +100,7 @@ static_assert(sizeof(CsInst) == 112, "CsInst layout");
 struct CsConsts {
   double tol, alpha_m, beta;
   int max_iter, max_mesh, max_nodes, min_nodes, max_ls;
+  int ls_grow;
 };
 
 // Must match struct CsBatch in cs_kernels.cuh.
@@ -712,6 +713,7 @@ extern "C" void cs_opts_default(cs_opts* o) {
   o->scale_by_time = 1;
   o->residual2 = 0;
   o->refine = 2;
+  o->ls_grow = 2;
 }
 
 
@@ -1109,6 +1111,7 @@ static CsConsts consts_of(const cs_opts& o) {
   c.max_nodes = o.max_nodes;
   c.min_nodes = o.min_nodes;
   c.max_ls = o.max_linesearch;
+  c.ls_grow = o.ls_grow;
   return c;
 }
 

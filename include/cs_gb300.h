@@ -115,6 +115,11 @@ typedef struct cs_opts {
                             residual of the condensed system in FP64, a correction from
                             the same tree); default 2, 0 off.  No reference counterpart
                             (the reference solves in FP64 only) */
+  int ls_grow;           /* speculative line search: after a search that rejected k trials,
+                            the next one evaluates min(20, ls_grow * k + 2) trials in its
+                            first super-step (the rest, if needed, in the next); default 2,
+                            0: all 20.  The trials are taken in the reference's order
+                            (CS:155-174), so results and counts do not depend on it */
 } cs_opts;
 
 void cs_opts_default(cs_opts* o);

@@ -471,3 +471,30 @@ def test_progress_hook_sees_every_check(cs):
     for a, b in zip(hooked, bt2.solution()):
         assert (a["success"], a["newton_steps"], a["N"]) == (b["success"], b["newton_steps"], b["N"])
         np.testing.assert_array_equal(a["y"], b["y"])
+
+
+def test_line_search_trial_count_changes_no_result(cs):
+    """cs_opts.ls_grow only splits a line search's trials over super-steps
+    (taken in the reference's order): a batch with failing and line-searching
+    instances solves to the same bits and counts with 1, 2 and all 20 trials
+    after a search that rejected some."""
+    pr = load_problem("vdp_family")
+    cp = cs.CompiledProblem(pr, 4)
+    insts = cs.workloads.vdp_batch(64, seed=31, n_range=(32, 400), m_choices=(4,))
+    fam = cs.warmstart.vdp_family()
+    N, t, y, z, p, th = cs.warmstart.pack_family(fam, insts)
+    bt = cs.Batch(cp, len(insts))
+    bt.set_guess_packed(N, t, y, z, p, th)
+    runs = []
+    for grow in (0, 1, 2):
+        bt.reset()
+        bt.profile_reset(timing=False)
+        bt.solve(cs.default_opts(pr, max_nodes=20000, ls_grow=grow))
+        runs.append((bt.solution(), bt.profile()["super_steps"]))
+    base, _ = runs[0]
+    assert sum(s["residual_evals"] > 2 * s["newton_steps"] + 2 for s in base) > 0  # some searches rejected trials
+    for sols, _ in runs[1:]:
+        for a, b in zip(sols, base):
+            assert (a["status"], a["newton_steps"], a["residual_evals"], a["N"]) == \
+                   (b["status"], b["newton_steps"], b["residual_evals"], b["N"])
+            np.testing.assert_array_equal(a["y"], b["y"])
