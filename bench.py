@@ -535,8 +535,8 @@ def run_warm(args, cs, rank, world, local_rank, cpu, cfg):
     cfg["l2"] = cfg["l2"] % ("%.1f" % ws_gb)
     for _ in range(args.warmup):
         runner.run(warm=True, speculate=args.speculate, spare_at=spare_at)
-    for g in runner.groups:
-        g["bt"].profile_reset(timing=False)
+    for bt in [g["bt"] for g in runner.groups] + solver.batches():
+        bt.profile_reset(timing=False)
     _log("warm-up done; timed warm-started steps")
     _barrier(dist)
     with ClockSampler(_gpu_index(local_rank)) as clk:
@@ -546,7 +546,10 @@ def run_warm(args, cs, rank, world, local_rank, cpu, cfg):
         dt = time.perf_counter() - t0
     dt = _max_over_ranks(dist, dt)
     runner_times = dict(runner.times)
-    launches = sum(g["bt"].profile()["launches"] for g in runner.groups) + args.steps * 7
+    # the m-group batches, the fallback solves' batches, and the network's
+    # 7 launches per step
+    launches = (sum(g["bt"].profile()["launches"] for g in runner.groups)
+                + sum(bt.profile()["launches"] for bt in solver.batches()) + args.steps * 7)
     value = _sum_over_ranks(dist, args.steps * solved) / dt
     newton_warm = np.mean([s["newton_steps"] for s in sols])
     # ---- plain batched solve of the same instances

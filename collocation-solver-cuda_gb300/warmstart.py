@@ -233,6 +233,12 @@ class BatchSolver:
                 return free.pop()
         return Batch(self.cp(m), n)
 
+    def batches(self):
+        """The idle batches kept for reuse (their profile counters count the
+        launches of the solves they ran)."""
+        with self._lock:
+            return [bt for v in self._idle.values() for bt in v]
+
     def _give(self, m, n, bt):
         with self._lock:
             self._idle.setdefault((m, n), []).append(bt)
