@@ -547,9 +547,9 @@ def run_warm(args, cs, rank, world, local_rank, cpu, cfg):
     dt = _max_over_ranks(dist, dt)
     runner_times = dict(runner.times)
     # the m-group batches, the fallback solves' batches, and the network's
-    # 7 launches per step
+    # 6 launches per step (input gather, 4 GEMMs, output scaling)
     launches = (sum(g["bt"].profile()["launches"] for g in runner.groups)
-                + sum(bt.profile()["launches"] for bt in solver.batches()) + args.steps * 7)
+                + sum(bt.profile()["launches"] for bt in solver.batches()) + args.steps * 6)
     value = _sum_over_ranks(dist, args.steps * solved) / dt
     newton_warm = np.mean([s["newton_steps"] for s in sols])
     # ---- plain batched solve of the same instances
